@@ -1,0 +1,140 @@
+/*
+ * hpsi_gb300.h — C ABI of the GB300 (sm_103a) H|psi> library, libhpsi_gb300.so.
+ *
+ * It replaces the reference's C++23-module operator API of src/H_psi:
+ *
+ *   reference                                            here
+ *   ---------------------------------------------------  ----------------------------------
+ *   Hamiltonian::finalize (src/H_psi/hamiltonian.cpp:267-392;
+ *     tables, lambda, FFT plan)                           hpsi_ctx_create
+ *   Hamiltonian::at_k / Callable::set_ikpt
+ *     (src/H_psi/hamiltonian.cppm:186-188,205;
+ *      src/H_psi/hamiltonian_callable.cpp:62-85)          hpsi_set_kpoint
+ *   Callable::operator()(psi, hpsi)
+ *     (src/H_psi/hamiltonian.cppm:177-178;
+ *      src/H_psi/hamiltonian_callable.cpp:94-356)         hpsi_apply (nb = 1)
+ *   Callable::operator()(n_bands, psi, hpsi)
+ *     (src/H_psi/hamiltonian.cppm:180-182; declared there,
+ *      never defined in the reference)                    hpsi_apply (nb > 1)
+ *   Callable::dim() (src/H_psi/hamiltonian.cppm:184)      hpsi_dim
+ *   Gradient::Callable::operator()(psi, GradHPsi)
+ *     (src/H_psi/hamiltonian.cppm:228-229;
+ *      src/H_psi/hamiltonian_gradient.cpp:116-294)        hpsi_grad_apply
+ *   (no counterpart; band-pair <psi_m|dH/dk_a|psi_n>)     hpsi_velocity_matrix
+ *   C++ exceptions (runtime_error, out_of_range,
+ *     domain_error)                                       negative status + hpsi_last_error
+ *
+ * Semantics kept from the reference:
+ *   - outputs ACCUMULATE (hpsi += H psi); the caller zeroes them first
+ *     (src/H_psi/hamiltonian_callable.cpp:90-92);
+ *   - psi/hpsi of one band are npw contiguous complex<double> values (re, im)
+ *     in the G-vector order of the k-point (the GKK/WG order); a block of nb
+ *     bands is band-major: psi[b*npw + g];
+ *   - a NULL gradient output skips that Cartesian direction (the reference's
+ *     empty GradHPsi span, src/H_psi/hamiltonian.cppm:53-70);
+ *   - projectors with |lambda| < 1e-15 are skipped
+ *     (src/H_psi/hamiltonian_callable.cpp:226-227);
+ *   - q > q_max is an error, like BetaqTables::interpolate's domain_error
+ *     (src/pseudo/ncpp_advance.cppm:656-661).
+ *
+ * Threading: one context per host thread; calls on one context are serialised
+ * by the caller.  All device work of a call is queued on `stream` (NULL = the
+ * legacy default stream); with HPSI_SYNC the call returns after it finished.
+ */
+#ifndef HPSI_GB300_H
+#define HPSI_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HPSI_ABI_VERSION 1
+
+/* status codes */
+#define HPSI_OK            0
+#define HPSI_ERR_BAD_ARG  -1   /* std::invalid_argument / out_of_range in the reference */
+#define HPSI_ERR_OOM      -2   /* device allocation failed */
+#define HPSI_ERR_RANGE    -3   /* q > q_max, or a G index outside the FFT grid (domain_error) */
+#define HPSI_ERR_TIMEOUT  -4   /* a bounded device-side wait gave up */
+#define HPSI_ERR_CUDA     -5   /* CUDA runtime error */
+#define HPSI_ERR_STATE    -6   /* k-point not set, missing table (runtime_error) */
+
+/* flags: precision in bits 0-3 */
+#define HPSI_PREC_FP64      0  /* complex128 FFTs, FP64 projector sums: parity path */
+#define HPSI_PREC_FP32      1  /* complex64 FFTs, FP32 projector GEMMs, FP64 phases */
+#define HPSI_PREC_TC        2  /* complex64 FFTs, tcgen05 tensor-core split-BF16 projector GEMMs */
+#define HPSI_PREC_MASK    0xF
+#define HPSI_DEVICE_PTRS  0x10 /* psi/outputs are device pointers (else host memory) */
+#define HPSI_SYNC         0x20 /* synchronise `stream` before returning */
+
+/* One pseudopotential species after the per-l diagonalisation of D
+ * (src/pseudo/ncpp_advance.cppm:65-153): projector i has angular momentum
+ * proj_l[i], KB strength lambda[i] (Ha) and a radial table on q_j = j*dq. */
+typedef struct hpsi_species {
+    int n_proj;
+    const int* proj_l;        /* [n_proj] */
+    const double* lambda;     /* [n_proj], Ha */
+    int nq;                   /* table length; interpolation needs floor(q/dq)+2 < nq */
+    double dq;                /* bohr^-1 */
+    double q_max;             /* interpolation domain; q > q_max -> HPSI_ERR_RANGE */
+    const double* beta_q;     /* [n_proj][nq] raw beta(q_j), without 1/sqrt(omega) */
+    const double* dbeta_q;    /* [n_proj][nq] raw dbeta/dq(q_j); NULL: no gradient */
+} hpsi_species;
+
+typedef struct hpsi_system {
+    int n1, n2, n3;           /* FFT grid */
+    double lattice[9];        /* row n = lattice vector a_n, bohr */
+    double omega;             /* cell volume (bohr^3): projector norm 1/sqrt(omega) */
+    const double* v_loc;      /* [n1*n2*n3] Ha, index (i*n2 + j)*n3 + k */
+    int n_species;
+    const hpsi_species* species;
+    int n_atoms;
+    const int* atom_species;  /* [n_atoms] index into species */
+    const double* atom_tau;   /* [n_atoms][3] fractional coordinates */
+} hpsi_system;
+
+/* G-sphere of one k-point: what GKK::loadKPoint provides (src/io/GKK.cppm:60-72). */
+typedef struct hpsi_kpoint {
+    int npw;
+    double k_frac[3];         /* k in reciprocal-lattice coordinates */
+    const int* g_idx;         /* [npw][3] integer G, centred convention */
+    const double* kvec;       /* [npw][3] K = k+G, Cartesian bohr^-1 */
+    const double* kinetic;    /* [npw] |k+G|^2/2, Ha, as provided (not recomputed) */
+} hpsi_kpoint;
+
+typedef struct hpsi_ctx hpsi_ctx;
+
+int hpsi_abi_version(void);
+
+/* Build a context on the current CUDA device: uploads V_loc, tables, atoms. */
+int hpsi_ctx_create(const hpsi_system* sys, hpsi_ctx** out);
+int hpsi_ctx_destroy(hpsi_ctx* ctx);
+
+/* Bind G-sphere data to slot `kid` (0 <= kid < 4096): derives q, theta, phi,
+ * Y_lm, beta(q), structure factors and the projector matrices on the device.
+ * Rebinding a slot replaces it. */
+int hpsi_set_kpoint(hpsi_ctx* ctx, int kid, const hpsi_kpoint* kp);
+
+/* Number of plane waves of slot kid (Callable::dim), or a negative status. */
+int hpsi_dim(const hpsi_ctx* ctx, int kid);
+
+/* hpsi[b] += H psi[b] for nb bands (kinetic + local + nonlocal). */
+int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
+               int flags, void* stream);
+
+/* d{x,y,z}[b] += dH/dk_{x,y,z} psi[b]; NULL outputs are skipped. */
+int hpsi_grad_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi,
+                    double* dx, double* dy, double* dz, int flags, void* stream);
+
+/* m[a][m][n] = <psi_m| dH/dk_a |psi_n>, a = x,y,z, complex, overwritten (not accumulated).
+ * Output layout [3][nb][nb] complex<double>; psi as in hpsi_apply. */
+int hpsi_velocity_matrix(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* m,
+                         int flags, void* stream);
+
+/* Message of the last failed call on ctx (never NULL). */
+const char* hpsi_last_error(const hpsi_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

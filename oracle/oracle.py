@@ -1,0 +1,139 @@
+"""ctypes wrapper of oracle/_build/libhpsi_oracle.so — TEST INFRASTRUCTURE.
+
+The CPU restatement of the reference's H|psi> path (oracle/hpsi_oracle.c).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use it,
+as the checker or as the timed CPU baseline.  The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from effmass_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhpsi_oracle.so")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+
+_lib = None
+
+
+def build(quiet: bool = True):
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+
+
+def build_ref(quiet: bool = True) -> bool:
+    """Build the reference driver if its generated sources can be had here."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref"],
+                       stdout=subprocess.DEVNULL if quiet else None,
+                       stderr=subprocess.DEVNULL if quiet else None)
+    return r.returncode == 0 and os.path.exists(REF_DRIVER)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+        sysp, kpp = C.POINTER(abi.HpsiSystem), C.POINTER(abi.HpsiKpoint)
+        L.oracle_hpsi.argtypes = [sysp, kpp, C.c_int, dp, dp, C.c_int]
+        L.oracle_grad.argtypes = [sysp, kpp, C.c_int, dp, dp, dp, dp]
+        L.oracle_velocity.argtypes = [sysp, kpp, C.c_int, dp, dp]
+        L.oracle_ylm.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
+        L.oracle_ylm.restype = None
+        L.oracle_beta_interp.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
+        L.oracle_structure_factor.argtypes = [C.c_int, ip, dp, dp, C.c_int, C.c_int, C.c_int, dp]
+        L.oracle_fft3d.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.oracle_fft3d.restype = None
+        L.oracle_fft1d.argtypes = [dp, C.c_int, C.c_int, C.c_double]
+        L.oracle_spherical.argtypes = [C.c_int, dp, dp, dp, dp]
+        L.oracle_spherical.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError(f"oracle status {abi.STATUS_NAMES.get(rc, rc)}")
+
+
+def hpsi(sysm, kp, psi: np.ndarray, hpsi_out: np.ndarray = None, threads: int = 1) -> np.ndarray:
+    psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1, kp.npw)
+    out = np.zeros_like(psi) if hpsi_out is None else hpsi_out
+    S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
+    _check(lib().oracle_hpsi(S.ref(), K.ref(), psi.shape[0], abi.cptr(psi), abi.cptr(out), threads))
+    return out
+
+
+def grad(sysm, kp, psi: np.ndarray):
+    psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1, kp.npw)
+    out = np.zeros((3,) + psi.shape, dtype=np.complex128)
+    S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
+    _check(lib().oracle_grad(S.ref(), K.ref(), psi.shape[0], abi.cptr(psi), abi.cptr(out[0]),
+                             abi.cptr(out[1]), abi.cptr(out[2])))
+    return out
+
+
+def velocity(sysm, kp, psi: np.ndarray):
+    psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1, kp.npw)
+    nb = psi.shape[0]
+    out = np.zeros((3, nb, nb), dtype=np.complex128)
+    S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
+    _check(lib().oracle_velocity(S.ref(), K.ref(), nb, abi.cptr(psi), abi.cptr(out)))
+    return out
+
+
+def ylm(lmax: int, theta, phi):
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    phi = np.ascontiguousarray(phi, dtype=np.float64)
+    ng = theta.shape[0]
+    nlm = (lmax + 1) ** 2
+    y = np.zeros((nlm, ng))
+    dth = np.zeros((nlm, ng))
+    dph = np.zeros((nlm, ng))
+    lib().oracle_ylm(lmax, ng, abi.cptr(theta), abi.cptr(phi), abi.cptr(y), abi.cptr(dth), abi.cptr(dph))
+    return y, dth, dph
+
+
+def beta_interp(table, dq, q_max, norm, q):
+    t = np.ascontiguousarray(table, dtype=np.float64)
+    out = C.c_double()
+    rc = lib().oracle_beta_interp(abi.cptr(t), t.shape[0], dq, q_max, norm, q, C.byref(out))
+    return rc, out.value
+
+
+def structure_factor(g_idx, k_frac, tau, n):
+    g = np.ascontiguousarray(g_idx, dtype=np.int32).reshape(-1, 3)
+    kf = np.ascontiguousarray(k_frac, dtype=np.float64)
+    t = np.ascontiguousarray(tau, dtype=np.float64)
+    out = np.zeros(g.shape[0], dtype=np.complex128)
+    rc = lib().oracle_structure_factor(g.shape[0], g.ctypes.data_as(C.POINTER(C.c_int)), abi.cptr(kf),
+                                       abi.cptr(t), n[0], n[1], n[2], abi.cptr(out))
+    return rc, out
+
+
+def fft3d(grid: np.ndarray, direction: str) -> np.ndarray:
+    g = np.ascontiguousarray(grid, dtype=np.complex128).copy()
+    n1, n2, n3 = g.shape
+    lib().oracle_fft3d(abi.cptr(g), n1, n2, n3, +1 if direction == "G2R" else -1)
+    return g
+
+
+def fft1d(x: np.ndarray, sign: int, fct: float) -> np.ndarray:
+    c = np.ascontiguousarray(x, dtype=np.complex128).copy()
+    _check(lib().oracle_fft1d(abi.cptr(c), c.shape[0], sign, fct))
+    return c
+
+
+def spherical(kvec):
+    K = np.ascontiguousarray(kvec, dtype=np.float64)
+    ng = K.shape[0]
+    q, th, ph = np.zeros(ng), np.zeros(ng), np.zeros(ng)
+    lib().oracle_spherical(ng, abi.cptr(K), abi.cptr(q), abi.cptr(th), abi.cptr(ph))
+    return q, th, ph
