@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""H|psi> band-applications per second on GB300.
+
+Workload (one "step"): H|psi> = (T + V_loc + V_NL)|psi> on a block of 128
+bands of the 64-atom simple-cubic diamond supercell (a = 20.52 bohr,
+Ecut 20 Ha -> 37,073 plane waves at Gamma, FFT grid 72^3, s/p/d x 2
+Kleinman-Bylander projectors per atom -> 1,152 projectors), synthetic
+seeded data of those shapes.  One band-application = H applied to one band.
+
+  value  — device-resident inputs (psi, hpsi in HBM), CUDA-event timed.
+  e2e    — the same call through the public API with pinned host buffers:
+           H2D of psi and hpsi, compute, D2H of hpsi inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--prec fp32|fp64|tc] [--impl gb300|reference]
+
+With --gpus N > 1 (launched under torchrun) every rank runs an independent
+replica of the workload (no collective on the data path); value is the sum.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--prec", default="fp32", choices=["fp32", "fp64", "tc"])
+    ap.add_argument("--system", default="sc64")
+    ap.add_argument("--nb", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(name, nb):
+    from effmass_gb300 import system as S
+    sysm = S.make_system(name)
+    kp = S.g_sphere(sysm.lattice, S.default_kpoint(name), sysm.ecut)
+    psi = S.make_bands(kp, nb, seed=11)
+    return sysm, kp, psi
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def nxs_of(sysm, kp):
+    import numpy as np
+    return int(len(np.unique(np.mod(kp.g_idx[:, 0], sysm.n1))))
+
+
+def run_gb300(args, rank, world, local):
+    import numpy as np
+    import torch
+    from effmass_gb300.hamiltonian import Hamiltonian
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sysm, kp, psi = workload(args.system, args.nb)
+    nb, npw, P = args.nb, kp.npw, sysm.n_proj_total
+    H = Hamiltonian(sysm)
+    H.set_kpoint(0, kp)
+    psi_d = torch.from_numpy(psi).cuda()
+    hpsi_d = torch.zeros_like(psi_d)
+    stream = torch.cuda.current_stream()
+
+    def step(prec):
+        H.apply(0, nb, psi_d, hpsi_d, prec)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # set-up call (builds the projector matrices of this precision once)
+    step(args.prec)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        step(args.prec)
+    barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(args.prec)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nb / (ms * 1e-3)
+
+    # per-phase CUDA-event profile over the same number of steps
+    H.profile(True)
+    for _ in range(args.steps):
+        step(args.prec)
+    prof = H.profile_read()
+    H.profile(False)
+    launches = sum(n for _, n in prof.values())
+    gpu_launches = launches  # our kernels in `steps` profiled steps == the timed region's count
+
+    # accuracy of this path against the FP64 GPU path on the same bands
+    nchk = min(nb, 16)
+    h64 = torch.zeros((nchk, npw), dtype=torch.complex128, device="cuda")
+    hmx = torch.zeros_like(h64)
+    H.apply(0, nchk, psi_d[:nchk].contiguous(), h64, "fp64")
+    H.apply(0, nchk, psi_d[:nchk].contiguous(), hmx, args.prec)
+    err = float(torch.linalg.norm(hmx - h64) / torch.linalg.norm(h64))
+    # band energies <psi|H|psi> (FP64 sums) of the mixed path vs FP64
+    e_mx = torch.einsum("bg,bg->b", psi_d[:nchk].conj(), hmx).real
+    e_64 = torch.einsum("bg,bg->b", psi_d[:nchk].conj(), h64).real
+    de = float((e_mx - e_64).abs().max())
+
+    fp64 = None
+    if not args.no_fp64 and args.prec != "fp64":
+        step("fp64")
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 2
+        f0.record(stream)
+        for _ in range(reps):
+            step("fp64")
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fp64 = nb / (f0.elapsed_time(f1) / reps * 1e-3)
+
+    # end to end through the public API with pinned host buffers
+    psi_h = torch.from_numpy(psi).pin_memory()
+    hpsi_h = torch.zeros_like(psi_h).pin_memory()
+    psi_np, hpsi_np = psi_h.numpy(), hpsi_h.numpy()
+    for _ in range(max(1, args.warmup)):
+        H.apply(0, nb, psi_np, hpsi_np, args.prec)
+    dstream = torch.cuda.default_stream()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    g0.record(dstream)
+    for _ in range(args.steps):
+        H.apply(0, nb, psi_np, hpsi_np, args.prec)
+    g1.record(dstream)
+    torch.cuda.synchronize()
+    e2e_ms = g0.elapsed_time(g1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": world * nb / (e2e_ms * 1e-3), "unit": "band-apps/s",
+           "h2d_bytes_per_step": 2 * psi.nbytes, "d2h_bytes_per_step": psi.nbytes}
+
+    # roofline of the dominant phase
+    hbm, bf16, src = peaks()
+    csz = 16 if args.prec == "fp64" else 8
+    nxs = nxs_of(sysm, kp)
+    plane = nxs * sysm.n2 * sysm.n3 * csz
+    steps = args.steps
+    N = sysm.n1 * sysm.n2 * sysm.n3
+    alg = {
+        # bytes the pass must move per step (band block) — see DESIGN.md, "Roofline units"
+        "g2r_planes": ("hbm", steps * nb * (npw * 16 + plane)),
+        "x_pass": ("hbm", steps * (nb * 2 * plane + N * csz // 2)),
+        "r2g_planes": ("hbm", steps * nb * (plane + 3 * npw * 16 + npw * 8)),
+        # algorithmic flops: 8 real flops per complex multiply-add
+        "proj_gemm": ("tensor", steps * 8.0 * P * npw * nb),
+        "expand_gemm": ("tensor", steps * 8.0 * P * npw * nb),
+    }
+    dom = max((k for k in alg), key=lambda k: prof[k][0])
+    bound, work = alg[dom]
+    tms = prof[dom][0]
+    if bound == "hbm":
+        ach = work / (tms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "peak_source": src}
+    else:
+        ach = work / (tms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": ach / bf16, "peak_source": src + " dense bf16 tensor peak"}
+    roof["traffic"] = None
+    phases = {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps} for k, v in prof.items() if v[1]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import cpu_baseline
+        cpu = cpu_baseline.run(sysm, kp, psi[:16], bands_per_worker=2)
+        cpu = {"value": cpu["value"], "unit": "band-apps/s", "cores": cpu["cores"], "kind": cpu["kind"],
+               "sample": cpu["sample"]}
+
+    out = {
+        "metric": "H|psi> band-applications/s (mixed precision, rel. err <= 1e-6 vs FP64)",
+        "value": value, "unit": "band-apps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "c64/f32", "fp64": "c128/f64", "tc": "c64/f32 + bf16x3 tensor"}[args.prec],
+        "precision_path": args.prec,
+        "data": "synthetic (seeded psi, V_loc, KB projectors of the named shapes)",
+        "config": {"workload": f"{args.system}: 64-atom SC diamond, 72^3 grid, Ecut 20 Ha, Gamma",
+                   "npw": npw, "fft_grid": [sysm.n1, sysm.n2, sysm.n3], "bands_per_step": nb, "projectors": P,
+                   "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "inputs larger than L2 (projector matrix %d MB, psi %d MB)" % (P * npw * csz >> 20,
+                                                                                       psi.nbytes >> 20)},
+        "rel_err_vs_fp64": err, "band_energy_max_abs_diff_Ha": de,
+        "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
+        "e2e": e2e, "roofline": roof, "phases": phases, "gpu_launches": gpu_launches,
+        "cpu_baseline": cpu, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    H.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return
+    from oracle import cpu_baseline
+    sysm, kp, psi = workload(args.system, 16)
+    workers = os.cpu_count() or 1
+    vals, secs = [], []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        r = cpu_baseline.run(sysm, kp, psi, bands_per_worker=1, workers=workers)
+        if i >= args.warmup:
+            vals.append(r["value"])
+            secs.append(time.perf_counter() - t0)
+    v = statistics.mean(vals)
+    out = {"metric": "H|psi> band-applications/s (mixed precision, rel. err <= 1e-6 vs FP64)", "impl": "reference",
+           "value": v, "unit": "band-apps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * statistics.mean(secs), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "c128/f64", "data": "synthetic",
+           "config": {"workload": f"{args.system}: 64-atom SC diamond, 72^3 grid, Ecut 20 Ha, Gamma", "npw": kp.npw,
+                      "fft_grid": [sysm.n1, sysm.n2, sysm.n3], "projectors": sysm.n_proj_total},
+           "cpu_baseline": {"value": v, "unit": "band-apps/s", "cores": workers, "kind": r["kind"],
+                            "sample": r["sample"]},
+           "e2e": {"value": v, "unit": "band-apps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,67 @@
+"""Loader of libhpsi_gb300.so (the CUDA library behind the C ABI).
+
+There is no fallback: if the library is missing or cannot be loaded, every
+entry point raises.  ``effmass_gb300.build.build()`` (or
+``__graft_entry__.build()``) compiles it in-tree.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhpsi_gb300.so")
+
+# every entry point declared in include/hpsi_gb300.h
+EXPORTS = ["hpsi_abi_version", "hpsi_ctx_create", "hpsi_ctx_destroy", "hpsi_set_kpoint", "hpsi_dim",
+           "hpsi_apply", "hpsi_grad_apply", "hpsi_velocity_matrix", "hpsi_profile", "hpsi_profile_read",
+           "hpsi_last_error"]
+
+_lib = None
+
+
+class HpsiError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m effmass_gb300.build` "
+                           "(the H|psi> path has no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    dp = C.POINTER(C.c_double)
+    ctxp = C.c_void_p
+    L.hpsi_abi_version.argtypes = []
+    L.hpsi_abi_version.restype = C.c_int
+    L.hpsi_ctx_create.argtypes = [C.POINTER(abi.HpsiSystem), C.POINTER(ctxp)]
+    L.hpsi_ctx_destroy.argtypes = [ctxp]
+    L.hpsi_set_kpoint.argtypes = [ctxp, C.c_int, C.POINTER(abi.HpsiKpoint)]
+    L.hpsi_dim.argtypes = [ctxp, C.c_int]
+    L.hpsi_apply.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    L.hpsi_grad_apply.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_int, C.c_void_p]
+    L.hpsi_velocity_matrix.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    L.hpsi_profile.argtypes = [ctxp, C.c_int]
+    L.hpsi_profile_read.argtypes = [ctxp, dp, C.POINTER(C.c_longlong)]
+    L.hpsi_last_error.argtypes = [ctxp]
+    L.hpsi_last_error.restype = C.c_char_p
+    for name in EXPORTS:
+        if name != "hpsi_last_error":
+            getattr(L, name).restype = C.c_int
+    if L.hpsi_abi_version() != 1:
+        raise RuntimeError("libhpsi_gb300.so ABI version mismatch")
+    _lib = L
+    return L
+
+
+def check(status: int, ctx=None):
+    if status != 0:
+        msg = load().hpsi_last_error(ctx)
+        raise HpsiError(status, msg.decode() if msg else "")
+    return status

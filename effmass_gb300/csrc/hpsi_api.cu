@@ -1,0 +1,782 @@
+// hpsi_api.cu — the C ABI (include/hpsi_gb300.h): context, k-point binding,
+// device memory and the launch sequence of H|psi>, dH/dk|psi> and the
+// band-pair velocity matrix.
+//
+// Device-resident state (kept in HBM for the life of the context):
+//   V_loc(r) in FP64 and FP32 ([i][j][k] layout), the raw beta / dbeta tables,
+//   atom positions, FFT twiddles; per bound k-point: kinetic, K, q, trig,
+//   Y_lm (+ angular gradients), beta(q) per radial function, S(G) per atom,
+//   the plane decomposition of the G-sphere, and the projector matrices
+//   Pr[P][npw] (+ dPr_alpha for the gradient) in the precisions requested.
+// Per call, a grow-only workspace holds host staging, the FFT intermediate and
+// the projection partial sums.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/hpsi_gb300.h"
+#include "kernels.cuh"
+
+namespace {
+
+struct KSlot {
+    bool valid = false;
+    int npw = 0;
+    double kf[3] = {0, 0, 0};
+    double* d_kin = nullptr;
+    double* d_kvec = nullptr;
+    int* d_g = nullptr;
+    double* d_q = nullptr;
+    double* d_trig = nullptr;
+    double* d_ylm = nullptr;   // ylm, yth, yph consecutive
+    double* d_beta = nullptr;  // beta, dbeta consecutive
+    double* d_dbeta0 = nullptr;
+    double2* d_sf = nullptr;
+    int nxs = 0;
+    int* d_plane = nullptr;    // plane_x[nxs], plane_off[nxs+1], ent_ig[npw], ent_jk[npw]
+    int P = 0;
+    ProjRow* d_rows = nullptr;
+    double* d_lam = nullptr;
+    double2* pr64 = nullptr;
+    bool pr64_grad = false;
+    float2* pr32 = nullptr;
+    bool pr32_grad = false;
+};
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+template <typename T>
+void dfree(T*& p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void slot_free(KSlot& s)
+{
+    dfree(s.d_kin); dfree(s.d_kvec); dfree(s.d_g); dfree(s.d_q); dfree(s.d_trig); dfree(s.d_ylm);
+    dfree(s.d_beta); dfree(s.d_dbeta0); dfree(s.d_sf); dfree(s.d_plane); dfree(s.d_rows); dfree(s.d_lam);
+    dfree(s.pr64); dfree(s.pr32);
+    s = KSlot();
+}
+
+}  // namespace
+
+struct hpsi_ctx {
+    int dev = 0;
+    int n1 = 0, n2 = 0, n3 = 0;
+    double omega = 0;
+    int natom = 0, nrad = 0, nq_max = 0, lmax = 0;
+    bool have_dbeta = true;
+    std::vector<int> atom_species, rad_off, rad_l, rad_nq;
+    std::vector<double> tau, rad_lam, rad_dq, rad_qmax;
+    double* d_tables = nullptr;   // beta then dbeta, [2][nrad][nq_max]
+    int* d_rad_nq = nullptr;
+    double* d_rad_dq = nullptr;
+    double* d_tau = nullptr;
+    double* d_v64 = nullptr;
+    float* d_v32 = nullptr;
+    double2* d_tw64 = nullptr;    // twiddles x, y, z consecutive
+    float2* d_tw32 = nullptr;
+    FftLen L[3];
+    std::map<int, KSlot> slots;
+    unsigned char* ws = nullptr;
+    size_t ws_size = 0;
+    Prof prof;
+    std::string err;
+};
+
+// Message of the last failure that had no context to hold it (hpsi_ctx_create).
+static thread_local std::string g_last_error;
+
+static int fail(hpsi_ctx* c, int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(ctx, expr)                                                                             \
+    do {                                                                                                \
+        cudaError_t e_ = (expr);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? HPSI_ERR_OOM : HPSI_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #expr, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+    } while (0)
+
+// Workspace carving: each piece 256-byte aligned.
+struct Carver {
+    size_t off = 0;
+    template <typename T>
+    size_t take(size_t count)
+    {
+        size_t o = off;
+        off += ((count * sizeof(T)) + 255) / 256 * 256;
+        return o;
+    }
+};
+
+static int ws_reserve(hpsi_ctx* c, size_t bytes)
+{
+    if (bytes <= c->ws_size) return HPSI_OK;
+    if (c->ws) cudaFree(c->ws);
+    c->ws = nullptr;
+    c->ws_size = 0;
+    size_t want = bytes + bytes / 8;
+    CUDA_TRY(c, cudaMalloc((void**)&c->ws, want));
+    c->ws_size = want;
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_abi_version(void) { return HPSI_ABI_VERSION; }
+
+extern "C" const char* hpsi_last_error(const hpsi_ctx* ctx)
+{
+    if (!ctx) return g_last_error.c_str();
+    return ctx->err.c_str();
+}
+
+extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
+{
+    if (!c) return HPSI_ERR_BAD_ARG;
+    cudaSetDevice(c->dev);
+    for (auto& kv : c->slots) slot_free(kv.second);
+    dfree(c->d_tables); dfree(c->d_rad_nq); dfree(c->d_rad_dq); dfree(c->d_tau); dfree(c->d_v64); dfree(c->d_v32);
+    dfree(c->d_tw64); dfree(c->d_tw32);
+    if (c->ws) cudaFree(c->ws);
+    for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : c->prof.pool) cudaEventDestroy(e);
+    delete c;
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_profile(hpsi_ctx* c, int enable)
+{
+    if (!c) return HPSI_ERR_BAD_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->dev));
+    for (auto& r : c->prof.recs) { c->prof.pool.push_back(r.a); c->prof.pool.push_back(r.b); }
+    c->prof.recs.clear();
+    c->prof.on = enable != 0;
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_profile_read(hpsi_ctx* c, double* ms, long long* launches)
+{
+    if (!c || !ms || !launches) return HPSI_ERR_BAD_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->dev));
+    for (int i = 0; i < HPSI_PROFILE_PHASES; ++i) { ms[i] = 0.0; launches[i] = 0; }
+    for (auto& r : c->prof.recs) {
+        CUDA_TRY(c, cudaEventSynchronize(r.b));
+        float t = 0.f;
+        CUDA_TRY(c, cudaEventElapsedTime(&t, r.a, r.b));
+        ms[r.phase] += t;
+        launches[r.phase] += 1;
+    }
+    return HPSI_OK;
+}
+
+static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
+{
+    if (s->n1 < 1 || s->n2 < 1 || s->n3 < 1) return fail(c, HPSI_ERR_BAD_ARG, "FFT grid must be positive");
+    if (!(s->omega > 0)) return fail(c, HPSI_ERR_BAD_ARG, "omega must be positive");
+    if (!s->v_loc) return fail(c, HPSI_ERR_BAD_ARG, "v_loc is NULL");
+    if (s->n_atoms < 0 || s->n_species < 0) return fail(c, HPSI_ERR_BAD_ARG, "negative counts");
+    if (s->n_atoms > 0 && (!s->atom_species || !s->atom_tau)) return fail(c, HPSI_ERR_BAD_ARG, "atoms NULL");
+    if (s->n_species > 0 && !s->species) return fail(c, HPSI_ERR_BAD_ARG, "species NULL");
+    c->n1 = s->n1; c->n2 = s->n2; c->n3 = s->n3;
+    const int ns[3] = {s->n1, s->n2, s->n3};
+    for (int d = 0; d < 3; ++d)
+        if (!fft_factor(ns[d], &c->L[d]))
+            return fail(c, HPSI_ERR_BAD_ARG, "FFT length %d not supported (primes <= 13, n <= %d)", ns[d], HPSI_FFT_MAXN);
+    c->omega = s->omega;
+    c->natom = s->n_atoms;
+    for (int a = 0; a < s->n_atoms; ++a) {
+        int sp = s->atom_species[a];
+        if (sp < 0 || sp >= s->n_species) return fail(c, HPSI_ERR_BAD_ARG, "atom %d: species index %d out of range", a, sp);
+        c->atom_species.push_back(sp);
+        for (int d = 0; d < 3; ++d) c->tau.push_back(s->atom_tau[3 * a + d]);
+    }
+    for (int sp = 0; sp < s->n_species; ++sp) {
+        const hpsi_species& S = s->species[sp];
+        c->rad_off.push_back(c->nrad);
+        if (S.n_proj < 0) return fail(c, HPSI_ERR_BAD_ARG, "species %d: n_proj < 0", sp);
+        if (S.n_proj > 0 && (!S.proj_l || !S.lambda || !S.beta_q))
+            return fail(c, HPSI_ERR_BAD_ARG, "species %d: NULL table", sp);
+        if (S.n_proj > 0 && (S.nq < 4 || !(S.dq > 0) || S.q_max < 0))
+            return fail(c, HPSI_ERR_BAD_ARG, "species %d: table needs nq >= 4, dq > 0, q_max >= 0", sp);
+        if (!S.dbeta_q) c->have_dbeta = false;
+        for (int i = 0; i < S.n_proj; ++i) {
+            if (S.proj_l[i] < 0 || S.proj_l[i] > HPSI_LMAX)
+                return fail(c, HPSI_ERR_BAD_ARG, "species %d projector %d: l=%d outside [0,%d]", sp, i, S.proj_l[i], HPSI_LMAX);
+            c->rad_l.push_back(S.proj_l[i]);
+            c->rad_lam.push_back(S.lambda[i]);
+            c->rad_nq.push_back(S.nq);
+            c->rad_dq.push_back(S.dq);
+            c->rad_qmax.push_back(S.q_max);
+            c->nq_max = std::max(c->nq_max, S.nq);
+            c->lmax = std::max(c->lmax, S.proj_l[i]);
+            c->nrad++;
+        }
+    }
+    // plane FFT kernels keep two n2*n3 planes in shared memory
+    LocalArgs la{};
+    la.n1 = c->n1; la.n2 = c->n2; la.n3 = c->n3; la.kt = 8;
+    if (local_smem_bytes(la, true) > 227 * 1024)
+        return fail(c, HPSI_ERR_BAD_ARG, "FFT grid %dx%dx%d: two complex128 n2*n3 planes exceed shared memory", c->n1, c->n2, c->n3);
+
+    CUDA_TRY(c, cudaGetDevice(&c->dev));
+    const size_t N = (size_t)c->n1 * c->n2 * c->n3;
+    CUDA_TRY(c, dalloc(&c->d_v64, N));
+    CUDA_TRY(c, dalloc(&c->d_v32, N));
+    CUDA_TRY(c, cudaMemcpy(c->d_v64, s->v_loc, N * sizeof(double), cudaMemcpyHostToDevice));
+    {
+        std::vector<float> v32(N);
+        for (size_t i = 0; i < N; ++i) v32[i] = (float)s->v_loc[i];
+        CUDA_TRY(c, cudaMemcpy(c->d_v32, v32.data(), N * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    const int ntw = c->n1 + c->n2 + c->n3;
+    std::vector<double2> tw64(ntw);
+    std::vector<float2> tw32(ntw);
+    int o = 0;
+    for (int d = 0; d < 3; ++d)
+        for (int j = 0; j < ns[d]; ++j, ++o) {
+            double a = 6.283185307179586476925286766559 * (double)j / (double)ns[d];
+            tw64[o] = make_double2(std::cos(a), std::sin(a));
+            tw32[o] = make_float2((float)tw64[o].x, (float)tw64[o].y);
+        }
+    CUDA_TRY(c, dalloc(&c->d_tw64, ntw));
+    CUDA_TRY(c, dalloc(&c->d_tw32, ntw));
+    CUDA_TRY(c, cudaMemcpy(c->d_tw64, tw64.data(), ntw * sizeof(double2), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c->d_tw32, tw32.data(), ntw * sizeof(float2), cudaMemcpyHostToDevice));
+    if (c->natom > 0) {
+        CUDA_TRY(c, dalloc(&c->d_tau, (size_t)3 * c->natom));
+        CUDA_TRY(c, cudaMemcpy(c->d_tau, c->tau.data(), 3 * c->natom * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (c->nrad > 0) {
+        std::vector<double> tab((size_t)2 * c->nrad * c->nq_max, 0.0);
+        int r = 0;
+        for (int sp = 0; sp < s->n_species; ++sp) {
+            const hpsi_species& S = s->species[sp];
+            for (int i = 0; i < S.n_proj; ++i, ++r) {
+                std::memcpy(&tab[(size_t)r * c->nq_max], S.beta_q + (size_t)i * S.nq, S.nq * sizeof(double));
+                if (S.dbeta_q)
+                    std::memcpy(&tab[((size_t)c->nrad + r) * c->nq_max], S.dbeta_q + (size_t)i * S.nq,
+                                S.nq * sizeof(double));
+            }
+        }
+        CUDA_TRY(c, dalloc(&c->d_tables, tab.size()));
+        CUDA_TRY(c, cudaMemcpy(c->d_tables, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, dalloc(&c->d_rad_nq, (size_t)c->nrad));
+        CUDA_TRY(c, dalloc(&c->d_rad_dq, (size_t)c->nrad));
+        CUDA_TRY(c, cudaMemcpy(c->d_rad_nq, c->rad_nq.data(), c->nrad * sizeof(int), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(c->d_rad_dq, c->rad_dq.data(), c->nrad * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_ctx_create(const hpsi_system* sys, hpsi_ctx** out)
+{
+    if (!out) return HPSI_ERR_BAD_ARG;
+    *out = nullptr;
+    if (!sys) return HPSI_ERR_BAD_ARG;
+    hpsi_ctx* c = new hpsi_ctx();
+    int rc = ctx_init(c, sys);
+    if (rc != HPSI_OK) {
+        g_last_error = c->err;  // readable through hpsi_last_error(NULL)
+        hpsi_ctx_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return HPSI_OK;
+}
+
+static KSlot* get_slot(hpsi_ctx* c, int kid)
+{
+    auto it = c->slots.find(kid);
+    if (it == c->slots.end() || !it->second.valid) return nullptr;
+    return &it->second;
+}
+
+extern "C" int hpsi_dim(const hpsi_ctx* ctx, int kid)
+{
+    if (!ctx) return HPSI_ERR_BAD_ARG;
+    auto it = ctx->slots.find(kid);
+    if (it == ctx->slots.end() || !it->second.valid) return HPSI_ERR_STATE;
+    return it->second.npw;
+}
+
+extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
+{
+    if (!c) return HPSI_ERR_BAD_ARG;
+    if (!kp) return fail(c, HPSI_ERR_BAD_ARG, "kpoint is NULL");
+    if (kid < 0 || kid >= 4096) return fail(c, HPSI_ERR_BAD_ARG, "kid %d outside [0, 4096)", kid);
+    const int npw = kp->npw;
+    if (npw < 0) return fail(c, HPSI_ERR_BAD_ARG, "npw < 0");
+    if (npw > 0 && (!kp->g_idx || !kp->kvec || !kp->kinetic)) return fail(c, HPSI_ERR_BAD_ARG, "kpoint arrays NULL");
+    CUDA_TRY(c, cudaSetDevice(c->dev));
+    const int n[3] = {c->n1, c->n2, c->n3};
+
+    // --- host-side validation: the reference's domain_error / assert cases
+    for (int ig = 0; ig < npw; ++ig) {
+        for (int d = 0; d < 3; ++d) {
+            int gd = kp->g_idx[3 * ig + d];
+            int idx = gd + n[d] / 2 + 4;  // structure-factor cache index, src/H_psi/structure_factor.cppm:68-72
+            if (idx < 0 || idx >= n[d] + 8)
+                return fail(c, HPSI_ERR_RANGE, "G %d: g[%d]=%d outside [-n/2-4, n/2+3] for n=%d", ig, d, gd, n[d]);
+        }
+        const double kx = kp->kvec[3 * ig], ky = kp->kvec[3 * ig + 1], kz = kp->kvec[3 * ig + 2];
+        const double q = std::sqrt(kx * kx + ky * ky + kz * kz);
+        for (int r = 0; r < c->nrad; ++r) {
+            if (std::fabs(c->rad_lam[r]) < 1e-15) continue;
+            if (q > c->rad_qmax[r])
+                return fail(c, HPSI_ERR_RANGE, "G %d: q=%.17g exceeds q_max=%.17g", ig, q, c->rad_qmax[r]);
+            if (q > 0 && (int)std::floor(q / c->rad_dq[r]) + 2 >= c->rad_nq[r])
+                return fail(c, HPSI_ERR_RANGE, "G %d: q=%.17g beyond the table (nq=%d)", ig, q, c->rad_nq[r]);
+        }
+    }
+
+    // --- plane decomposition of the sphere on the FFT grid
+    std::vector<int> gi(npw), jk(npw);
+    std::vector<int> plane_of_x(c->n1, -1);
+    std::map<long, int> last;
+    for (int ig = 0; ig < npw; ++ig) {
+        int i = ((kp->g_idx[3 * ig] % n[0]) + n[0]) % n[0];
+        int j = ((kp->g_idx[3 * ig + 1] % n[1]) + n[1]) % n[1];
+        int k = ((kp->g_idx[3 * ig + 2] % n[2]) + n[2]) % n[2];
+        gi[ig] = i;
+        jk[ig] = j * n[2] + k;
+        last[(long)i * n[1] * n[2] + jk[ig]] = ig;  // the reference's scatter: the last write wins
+        plane_of_x[i] = 1;
+    }
+    std::vector<int> plane_x;
+    for (int i = 0; i < c->n1; ++i)
+        if (plane_of_x[i] > 0) { plane_of_x[i] = (int)plane_x.size(); plane_x.push_back(i); }
+    const int nxs = (int)plane_x.size();
+    std::vector<int> plane_off(nxs + 1, 0);
+    for (int ig = 0; ig < npw; ++ig) plane_off[plane_of_x[gi[ig]] + 1]++;
+    for (int p = 0; p < nxs; ++p) plane_off[p + 1] += plane_off[p];
+    std::vector<int> fill(plane_off.begin(), plane_off.end() - 1);
+    std::vector<int> ent_ig(npw), ent_jk(npw);
+    for (int ig = 0; ig < npw; ++ig) {
+        int p = plane_of_x[gi[ig]];
+        int e = fill[p]++;
+        bool scatter = last[(long)gi[ig] * n[1] * n[2] + jk[ig]] == ig;
+        ent_ig[e] = scatter ? ig : (int)((unsigned)ig | 0x80000000u);
+        ent_jk[e] = jk[ig];
+    }
+
+    // --- projector rows
+    std::vector<ProjRow> rows;
+    std::vector<double> lam;
+    for (int a = 0; a < c->natom; ++a) {
+        int sp = c->atom_species[a];
+        int r0 = c->rad_off[sp];
+        int r1 = (sp + 1 < (int)c->rad_off.size()) ? c->rad_off[sp + 1] : c->nrad;
+        for (int r = r0; r < r1; ++r) {
+            if (std::fabs(c->rad_lam[r]) < 1e-15) continue;  // src/H_psi/hamiltonian_callable.cpp:226-227
+            int l = c->rad_l[r];
+            for (int m = -l; m <= l; ++m) {
+                rows.push_back(ProjRow{a, r, l, m});
+                lam.push_back(c->rad_lam[r]);
+            }
+        }
+    }
+
+    KSlot& s = c->slots[kid];
+    slot_free(s);
+    s.npw = npw;
+    for (int d = 0; d < 3; ++d) s.kf[d] = kp->k_frac[d];
+    s.nxs = nxs;
+    s.P = (int)rows.size();
+    if (npw > 0) {
+        const int nlm = (c->lmax + 1) * (c->lmax + 1);
+        const bool grads = c->have_dbeta;
+        CUDA_TRY(c, dalloc(&s.d_kin, (size_t)npw));
+        CUDA_TRY(c, dalloc(&s.d_kvec, (size_t)3 * npw));
+        CUDA_TRY(c, dalloc(&s.d_g, (size_t)3 * npw));
+        CUDA_TRY(c, dalloc(&s.d_q, (size_t)npw));
+        CUDA_TRY(c, dalloc(&s.d_trig, (size_t)4 * npw));
+        CUDA_TRY(c, dalloc(&s.d_ylm, (size_t)(grads ? 3 : 1) * nlm * npw));
+        CUDA_TRY(c, dalloc(&s.d_plane, (size_t)2 * nxs + 1 + 2 * (size_t)npw));
+        CUDA_TRY(c, cudaMemcpy(s.d_kin, kp->kinetic, npw * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(s.d_kvec, kp->kvec, 3 * npw * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(s.d_g, kp->g_idx, 3 * npw * sizeof(int), cudaMemcpyHostToDevice));
+        std::vector<int> pl;
+        pl.insert(pl.end(), plane_x.begin(), plane_x.end());
+        pl.insert(pl.end(), plane_off.begin(), plane_off.end());
+        pl.insert(pl.end(), ent_ig.begin(), ent_ig.end());
+        pl.insert(pl.end(), ent_jk.begin(), ent_jk.end());
+        CUDA_TRY(c, cudaMemcpy(s.d_plane, pl.data(), pl.size() * sizeof(int), cudaMemcpyHostToDevice));
+
+        GTabArgs ga{npw, c->lmax, s.d_kvec, s.d_q, s.d_trig, s.d_ylm, grads ? s.d_ylm + (size_t)nlm * npw : nullptr,
+                    grads ? s.d_ylm + (size_t)2 * nlm * npw : nullptr};
+        CUDA_TRY(c, launch_gtab(ga, 0));
+        if (c->nrad > 0) {
+            CUDA_TRY(c, dalloc(&s.d_beta, (size_t)(grads ? 2 : 1) * c->nrad * npw));
+            CUDA_TRY(c, dalloc(&s.d_dbeta0, (size_t)c->nrad));
+            BetaArgs ba{npw, c->nrad, s.d_q, c->d_tables, grads ? c->d_tables + (size_t)c->nrad * c->nq_max : nullptr,
+                        c->d_rad_nq, c->d_rad_dq, c->nq_max, 1.0 / std::sqrt(c->omega), s.d_beta,
+                        grads ? s.d_beta + (size_t)c->nrad * npw : nullptr, grads ? s.d_dbeta0 : nullptr};
+            CUDA_TRY(c, launch_beta(ba, 0));
+        }
+        if (c->natom > 0) {
+            CUDA_TRY(c, dalloc(&s.d_sf, (size_t)c->natom * npw));
+            SfArgs sa{npw, c->natom, s.d_g, c->d_tau, s.kf[0], s.kf[1], s.kf[2], s.d_sf};
+            CUDA_TRY(c, launch_sf(sa, 0));
+        }
+        if (s.P > 0) {
+            CUDA_TRY(c, dalloc(&s.d_rows, (size_t)s.P));
+            CUDA_TRY(c, dalloc(&s.d_lam, (size_t)s.P));
+            CUDA_TRY(c, cudaMemcpy(s.d_rows, rows.data(), s.P * sizeof(ProjRow), cudaMemcpyHostToDevice));
+            CUDA_TRY(c, cudaMemcpy(s.d_lam, lam.data(), s.P * sizeof(double), cudaMemcpyHostToDevice));
+        }
+        CUDA_TRY(c, cudaDeviceSynchronize());
+    }
+    s.valid = true;
+    return HPSI_OK;
+}
+
+// Build (once) the projector matrices of slot s in complex type C.
+template <typename C>
+static int ensure_proj(hpsi_ctx* c, KSlot& s, bool grad, cudaStream_t st)
+{
+    C*& pr = std::is_same<C, double2>::value ? reinterpret_cast<C*&>(s.pr64) : reinterpret_cast<C*&>(s.pr32);
+    bool& has_grad = std::is_same<C, double2>::value ? s.pr64_grad : s.pr32_grad;
+    if (s.P == 0 || s.npw == 0) return HPSI_OK;
+    if (pr && (has_grad || !grad)) return HPSI_OK;
+    if (grad && !c->have_dbeta) return fail(c, HPSI_ERR_STATE, "gradient needs dbeta tables for every species");
+    dfree(pr);
+    const bool g = grad || c->have_dbeta;  // build the derivative rows together when tables allow
+    CUDA_TRY(c, dalloc(&pr, (size_t)(g ? 4 : 1) * s.P * s.npw));
+    const int nlm = (c->lmax + 1) * (c->lmax + 1);
+    const double* yth = c->have_dbeta ? s.d_ylm + (size_t)nlm * s.npw : nullptr;
+    const double* yph = c->have_dbeta ? s.d_ylm + (size_t)2 * nlm * s.npw : nullptr;
+    const double* dbeta = c->have_dbeta ? s.d_beta + (size_t)c->nrad * s.npw : nullptr;
+    int h = c->prof.open(PH_BUILD, st);
+    CUDA_TRY(c, launch_assemble<C>(s.P, s.npw, s.d_rows, s.d_beta, dbeta, s.d_dbeta0, s.d_q, s.d_trig, s.d_ylm, yth,
+                                   yph, s.d_sf, g, pr, (size_t)s.npw, st));
+    c->prof.close(h, st);
+    has_grad = g;
+    return HPSI_OK;
+}
+
+static int split_for(int M, int N, int K)
+{
+    int blocks = ceil_div(M, 64) * ceil_div(N, 64);
+    int ns = ceil_div(2 * 152 * 2, blocks);
+    int maxs = std::max(1, K / 512);
+    return std::max(1, std::min(ns, maxs));
+}
+
+// hpsi_out[nb][npw] += nonlocal(psi) using projector matrix pr (complex C)
+template <typename C, typename Acc>
+static int nonlocal_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, const C* pr,
+                          unsigned char* ws, cudaStream_t st)
+{
+    if (s.P == 0 || nb == 0) return HPSI_OK;
+    const int ns = split_for(s.P, nb, s.npw);
+    Carver cv;
+    size_t o_part = cv.take<Acc>((size_t)ns * s.P * nb);
+    size_t o_w = cv.take<C>((size_t)s.P * nb);
+    Acc* part = reinterpret_cast<Acc*>(ws + o_part);
+    C* W = reinterpret_cast<C*>(ws + o_w);
+    int h = c->prof.open(PH_PROJ, st);
+    CUDA_TRY(c, (launch_proj_gemm<C, double2, Acc>(s.P, nb, s.npw, pr, (size_t)s.npw, psi, (size_t)s.npw, part, ns, st)));
+    c->prof.close(h, st);
+    h = c->prof.open(PH_REDUCE, st);
+    CUDA_TRY(c, (launch_reduce_splits<Acc, C>(s.P, nb, ns, part, s.d_lam, s.P, W, (size_t)nb, st)));
+    c->prof.close(h, st);
+    h = c->prof.open(PH_EXPAND, st);
+    CUDA_TRY(c, launch_expand_gemm<C>(s.P, nb, s.npw, W, (size_t)nb, pr, (size_t)s.npw, hpsi, (size_t)s.npw, st));
+    c->prof.close(h, st);
+    return HPSI_OK;
+}
+
+template <typename C, typename Acc>
+static size_t nonlocal_ws(const KSlot& s, int nb, int rows_mult)
+{
+    const int M = rows_mult * s.P;
+    const int ns = split_for(M, nb, s.npw);
+    Carver cv;
+    cv.take<Acc>((size_t)ns * M * nb);
+    cv.take<C>((size_t)M * nb);
+    return cv.off;
+}
+
+static int chunk_bands(const KSlot& s, const hpsi_ctx* c, int nb, size_t csize)
+{
+    size_t per = (size_t)s.nxs * c->n2 * c->n3 * csize;
+    if (per == 0) return nb;
+    long ch = (long)((64ull << 20) / per);
+    return (int)std::max(1L, std::min((long)nb, ch));
+}
+
+template <typename C, typename V>
+static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
+                       const V* vloc, const C* tw, cudaStream_t st)
+{
+    if (nb == 0 || s.npw == 0) return HPSI_OK;
+    const int* pl = s.d_plane;
+    LocalArgs a{};
+    a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
+    a.npw = s.npw;
+    a.nxs = s.nxs;
+    a.kt = sizeof(C) == 16 ? 8 : 16;
+    a.inv_n = 1.0 / ((double)c->n1 * c->n2 * c->n3);
+    a.plane_x = pl;
+    a.plane_off = pl + s.nxs;
+    a.ent_ig = pl + 2 * s.nxs + 1;
+    a.ent_jk = pl + 2 * s.nxs + 1 + s.npw;
+    a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
+    const int ch = chunk_bands(s, c, nb, sizeof(C));
+    C* T = reinterpret_cast<C*>(ws);
+    for (int b0 = 0; b0 < nb; b0 += ch) {
+        int nbc = std::min(ch, nb - b0);
+        CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
+                                        tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
+    }
+    return HPSI_OK;
+}
+
+static size_t local_ws(const hpsi_ctx* c, const KSlot& s, int nb, size_t csize)
+{
+    int ch = chunk_bands(s, c, nb, csize);
+    Carver cv;
+    cv.take<unsigned char>((size_t)ch * s.nxs * c->n2 * c->n3 * csize);
+    return cv.off;
+}
+
+static int check_call(hpsi_ctx* c, int kid, int nb, KSlot** sp, int flags)
+{
+    if (!c) return HPSI_ERR_BAD_ARG;
+    if (nb < 0) return fail(c, HPSI_ERR_BAD_ARG, "nb < 0");
+    int prec = flags & HPSI_PREC_MASK;
+    if (prec != HPSI_PREC_FP64 && prec != HPSI_PREC_FP32 && prec != HPSI_PREC_TC)
+        return fail(c, HPSI_ERR_BAD_ARG, "unknown precision %d", prec);
+    KSlot* s = get_slot(c, kid);
+    if (!s) return fail(c, HPSI_ERR_STATE, "k-point slot %d is not bound", kid);
+    *sp = s;
+    cudaError_t e = cudaSetDevice(c->dev);
+    if (e) return fail(c, HPSI_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* hpsi_, int flags, void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (nb > 0 && (!psi_ || !hpsi_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/hpsi NULL");
+    if (nb == 0 || s->npw == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const bool fp64 = prec == HPSI_PREC_FP64;
+    const size_t nel = (size_t)nb * s->npw;
+    // workspace: [staging psi, hpsi] [max(local, nonlocal)]
+    Carver cv;
+    size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_hpsi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_work = cv.off;
+    size_t wl = local_ws(c, *s, nb, fp64 ? sizeof(double2) : sizeof(float2));
+    size_t wn = fp64 ? nonlocal_ws<double2, double2>(*s, nb, 1) : nonlocal_ws<float2, float2>(*s, nb, 1);
+    if ((rc = ws_reserve(c, o_work + std::max(wl, wn)))) return rc;
+    const double2* psi = (const double2*)psi_;
+    double2* hpsi = (double2*)hpsi_;
+    if (!dev) {
+        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
+        hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+    }
+    unsigned char* work = c->ws + o_work;
+    if (fp64) {
+        if ((rc = ensure_proj<double2>(c, *s, false, st))) return rc;
+        if ((rc = local_apply<double2, double>(c, *s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st))) return rc;
+        if ((rc = nonlocal_apply<double2, double2>(c, *s, nb, psi, hpsi, s->pr64, work, st))) return rc;
+    } else {
+        if ((rc = ensure_proj<float2>(c, *s, false, st))) return rc;
+        if ((rc = local_apply<float2, float>(c, *s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
+        if ((rc = nonlocal_apply<float2, float2>(c, *s, nb, psi, hpsi, s->pr32, work, st))) return rc;
+    }
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    return HPSI_OK;
+}
+
+__global__ void grad_kinetic_kernel(int npw, int nb, const double* __restrict__ kvec, const double2* __restrict__ psi,
+                                    double2* dx, double2* dy, double2* dz)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)npw * nb) return;
+    int g = (int)(i % npw);
+    double2 p = psi[i];
+    double2* out[3] = {dx, dy, dz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (!out[d]) continue;
+        double k = kvec[3 * g + d];
+        double2 o = out[d][i];
+        o.x += k * p.x;
+        o.y += k * p.y;
+        out[d][i] = o;
+    }
+}
+
+// d_alpha += dH/dk_alpha psi, all pointers on the device
+template <typename C, typename Acc>
+static int grad_device(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* d[3], unsigned char* work,
+                       cudaStream_t st)
+{
+    const size_t nel = (size_t)nb * s.npw;
+    int h = c->prof.open(PH_OTHER, st);
+    grad_kinetic_kernel<<<ceil_div((long)nel, 256), 256, 0, st>>>(s.npw, nb, s.d_kvec, psi, d[0], d[1], d[2]);
+    c->prof.close(h, st);
+    CUDA_TRY(c, cudaGetLastError());
+    if (s.P == 0) return HPSI_OK;
+    int rc;
+    if ((rc = ensure_proj<C>(c, s, true, st))) return rc;
+    const C* pr = std::is_same<C, double2>::value ? (const C*)s.pr64 : (const C*)s.pr32;
+    const int M = 4 * s.P;
+    const int ns = split_for(M, nb, s.npw);
+    Carver cv;
+    size_t o_part = cv.take<Acc>((size_t)ns * M * nb);
+    size_t o_w = cv.take<C>((size_t)M * nb);
+    Acc* part = reinterpret_cast<Acc*>(work + o_part);
+    C* W = reinterpret_cast<C*>(work + o_w);
+    h = c->prof.open(PH_PROJ, st);
+    CUDA_TRY(c, (launch_proj_gemm<C, double2, Acc>(M, nb, s.npw, pr, (size_t)s.npw, psi, (size_t)s.npw, part, ns, st)));
+    c->prof.close(h, st);
+    h = c->prof.open(PH_REDUCE, st);
+    CUDA_TRY(c, (launch_reduce_splits<Acc, C>(M, nb, ns, part, s.d_lam, s.P, W, (size_t)nb, st)));
+    c->prof.close(h, st);
+    const size_t PN = (size_t)s.P * s.npw;
+    for (int a = 0; a < 3; ++a) {
+        if (!d[a]) continue;
+        h = c->prof.open(PH_EXPAND, st);
+        // lambda <dp_a|psi> p
+        CUDA_TRY(c, launch_expand_gemm<C>(s.P, nb, s.npw, W + (size_t)(a + 1) * s.P * nb, (size_t)nb, pr, (size_t)s.npw,
+                                          d[a], (size_t)s.npw, st));
+        // lambda <p|psi> dp_a
+        CUDA_TRY(c, launch_expand_gemm<C>(s.P, nb, s.npw, W, (size_t)nb, pr + (size_t)(a + 1) * PN, (size_t)s.npw, d[a],
+                                          (size_t)s.npw, st));
+        c->prof.close(h, st);
+    }
+    return HPSI_OK;
+}
+
+template <typename C, typename Acc>
+static size_t grad_ws(const KSlot& s, int nb)
+{
+    return nonlocal_ws<C, Acc>(s, nb, 4);
+}
+
+extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* dx, double* dy, double* dz,
+                               int flags, void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (nb > 0 && !psi_) return fail(c, HPSI_ERR_BAD_ARG, "psi NULL");
+    if (nb == 0 || s->npw == 0 || (!dx && !dy && !dz)) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool fp64 = (flags & HPSI_PREC_MASK) == HPSI_PREC_FP64;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t nel = (size_t)nb * s->npw;
+    double* outs[3] = {dx, dy, dz};
+    Carver cv;
+    size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_out[3] = {0, 0, 0};
+    for (int a = 0; a < 3; ++a)
+        if (!dev && outs[a]) o_out[a] = cv.take<double2>(nel);
+    size_t o_work = cv.off;
+    size_t wn = fp64 ? grad_ws<double2, double2>(*s, nb) : grad_ws<float2, float2>(*s, nb);
+    if ((rc = ws_reserve(c, o_work + wn))) return rc;
+    const double2* psi = (const double2*)psi_;
+    double2* d[3] = {(double2*)dx, (double2*)dy, (double2*)dz};
+    if (!dev) {
+        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        for (int a = 0; a < 3; ++a) {
+            if (!outs[a]) continue;
+            d[a] = reinterpret_cast<double2*>(c->ws + o_out[a]);
+            CUDA_TRY(c, cudaMemcpyAsync(d[a], outs[a], nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        }
+    }
+    unsigned char* work = c->ws + o_work;
+    rc = fp64 ? grad_device<double2, double2>(c, *s, nb, psi, d, work, st)
+              : grad_device<float2, float2>(c, *s, nb, psi, d, work, st);
+    if (rc) return rc;
+    if (!dev)
+        for (int a = 0; a < 3; ++a)
+            if (outs[a]) CUDA_TRY(c, cudaMemcpyAsync(outs[a], d[a], nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_velocity_matrix(hpsi_ctx* c, int kid, int nb, const double* psi_, double* m_, int flags,
+                                    void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (nb > 0 && (!psi_ || !m_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/m NULL");
+    if (nb == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool fp64 = (flags & HPSI_PREC_MASK) == HPSI_PREC_FP64;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t nel = (size_t)nb * s->npw;
+    const size_t nm = (size_t)3 * nb * nb;
+    Carver cv;
+    size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_m = dev ? 0 : cv.take<double2>(nm);
+    size_t o_g = cv.take<double2>(3 * nel);
+    const int nsv = split_for(nb, nb, s->npw);
+    size_t o_vp = cv.take<double2>((size_t)nsv * nb * nb);
+    size_t o_work = cv.off;
+    size_t wn = fp64 ? grad_ws<double2, double2>(*s, nb) : grad_ws<float2, float2>(*s, nb);
+    if ((rc = ws_reserve(c, o_work + wn))) return rc;
+    const double2* psi = (const double2*)psi_;
+    double2* m = (double2*)m_;
+    if (!dev) {
+        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
+        m = reinterpret_cast<double2*>(c->ws + o_m);
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+    }
+    double2* g = reinterpret_cast<double2*>(c->ws + o_g);
+    CUDA_TRY(c, cudaMemsetAsync(g, 0, 3 * nel * sizeof(double2), st));
+    double2* d[3] = {g, g + nel, g + 2 * nel};
+    unsigned char* work = c->ws + o_work;
+    rc = fp64 ? grad_device<double2, double2>(c, *s, nb, psi, d, work, st)
+              : grad_device<float2, float2>(c, *s, nb, psi, d, work, st);
+    if (rc) return rc;
+    double2* vp = reinterpret_cast<double2*>(c->ws + o_vp);
+    for (int a = 0; a < 3; ++a) {
+        // m[a][i][j] = sum_G conj(psi_i) (dH_a psi_j)
+        int h = c->prof.open(PH_OTHER, st);
+        CUDA_TRY(c, (launch_proj_gemm<double2, double2, double2>(nb, nb, s->npw, psi, (size_t)s->npw, d[a],
+                                                                 (size_t)s->npw, vp, nsv, st)));
+        CUDA_TRY(c, (launch_reduce_splits<double2, double2>(nb, nb, nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
+                                                            (size_t)nb, st)));
+        c->prof.close(h, st);
+    }
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(m_, m, nm * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    return HPSI_OK;
+}

@@ -1,0 +1,139 @@
+// kernels.cuh — argument blocks and launchers shared between the kernel
+// translation units and the C-ABI layer (hpsi_api.cu).
+#pragma once
+
+#include "common.cuh"
+#include "fft.cuh"
+
+#define HPSI_LMAX 4  // highest angular momentum of a projector (s, p, d, f, g)
+
+#include <vector>
+
+// Phases timed by the optional per-launch CUDA-event profile (hpsi_profile).
+enum HpsiPhase {
+    PH_BUILD = 0,    // projector build (set-up, lazily on first use of a precision)
+    PH_G2R = 1,      // scatter + y/z FFT planes
+    PH_XPASS = 2,    // x FFT, V multiply, x FFT
+    PH_R2G = 3,      // z/y FFT planes + gather + kinetic
+    PH_PROJ = 4,     // projection GEMM (split-K partials)
+    PH_REDUCE = 5,   // split reduction * lambda
+    PH_EXPAND = 6,   // expansion GEMM
+    PH_OTHER = 7,    // gradient kinetic term, velocity GEMMs, conversions
+    PH_COUNT = 8
+};
+
+// Event pairs around launches; read back and summed by hpsi_profile_read.
+struct Prof {
+    bool on = false;
+    struct Rec { int phase; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t take()
+    {
+        if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    int open(int phase, cudaStream_t st)
+    {
+        if (!on) return -1;
+        Rec r{phase, take(), take()};
+        cudaEventRecord(r.a, st);
+        recs.push_back(r);
+        return (int)recs.size() - 1;
+    }
+    void close(int h, cudaStream_t st)
+    {
+        if (h >= 0) cudaEventRecord(recs[h].b, st);
+    }
+};
+
+// ---- local potential (local.cu) -------------------------------------------
+struct LocalArgs {
+    int n1, n2, n3;
+    int npw;
+    int nxs;                // x-planes that hold sphere points
+    int kt;                 // x-lines per block in the x pass
+    double inv_n;           // 1/(n1*n2*n3): the R2G normalisation
+    const int* plane_x;     // [nxs] grid x index of plane p
+    const int* plane_off;   // [nxs+1] entry range of plane p
+    const int* ent_ig;      // [npw] caller-order G index; negative = gather only
+    const int* ent_jk;      // [npw] j*n3 + k of the entry
+    FftLen Lx, Ly, Lz;
+};
+
+size_t local_smem_bytes(const LocalArgs& a, bool fp64);
+
+template <typename C, typename V>
+cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
+                         const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof);
+
+// ---- projector build (projectors.cu) --------------------------------------
+// Per G: spherical coordinates, trig, Y_lm and its angular gradients.
+struct GTabArgs {
+    int npw, lmax;
+    const double* kvec;     // [npw][3]
+    double* q;              // [npw]
+    double* trig;           // [4][npw]: sin th, cos th, sin ph, cos ph
+    double* ylm;            // [(lmax+1)^2][npw]
+    double* yth;            // [(lmax+1)^2][npw] dY/dtheta (may be null)
+    double* yph;            // [(lmax+1)^2][npw] (1/sin th) dY/dphi (may be null)
+};
+cudaError_t launch_gtab(const GTabArgs& a, cudaStream_t st);
+
+// Per (species, projector, G): beta(q) and dbeta/dq with the plane-wave norm.
+struct BetaArgs {
+    int npw, nrad;          // nrad = sum over species of n_proj
+    const double* q;
+    const double* tables;   // [nrad][nq_max] raw beta tables
+    const double* dtables;  // [nrad][nq_max] raw dbeta tables (may be null)
+    const int* rad_nq;      // [nrad]
+    const double* rad_dq;   // [nrad]
+    int nq_max;
+    double norm;            // 1/sqrt(omega)
+    double* beta;           // [nrad][npw]
+    double* dbeta;          // [nrad][npw] (may be null)
+    double* dbeta0;         // [nrad] dbeta at q = 0 (may be null)
+};
+cudaError_t launch_beta(const BetaArgs& a, cudaStream_t st);
+
+// Per (atom, G): S = exp(-i 2 pi k.tau) * prod_d exp(-i 2 pi g_d tau_d).
+struct SfArgs {
+    int npw, natom;
+    const int* g;           // [npw][3]
+    const double* tau;      // [natom][3]
+    double kf0, kf1, kf2;
+    double2* sf;            // [natom][npw]
+};
+cudaError_t launch_sf(const SfArgs& a, cudaStream_t st);
+
+// One projector row: atom a, radial function rad (global index), l, m.
+struct ProjRow {
+    int atom, rad, l, m;
+};
+
+// Projector matrices Pr[row][G] = beta*Y*S and, with grad, dPr_alpha rows at
+// row offsets (1+alpha)*P.
+template <typename C>
+cudaError_t launch_assemble(int P, int npw, const ProjRow* rows, const double* beta, const double* dbeta,
+                            const double* dbeta0, const double* q, const double* trig, const double* ylm,
+                            const double* yth, const double* yph, const double2* sf, bool grad, C* out,
+                            size_t ld, cudaStream_t st);
+
+// ---- SIMT complex GEMMs (gemm.cu) -----------------------------------------
+// Projection, split over K: part[s][m][n] = sum_{k in split s} conj(A[m][k]) * B[n][k]
+template <typename TA, typename TB, typename Acc>
+cudaError_t launch_proj_gemm(int M, int N, int K, const TA* A, size_t lda, const TB* B, size_t ldb, Acc* part,
+                             int nsplit, cudaStream_t st);
+// W[m][n] = scale[m] * sum_s part[s][m][n]   (scale may be null -> 1)
+template <typename Acc, typename CW>
+cudaError_t launch_reduce_splits(int M, int N, int nsplit, const Acc* part, const double* scale, int scale_period,
+                                 CW* W, size_t ldw, cudaStream_t st);
+// Expansion: out[n][k] += sum_m W[m][n] * A[m][k]   (out is complex128)
+template <typename C>
+cudaError_t launch_expand_gemm(int M, int N, int K, const C* W, size_t ldw, const C* A, size_t lda, double2* out,
+                               size_t ldo, cudaStream_t st);
+// out[i] = from_c128(in[i])
+template <typename C>
+cudaError_t launch_convert(size_t n, const double2* in, C* out, cudaStream_t st);

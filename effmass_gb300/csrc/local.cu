@@ -1,0 +1,183 @@
+// local.cu — kinetic + local-potential term of H|psi>, batched over bands.
+//
+// Reference: src/H_psi/hamiltonian_callable.cpp:119-182 — kinetic loop,
+// scatter of psi(G) onto the grid at (g mod n), FFT3D G2R (unnormalised,
+// exp(+iG.r)), multiply by V(r), FFT3D R2G (forward, 1/n per axis), gather.
+//
+// GB300 layout: the sphere occupies only nxs of the n1 x-planes, so the work
+// is split into three passes over an intermediate T[band][plane][j][k]
+// (complex, nxs planes of n2*n3):
+//   A  g2r_planes : per (plane, band): scatter psi into a shared-memory plane,
+//                   FFT along z then y (G2R), store the plane to T.
+//   B  x_pass     : per (j, k-tile), looping over bands: gather the nxs
+//                   planes of T into shared memory x-lines (zeros elsewhere),
+//                   FFT along x (G2R), multiply by V, FFT along x (R2G), and
+//                   store the nxs sphere planes back into T in place.
+//   C  r2g_planes : per (plane, band): FFT along y then z (R2G), then gather
+//                   the sphere points: hpsi += kinetic*psi + grid/N.
+// T is sized for a chunk of bands so that it stays resident in L2 between
+// the passes.  Kinetic energy is fused into pass C.
+#include "fft.cuh"
+#include "kernels.cuh"
+
+template <typename C>
+__global__ void __launch_bounds__(256) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
+                                                  const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n2 = a.n2, n3 = a.n3, n23 = n2 * n3;
+    C* b0 = reinterpret_cast<C*>(smem_raw);
+    C* b1 = b0 + n23;
+    C* twy = b1 + n23;
+    C* twz = twy + n2;
+    const int p = blockIdx.x;
+    const int b = blockIdx.y;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
+    for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
+    for (int t = threadIdx.x; t < n23; t += blockDim.x) b0[t] = cmake<C>(0, 0);
+    __syncthreads();
+    const double2* ps = psi + (size_t)b * a.npw;
+    const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        int ig = a.ent_ig[e];
+        if (ig >= 0) b0[a.ent_jk[e]] = from_c128<C>(ps[ig]);
+    }
+    __syncthreads();
+    int cur = fft_lines<C, false>(b0, b1, 0, a.Lz, n2, n3, 1, twz, +1);
+    cur = fft_lines<C, true>(b0, b1, cur, a.Ly, n3, 1, n3, twy, +1);
+    const C* res = cur ? b1 : b0;
+    C* out = T + ((size_t)b * a.nxs + p) * n23;
+    for (int t = threadIdx.x; t < n23; t += blockDim.x) out[t] = res[t];
+}
+
+template <typename C, typename V>
+__global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
+                                              const C* __restrict__ tw_x_g)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3, KT = a.kt;
+    C* b0 = reinterpret_cast<C*>(smem_raw);
+    C* b1 = b0 + n1 * KT;
+    C* twx = b1 + n1 * KT;
+    V* vt = reinterpret_cast<V*>(twx + n1);
+    const int j = blockIdx.y;
+    const int k0 = blockIdx.x * KT;
+    const int kt = min(KT, n3 - k0);
+    const int nxs = a.nxs;
+    for (int t = threadIdx.x; t < n1; t += blockDim.x) twx[t] = tw_x_g[t];
+    for (int t = threadIdx.x; t < n1 * kt; t += blockDim.x) {
+        int x = t / kt, kk = t % kt;
+        vt[x * KT + kk] = vloc[((size_t)x * n2 + j) * n3 + k0 + kk];
+    }
+    const size_t plane = (size_t)n2 * n3;
+    for (int b = 0; b < nb; ++b) {
+        for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) b0[t] = cmake<C>(0, 0);
+        __syncthreads();
+        C* Tb = T + (size_t)b * nxs * plane + (size_t)j * n3 + k0;
+        for (int t = threadIdx.x; t < nxs * kt; t += blockDim.x) {
+            int pp = t / kt, kk = t % kt;
+            b0[a.plane_x[pp] * KT + kk] = Tb[(size_t)pp * plane + kk];
+        }
+        __syncthreads();
+        int cur = fft_lines<C, true>(b0, b1, 0, a.Lx, kt, 1, KT, twx, +1);
+        C* res = cur ? b1 : b0;
+        for (int t = threadIdx.x; t < n1 * kt; t += blockDim.x) {
+            int x = t / kt, kk = t % kt;
+            res[x * KT + kk] = cscale(res[x * KT + kk], (typename Real<C>::type)vt[x * KT + kk]);
+        }
+        __syncthreads();
+        cur = fft_lines<C, true>(b0, b1, cur, a.Lx, kt, 1, KT, twx, -1);
+        res = cur ? b1 : b0;
+        for (int t = threadIdx.x; t < nxs * kt; t += blockDim.x) {
+            int pp = t / kt, kk = t % kt;
+            Tb[(size_t)pp * plane + kk] = res[a.plane_x[pp] * KT + kk];
+        }
+        __syncthreads();
+    }
+}
+
+template <typename C>
+__global__ void __launch_bounds__(256) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
+                                                  double2* __restrict__ hpsi, const double* __restrict__ kinetic,
+                                                  const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n2 = a.n2, n3 = a.n3, n23 = n2 * n3;
+    C* b0 = reinterpret_cast<C*>(smem_raw);
+    C* b1 = b0 + n23;
+    C* twy = b1 + n23;
+    C* twz = twy + n2;
+    const int p = blockIdx.x;
+    const int b = blockIdx.y;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
+    for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
+    const C* in = T + ((size_t)b * a.nxs + p) * n23;
+    for (int t = threadIdx.x; t < n23; t += blockDim.x) b0[t] = in[t];
+    __syncthreads();
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Ly, n3, 1, n3, twy, -1);
+    cur = fft_lines<C, false>(b0, b1, cur, a.Lz, n2, n3, 1, twz, -1);
+    const C* res = cur ? b1 : b0;
+    const double2* ps = psi + (size_t)b * a.npw;
+    double2* hp = hpsi + (size_t)b * a.npw;
+    const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        int ig = a.ent_ig[e] & 0x7fffffff;
+        double2 g = as_c128(res[a.ent_jk[e]]);
+        double2 s = ps[ig];
+        double kin = kinetic[ig];
+        double2 h = hp[ig];
+        h.x += kin * s.x + g.x * a.inv_n;
+        h.y += kin * s.y + g.y * a.inv_n;
+        hp[ig] = h;
+    }
+}
+
+template <typename C>
+static size_t plane_smem(const LocalArgs& a)
+{
+    return sizeof(C) * (2 * (size_t)a.n2 * a.n3 + a.n2 + a.n3);
+}
+
+template <typename C, typename V>
+static size_t xpass_smem(const LocalArgs& a)
+{
+    return sizeof(C) * (2 * (size_t)a.n1 * a.kt + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt;
+}
+
+size_t local_smem_bytes(const LocalArgs& a, bool fp64)
+{
+    size_t p = fp64 ? plane_smem<double2>(a) : plane_smem<float2>(a);
+    size_t x = fp64 ? xpass_smem<double2, double>(a) : xpass_smem<float2, float>(a);
+    return p > x ? p : x;
+}
+
+template <typename C, typename V>
+cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
+                         const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof)
+{
+    const size_t sp = plane_smem<C>(a), sx = xpass_smem<C, V>(a);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(g2r_planes<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(r2g_planes<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(x_pass<C, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
+    if (a.nxs == 0 || nb == 0) return cudaSuccess;
+    dim3 gp(a.nxs, nb);
+    int h = prof->open(PH_G2R, st);
+    g2r_planes<C><<<gp, 256, sp, st>>>(a, psi, T, twy, twz);
+    prof->close(h, st);
+    dim3 gx(ceil_div(a.n3, a.kt), a.n2);
+    h = prof->open(PH_XPASS, st);
+    x_pass<C, V><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    prof->close(h, st);
+    h = prof->open(PH_R2G, st);
+    r2g_planes<C><<<gp, 256, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
+    prof->close(h, st);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_local<double2, double>(const LocalArgs&, int, const double2*, double2*, const double*,
+                                                   double2*, const double*, const double2*, const double2*,
+                                                   const double2*, cudaStream_t, Prof*);
+template cudaError_t launch_local<float2, float>(const LocalArgs&, int, const double2*, double2*, const double*,
+                                                 float2*, const float*, const float2*, const float2*, const float2*,
+                                                 cudaStream_t, Prof*);

@@ -1,0 +1,237 @@
+"""Python mirror of the reference's H_psi operator API over libhpsi_gb300.so.
+
+Reference interface (bzzlfd/effmass, src/H_psi/hamiltonian.cppm):
+
+    Hamiltonian H(...); H.load...(); H.finalize(...)      -> Hamiltonian(system)
+    auto op = H.at_k(ik);                                 -> op = H.at_k(ik, kpoint)
+    op(psi, hpsi)            // hpsi += H psi, one band    -> op(psi, hpsi)
+    op(n_bands, psi, hpsi)   // declared, never defined    -> op(n_bands, psi, hpsi)
+    op.dim(); op.set_ikpt(j)                              -> op.dim(); op.set_ikpt(j)
+    H.gradient().at_k(ik)(psi, GradHPsi{x, y, z})         -> H.gradient().at_k(ik)(psi, GradHPsi(x, y, z))
+
+Outputs accumulate, as in the reference (the caller zeroes them).  Arrays
+may be numpy complex128 (host memory: copied in and out inside the call) or
+CUDA torch complex128 tensors (device memory: used in place, launched on the
+current torch stream).  Errors raise ``HpsiError`` with the library's status
+(BAD_ARG / RANGE / STATE ... for the reference's invalid_argument /
+domain_error / runtime_error).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Optional
+
+import numpy as np
+
+from . import abi
+from ._lib import HpsiError, check, load
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(x, npw: int, nb: int, name: str):
+    """(pointer, is_device) of a complex128 block of nb*npw values."""
+    if x is None:
+        return None, None
+    if _is_torch(x):
+        import torch
+        if x.dtype != torch.complex128 or not x.is_contiguous():
+            raise HpsiError(abi.HPSI_ERR_BAD_ARG, f"{name}: need a contiguous complex128 tensor")
+        if x.numel() < nb * npw:
+            raise HpsiError(abi.HPSI_ERR_BAD_ARG, f"{name}: {x.numel()} values < {nb}*{npw}")
+        return C.c_void_p(x.data_ptr()), bool(x.is_cuda)
+    if not isinstance(x, np.ndarray) or x.dtype != np.complex128 or not x.flags["C_CONTIGUOUS"]:
+        raise HpsiError(abi.HPSI_ERR_BAD_ARG, f"{name}: need a C-contiguous complex128 array")
+    if x.size < nb * npw:
+        raise HpsiError(abi.HPSI_ERR_BAD_ARG, f"{name}: {x.size} values < {nb}*{npw}")
+    return C.c_void_p(x.ctypes.data), False
+
+
+def _stream_for(device: bool):
+    if not device:
+        return None
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@dataclasses.dataclass
+class GradHPsi:
+    """Outputs of dH/dk_{x,y,z}|psi>; None skips a direction (the reference's empty span)."""
+    x: Optional[object] = None
+    y: Optional[object] = None
+    z: Optional[object] = None
+
+
+class Hamiltonian:
+    """Device-resident system (V_loc, tables, atoms) — the reference's finalized Hamiltonian."""
+
+    def __init__(self, system, precision: str = "fp64"):
+        self._lib = load()
+        self.system = system
+        self.precision = precision
+        self._packed = abi.pack_system(system)
+        h = C.c_void_p()
+        st = self._lib.hpsi_ctx_create(C.byref(self._packed.struct), C.byref(h))
+        check(st, None)
+        self._ctx = h
+        self._kpoints = {}
+
+    # -- lifetime --
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.hpsi_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def flags(self, precision: Optional[str] = None, device: bool = False) -> int:
+        f = abi.PRECISIONS[precision or self.precision]
+        if device:
+            f |= abi.HPSI_DEVICE_PTRS
+        return f
+
+    # -- k-points --
+    def set_kpoint(self, kid: int, kpoint):
+        packed = abi.pack_kpoint(kpoint)
+        check(self._lib.hpsi_set_kpoint(self._ctx, kid, C.byref(packed.struct)), self._ctx)
+        self._kpoints[kid] = kpoint
+
+    def dim(self, kid: int) -> int:
+        n = self._lib.hpsi_dim(self._ctx, kid)
+        if n < 0:
+            check(n, self._ctx)
+        return n
+
+    def at_k(self, kid: int, kpoint=None, precision: Optional[str] = None) -> "Callable":
+        if kpoint is not None:
+            self.set_kpoint(kid, kpoint)
+        return Callable(self, kid, precision)
+
+    def gradient(self) -> "Gradient":
+        return Gradient(self)
+
+    # -- instrumentation --
+    PHASES = ["build", "g2r_planes", "x_pass", "r2g_planes", "proj_gemm", "reduce", "expand_gemm", "other"]
+
+    def profile(self, on: bool = True):
+        """Reset and switch the per-phase CUDA-event profile of later calls."""
+        check(self._lib.hpsi_profile(self._ctx, 1 if on else 0), self._ctx)
+
+    def profile_read(self):
+        """{phase: (milliseconds, launches)} summed over the calls since profile(True)."""
+        ms = (C.c_double * 8)()
+        n = (C.c_longlong * 8)()
+        check(self._lib.hpsi_profile_read(self._ctx, ms, n), self._ctx)
+        return {name: (ms[i], int(n[i])) for i, name in enumerate(self.PHASES)}
+
+    # -- raw calls --
+    def apply(self, kid: int, nb: int, psi, hpsi, precision: Optional[str] = None):
+        npw = self.dim(kid)
+        p, dev_p = _ptr(psi, npw, nb, "psi")
+        h, dev_h = _ptr(hpsi, npw, nb, "hpsi")
+        if dev_p != dev_h:
+            raise HpsiError(abi.HPSI_ERR_BAD_ARG, "psi and hpsi must both be host or both be device arrays")
+        check(self._lib.hpsi_apply(self._ctx, kid, nb, p, h, self.flags(precision, dev_p), _stream_for(dev_p)),
+              self._ctx)
+
+    def grad_apply(self, kid: int, nb: int, psi, out: GradHPsi, precision: Optional[str] = None):
+        npw = self.dim(kid)
+        p, dev = _ptr(psi, npw, nb, "psi")
+        ptrs = []
+        for name in ("x", "y", "z"):
+            o = getattr(out, name)
+            q, d = _ptr(o, npw, nb, name)
+            if o is not None and d != dev:
+                raise HpsiError(abi.HPSI_ERR_BAD_ARG, "psi and outputs must live in the same memory")
+            ptrs.append(q)
+        check(self._lib.hpsi_grad_apply(self._ctx, kid, nb, p, ptrs[0], ptrs[1], ptrs[2],
+                                        self.flags(precision, dev), _stream_for(dev)), self._ctx)
+
+    def velocity_matrix(self, kid: int, nb: int, psi, out=None, precision: Optional[str] = None):
+        """M[a][m][n] = <psi_m|dH/dk_a|psi_n> (complex128 [3, nb, nb], overwritten)."""
+        npw = self.dim(kid)
+        p, dev = _ptr(psi, npw, nb, "psi")
+        if out is None:
+            if dev:
+                import torch
+                out = torch.zeros((3, nb, nb), dtype=torch.complex128, device=psi.device)
+            else:
+                out = np.zeros((3, nb, nb), dtype=np.complex128)
+        m, dm = _ptr(out, nb, 3 * nb, "m")
+        if dm != dev:
+            raise HpsiError(abi.HPSI_ERR_BAD_ARG, "psi and m must live in the same memory")
+        check(self._lib.hpsi_velocity_matrix(self._ctx, kid, nb, p, m, self.flags(precision, dev),
+                                             _stream_for(dev)), self._ctx)
+        return out
+
+
+class Callable:
+    """H|psi> at a fixed k-point (the reference's Hamiltonian::Callable)."""
+
+    def __init__(self, parent: Hamiltonian, kid: int, precision: Optional[str] = None):
+        self._h = parent
+        self._kid = kid
+        self._prec = precision
+        parent.dim(kid)  # raises STATE if the slot is unbound
+
+    def dim(self) -> int:
+        return self._h.dim(self._kid)
+
+    def set_ikpt(self, kid: int, kpoint=None):
+        if kpoint is not None:
+            self._h.set_kpoint(kid, kpoint)
+        self._h.dim(kid)
+        self._kid = kid
+
+    def __call__(self, *args):
+        if len(args) == 2:
+            psi, hpsi = args
+            nb = 1
+        elif len(args) == 3:
+            nb, psi, hpsi = args
+        else:
+            raise TypeError("call as op(psi, hpsi) or op(n_bands, psi, hpsi)")
+        self._h.apply(self._kid, int(nb), psi, hpsi, self._prec)
+
+
+class Gradient:
+    def __init__(self, parent: Hamiltonian):
+        self._h = parent
+
+    def at_k(self, kid: int, kpoint=None, precision: Optional[str] = None) -> "GradientCallable":
+        if kpoint is not None:
+            self._h.set_kpoint(kid, kpoint)
+        return GradientCallable(self._h, kid, precision)
+
+
+class GradientCallable:
+    """dH/dk_alpha|psi> at a fixed k-point (the reference's Gradient::Callable)."""
+
+    def __init__(self, parent: Hamiltonian, kid: int, precision: Optional[str] = None):
+        self._h = parent
+        self._kid = kid
+        self._prec = precision
+        parent.dim(kid)
+
+    def dim(self) -> int:
+        return self._h.dim(self._kid)
+
+    def __call__(self, psi, out: GradHPsi, n_bands: int = 1):
+        self._h.grad_apply(self._kid, int(n_bands), psi, out, self._prec)

@@ -106,7 +106,8 @@ typedef struct hpsi_ctx hpsi_ctx;
 
 int hpsi_abi_version(void);
 
-/* Build a context on the current CUDA device: uploads V_loc, tables, atoms. */
+/* Build a context on the current CUDA device: uploads V_loc, tables, atoms.
+ * On failure *out is NULL and hpsi_last_error(NULL) gives the reason. */
 int hpsi_ctx_create(const hpsi_system* sys, hpsi_ctx** out);
 int hpsi_ctx_destroy(hpsi_ctx* ctx);
 
@@ -131,7 +132,20 @@ int hpsi_grad_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi,
 int hpsi_velocity_matrix(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* m,
                          int flags, void* stream);
 
-/* Message of the last failed call on ctx (never NULL). */
+/* Per-phase CUDA-event profile of the device work queued by later calls
+ * (instrumentation for benchmarks; off by default).  hpsi_profile(ctx, on)
+ * resets the record and switches it on or off; hpsi_profile_read waits for
+ * the recorded work and fills, per phase, the summed milliseconds and the
+ * number of kernel launches.  Phases: 0 projector build, 1 G->r planes
+ * (scatter + z/y FFT), 2 x pass (x FFT, V, x FFT), 3 r->G planes (y/z FFT +
+ * gather + kinetic), 4 projection GEMM, 5 split-K reduction, 6 expansion GEMM,
+ * 7 other (gradient kinetic term, velocity GEMMs). */
+#define HPSI_PROFILE_PHASES 8
+int hpsi_profile(hpsi_ctx* ctx, int enable);
+int hpsi_profile_read(hpsi_ctx* ctx, double* ms, long long* launches);
+
+/* Message of the last failed call on ctx (never NULL); with ctx == NULL the
+ * message of the calling thread's last failed hpsi_ctx_create. */
 const char* hpsi_last_error(const hpsi_ctx* ctx);
 
 #ifdef __cplusplus

@@ -1,0 +1,99 @@
+"""CPU checks of the C ABI boundary: the library builds, loads and exports
+every entry point include/hpsi_gb300.h declares; the ctypes structs match the
+C layout; without a GPU the library fails loudly instead of computing on the
+host."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import ROOT
+from effmass_gb300 import abi
+
+HEADER = os.path.join(ROOT, "include", "hpsi_gb300.h")
+
+
+def declared_functions():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(hpsi_[a-z_0-9]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from effmass_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_api():
+    names = declared_functions()
+    for n in ["hpsi_ctx_create", "hpsi_ctx_destroy", "hpsi_set_kpoint", "hpsi_apply", "hpsi_grad_apply",
+              "hpsi_velocity_matrix", "hpsi_last_error", "hpsi_dim", "hpsi_abi_version"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from effmass_gb300 import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    assert lib.hpsi_abi_version() == 1
+
+
+def test_struct_layout_matches_c():
+    src = r"""
+    #include <stdio.h>
+    #include <stddef.h>
+    #include "hpsi_gb300.h"
+    int main(void){
+      printf("%zu %zu %zu %zu\n", sizeof(hpsi_species), offsetof(hpsi_species,dq), offsetof(hpsi_species,beta_q), offsetof(hpsi_species,dbeta_q));
+      printf("%zu %zu %zu %zu %zu\n", sizeof(hpsi_system), offsetof(hpsi_system,lattice), offsetof(hpsi_system,omega), offsetof(hpsi_system,species), offsetof(hpsi_system,atom_tau));
+      printf("%zu %zu %zu %zu\n", sizeof(hpsi_kpoint), offsetof(hpsi_kpoint,k_frac), offsetof(hpsi_kpoint,g_idx), offsetof(hpsi_kpoint,kinetic));
+      return 0; }
+    """
+    with tempfile.TemporaryDirectory() as td:
+        cfile = os.path.join(td, "l.c")
+        exe = os.path.join(td, "l")
+        open(cfile, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.dirname(HEADER), cfile, "-o", exe], check=True)
+        got = [list(map(int, l.split())) for l in subprocess.run([exe], capture_output=True, text=True).stdout.splitlines()]
+    S, Y, K = abi.HpsiSpecies, abi.HpsiSystem, abi.HpsiKpoint
+    assert got[0] == [C.sizeof(S), S.dq.offset, S.beta_q.offset, S.dbeta_q.offset]
+    assert got[1] == [C.sizeof(Y), Y.lattice.offset, Y.omega.offset, Y.species.offset, Y.atom_tau.offset]
+    assert got[2] == [C.sizeof(K), K.k_frac.offset, K.g_idx.offset, K.kinetic.offset]
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-GPU failure path")
+def test_no_gpu_fails_loudly(lib):
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import Hamiltonian
+    from effmass_gb300._lib import HpsiError
+    sysm = S.make_system("tiny")
+    with pytest.raises(HpsiError) as ei:
+        Hamiltonian(sysm)
+    assert ei.value.status in (abi.HPSI_ERR_CUDA, abi.HPSI_ERR_OOM)
+
+
+def test_invalid_system_rejected_before_device_use(lib):
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import Hamiltonian
+    from effmass_gb300._lib import HpsiError
+    sysm = S.make_system("tiny")
+    sysm.n1 = 17 * 19  # prime factors beyond the FFT radices
+    with pytest.raises(HpsiError) as ei:
+        Hamiltonian(sysm)
+    assert ei.value.status == abi.HPSI_ERR_BAD_ARG
+    assert "FFT length" in str(ei.value)
