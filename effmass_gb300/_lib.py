@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhpsi_gb3
 # every entry point declared in include/hpsi_gb300.h
 EXPORTS = ["hpsi_abi_version", "hpsi_ctx_create", "hpsi_ctx_destroy", "hpsi_set_kpoint", "hpsi_dim",
            "hpsi_apply", "hpsi_grad_apply", "hpsi_velocity_matrix", "hpsi_profile", "hpsi_profile_read",
-           "hpsi_last_error"]
+           "hpsi_apply_noalloc", "hpsi_last_error"]
 
 _lib = None
 
@@ -47,6 +47,7 @@ def load():
     L.hpsi_grad_apply.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.c_void_p]
     L.hpsi_velocity_matrix.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    L.hpsi_apply_noalloc.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     L.hpsi_profile.argtypes = [ctxp, C.c_int]
     L.hpsi_profile_read.argtypes = [ctxp, dp, C.POINTER(C.c_longlong)]
     L.hpsi_last_error.argtypes = [ctxp]

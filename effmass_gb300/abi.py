@@ -25,6 +25,7 @@ HPSI_PREC_FP32 = 1
 HPSI_PREC_TC = 2
 HPSI_DEVICE_PTRS = 0x10
 HPSI_SYNC = 0x20
+HPSI_NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
 PRECISIONS = {"fp64": HPSI_PREC_FP64, "fp32": HPSI_PREC_FP32, "tc": HPSI_PREC_TC}
 

@@ -780,3 +780,147 @@ extern "C" int hpsi_velocity_matrix(hpsi_ctx* c, int kid, int nb, const double* 
     if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
     return HPSI_OK;
 }
+
+// ---------------------------------------------------------------------------
+// hpsi_apply_noalloc — H|psi> for callers that cannot allocate device memory.
+//
+// Some callers of this library may not call cudaMalloc once they are running:
+// a k.p or eigensolver loop that runs under a fixed device-memory budget set
+// at start-up, a host runtime whose own allocator owns all device memory and
+// forbids other allocations, or code that must not add the implicit device
+// synchronisation an allocation can cause between its kernels.  For them this
+// entry point computes exactly what hpsi_apply computes, but all per-call
+// scratch (the FFT planes of the local term, the split-K partial sums and the
+// projected coefficients of the nonlocal term) lives in one file-scope device
+// array of HPSI_NOALLOC_SCRATCH_BYTES (32 MiB).  Every GPU that loads this
+// library holds that array until the process exits.
+//
+// Rules:
+//  * psi and hpsi are device pointers (HPSI_DEVICE_PTRS is required);
+//  * the projector matrices of the requested precision must already exist:
+//    the first hpsi_apply / hpsi_grad_apply at that precision on the k-point
+//    builds them (that call allocates); otherwise HPSI_ERR_STATE;
+//  * sizes beyond the scratch (one band's FFT planes, or one band's
+//    projection partials) are rejected with HPSI_ERR_BAD_ARG;
+//  * the first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress (which may load the module); make that first call
+//    before any stream capture;
+//  * every call shares the one array and leaves its contents behind (each
+//    call writes all scratch it reads, so nothing needs clearing); calls that
+//    overlap on the GPU — on two streams, or from two threads — race.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[HPSI_NOALLOC_SCRATCH_BYTES];
+
+static int noalloc_scratch(hpsi_ctx* c, unsigned char** out)
+{
+    static std::mutex mu;
+    static void* ptrs[256] = {nullptr};
+    if (c->dev < 0 || c->dev >= 256) return fail(c, HPSI_ERR_BAD_ARG, "device ordinal %d out of range", c->dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[c->dev]) {
+        // host-side name of the array is a stand-in; its device address comes from the runtime
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(c, HPSI_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+        ptrs[c->dev] = p;
+    }
+    *out = static_cast<unsigned char*>(ptrs[c->dev]);
+    return HPSI_OK;
+}
+
+template <typename C, typename Acc, typename V>
+static int apply_noalloc_impl(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, const C* pr,
+                              const V* vloc, const C* tw, unsigned char* scratch, cudaStream_t st)
+{
+    const size_t cap = HPSI_NOALLOC_SCRATCH_BYTES;
+    Prof off;  // never records: creating events is not allowed here
+    // local term: bands in chunks whose FFT planes fit the scratch
+    const size_t plane_bytes = (size_t)s.nxs * c->n2 * c->n3 * sizeof(C);
+    if (plane_bytes > cap)
+        return fail(c, HPSI_ERR_BAD_ARG,
+                    "hpsi_apply_noalloc: one band's FFT planes need %zu bytes, above the %zu-byte scratch", plane_bytes,
+                    cap);
+    if (plane_bytes > 0) {
+        LocalArgs a{};
+        a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
+        a.npw = s.npw;
+        a.nxs = s.nxs;
+        a.kt = sizeof(C) == 16 ? 8 : 16;
+        a.inv_n = 1.0 / ((double)c->n1 * c->n2 * c->n3);
+        a.plane_x = s.d_plane;
+        a.plane_off = s.d_plane + s.nxs;
+        a.ent_ig = s.d_plane + 2 * s.nxs + 1;
+        a.ent_jk = s.d_plane + 2 * s.nxs + 1 + s.npw;
+        a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
+        const int ch = (int)std::min<size_t>((size_t)nb, cap / plane_bytes);
+        for (int b0 = 0; b0 < nb; b0 += ch) {
+            const int nbc = std::min(ch, nb - b0);
+            CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin,
+                                            reinterpret_cast<C*>(scratch), vloc, tw, tw + c->n1, tw + c->n1 + c->n2,
+                                            st, &off)));
+        }
+    }
+    // nonlocal term: bands in chunks whose partials and coefficients fit
+    if (s.P == 0) return HPSI_OK;
+    auto need = [&](int nbc, int* ns) {
+        *ns = split_for(s.P, nbc, s.npw);
+        Carver cv;
+        cv.take<Acc>((size_t)*ns * s.P * nbc);
+        cv.take<C>((size_t)s.P * nbc);
+        return cv.off;
+    };
+    int nbc = nb, ns = 1;
+    while (nbc > 1 && need(nbc, &ns) > cap) nbc = (nbc + 1) / 2;
+    if (need(nbc, &ns) > cap)
+        return fail(c, HPSI_ERR_BAD_ARG,
+                    "hpsi_apply_noalloc: %d projectors need %zu bytes of partial sums per band, above the %zu-byte "
+                    "scratch", s.P, need(1, &ns), cap);
+    for (int b0 = 0; b0 < nb; b0 += nbc) {
+        const int n = std::min(nbc, nb - b0);
+        if (need(n, &ns) > cap)
+            return fail(c, HPSI_ERR_BAD_ARG, "hpsi_apply_noalloc: %d bands of partial sums exceed the scratch", n);
+        Carver cv;
+        const size_t o_part = cv.take<Acc>((size_t)ns * s.P * n);
+        const size_t o_w = cv.take<C>((size_t)s.P * n);
+        Acc* part = reinterpret_cast<Acc*>(scratch + o_part);
+        C* W = reinterpret_cast<C*>(scratch + o_w);
+        CUDA_TRY(c, (launch_proj_gemm<C, double2, Acc>(s.P, n, s.npw, pr, (size_t)s.npw, psi + (size_t)b0 * s.npw,
+                                                       (size_t)s.npw, part, ns, st)));
+        CUDA_TRY(c, (launch_reduce_splits<Acc, C>(s.P, n, ns, part, s.d_lam, s.P, W, (size_t)n, st)));
+        CUDA_TRY(c, launch_expand_gemm<C>(s.P, n, s.npw, W, (size_t)n, pr, (size_t)s.npw, hpsi + (size_t)b0 * s.npw,
+                                          (size_t)s.npw, st));
+    }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_apply_noalloc(hpsi_ctx* c, int kid, int nb, const double* psi_, double* hpsi_, int flags,
+                                  void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (!(flags & HPSI_DEVICE_PTRS))
+        return fail(c, HPSI_ERR_BAD_ARG, "hpsi_apply_noalloc: psi/hpsi must be device pointers (HPSI_DEVICE_PTRS)");
+    if (nb > 0 && (!psi_ || !hpsi_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/hpsi NULL");
+    if (nb == 0 || s->npw == 0) return HPSI_OK;
+    const bool fp64 = (flags & HPSI_PREC_MASK) == HPSI_PREC_FP64;
+    if (s->P > 0 && !(fp64 ? (void*)s->pr64 : (void*)s->pr32))
+        return fail(c, HPSI_ERR_STATE,
+                    "hpsi_apply_noalloc: projector matrices of this precision are not built yet; one hpsi_apply or "
+                    "hpsi_grad_apply at this precision on k-point %d builds them", kid);
+    unsigned char* scratch = nullptr;
+    if ((rc = noalloc_scratch(c, &scratch))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2* psi = (const double2*)psi_;
+    double2* hpsi = (double2*)hpsi_;
+    rc = fp64 ? apply_noalloc_impl<double2, double2, double>(c, *s, nb, psi, hpsi, s->pr64, c->d_v64, c->d_tw64,
+                                                              scratch, st)
+              : apply_noalloc_impl<float2, float2, float>(c, *s, nb, psi, hpsi, s->pr32, c->d_v32, c->d_tw32, scratch,
+                                                           st);
+    if (rc) return rc;
+    if (flags & HPSI_SYNC) CUDA_TRY(c, cudaStreamSynchronize(st));
+    return HPSI_OK;
+}

@@ -132,6 +132,22 @@ int hpsi_grad_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi,
 int hpsi_velocity_matrix(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* m,
                          int flags, void* stream);
 
+/* hpsi_apply for callers that cannot allocate device memory during the call
+ * (a fixed device-memory budget, a host runtime whose allocator owns all
+ * device memory, or code that must not add an allocation's implicit device
+ * synchronisation).  No counterpart in the reference.  Same result as
+ * hpsi_apply; psi/hpsi must be device pointers (HPSI_DEVICE_PTRS).  All
+ * scratch lives in one static device array of HPSI_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library holds until exit; sizes that do not fit are
+ * rejected with HPSI_ERR_BAD_ARG.  The projector matrices of the precision
+ * must exist (built by a first hpsi_apply/hpsi_grad_apply at that precision),
+ * else HPSI_ERR_STATE.  The first call on a device looks up the array's
+ * address (make it before any stream capture).  Calls share the array:
+ * calls that overlap on the GPU race. */
+#define HPSI_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int hpsi_apply_noalloc(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
+                       int flags, void* stream);
+
 /* Per-phase CUDA-event profile of the device work queued by later calls
  * (instrumentation for benchmarks; off by default).  hpsi_profile(ctx, on)
  * resets the record and switches it on or off; hpsi_profile_read waits for
