@@ -27,15 +27,18 @@ struct FftLen {
     int rad[HPSI_FFT_MAXST];
 };
 
-// Factor n into stage radices, preferring 4 over 2*2.  Returns false if n has
-// a prime factor above HPSI_FFT_MAXR or n exceeds HPSI_FFT_MAXN.
+// Factor n into stage radices, preferring the composite radices 8 and 9
+// (fewest stages: 72 = 8*9), then 4, then primes.  Returns false if n has a
+// prime factor above HPSI_FFT_MAXR or n exceeds HPSI_FFT_MAXN.
 static inline bool fft_factor(int n, FftLen* L)
 {
     L->n = n;
     L->nst = 0;
     if (n < 1 || n > HPSI_FFT_MAXN) return false;
     int m = n;
-    while (m % 4 == 0) { L->rad[L->nst++] = 4; m /= 4; }
+    const int pref[3] = {8, 9, 4};
+    for (int r : pref)
+        while (m % r == 0 && L->nst < HPSI_FFT_MAXST) { L->rad[L->nst++] = r; m /= r; }
     for (int p = 2; p <= HPSI_FFT_MAXR && m > 1; ++p) {
         while (m % p == 0) {
             if (L->nst >= HPSI_FFT_MAXST) return false;
@@ -55,12 +58,83 @@ HPSI_D C tw_get(const C* tw, int j, int sign)
     return w;
 }
 
+// 3-point DFT of (a, b, c) in place with W_3 = exp(sign*2*pi*i/3)
+template <typename C>
+HPSI_D void dft3(C& a, C& b, C& c, int sign)
+{
+    using R = typename Real<C>::type;
+    const R h = (R)0.86602540378443864676;  // sin(2 pi/3)
+    C s = cadd(b, c), d = csub(b, c);
+    C a0 = a;
+    a = cadd(a0, s);
+    C m = cmake<C>(a0.x - (R)0.5 * s.x, a0.y - (R)0.5 * s.y);
+    // +/- i*sign*h*d
+    C t = cmake<C>(-(R)sign * h * d.y, (R)sign * h * d.x);
+    b = cadd(m, t);
+    c = csub(m, t);
+}
+
+// 4-point DFT of v[o], v[o+st], v[o+2st], v[o+3st] in place
+template <typename C>
+HPSI_D void dft4_at(C* v, int o, int st, int sign)
+{
+    C a0 = cadd(v[o], v[o + 2 * st]), a1 = csub(v[o], v[o + 2 * st]);
+    C b0 = cadd(v[o + st], v[o + 3 * st]), b1 = cmul_i(csub(v[o + st], v[o + 3 * st]), sign);
+    v[o] = cadd(a0, b0);
+    v[o + 2 * st] = csub(a0, b0);
+    v[o + st] = cadd(a1, b1);
+    v[o + 3 * st] = csub(a1, b1);
+}
+
 // p-point DFT of v[0..p) in registers: v[q] <- sum_r v[r] W_p^{r q}
 template <typename C, int P>
 HPSI_D void dft_small(C (&v)[HPSI_FFT_MAXR], const C* tw, int n, int sign)
 {
     using R = typename Real<C>::type;
-    if constexpr (P == 2) {
+    if constexpr (P == 3) {
+        dft3(v[0], v[1], v[2], sign);
+    } else if constexpr (P == 8) {
+        // 8 = 2 x 4: x[2 n1 + n2]; inner 4-point DFTs over n1 (even / odd),
+        // twiddle the odd one by W_8^{k1}, then 2-point DFTs
+        C e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+        dft4_at(e, 0, 1, sign);
+        dft4_at(o, 0, 1, sign);
+        const R r2 = (R)0.70710678118654752440;
+        // W_8^1 = (r2, sign r2), W_8^2 = sign i, W_8^3 = (-r2, sign r2)
+        o[1] = cmul(o[1], cmake<C>(r2, (R)sign * r2));
+        o[2] = cmul_i(o[2], sign);
+        o[3] = cmul(o[3], cmake<C>(-r2, (R)sign * r2));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[k] = cadd(e[k], o[k]);
+            v[k + 4] = csub(e[k], o[k]);
+        }
+    } else if constexpr (P == 9) {
+        // 9 = 3 x 3: x[3 n1 + n2]; inner 3-point DFTs over n1, twiddle by
+        // W_9^{n2 k1}, then 3-point DFTs over n2; output index k1 + 3 k2
+        C y[9];
+#pragma unroll
+        for (int n2 = 0; n2 < 3; ++n2) {
+            C a = v[n2], b = v[3 + n2], c = v[6 + n2];
+            dft3(a, b, c, sign);
+            y[3 * n2] = a;
+            y[3 * n2 + 1] = b;
+            y[3 * n2 + 2] = c;
+        }
+        const int step = n / 9;
+        y[4] = cmul(y[4], tw_get(tw, 1 * step, sign));
+        y[5] = cmul(y[5], tw_get(tw, 2 * step, sign));
+        y[7] = cmul(y[7], tw_get(tw, 2 * step, sign));
+        y[8] = cmul(y[8], tw_get(tw, 4 * step, sign));
+#pragma unroll
+        for (int k1 = 0; k1 < 3; ++k1) {
+            C a = y[k1], b = y[3 + k1], c = y[6 + k1];
+            dft3(a, b, c, sign);
+            v[k1] = a;
+            v[k1 + 3] = b;
+            v[k1 + 6] = c;
+        }
+    } else if constexpr (P == 2) {
         C a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
@@ -126,6 +200,8 @@ template <typename C, bool LINE_FAST>
 HPSI_D void fft_stage(const C* src, C* dst, int p, int n, int Ns, int nl, int ls, int es, const C* tw, int sign)
 {
     switch (p) {
+        case 8: fft_stage_p<C, 8, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
+        case 9: fft_stage_p<C, 9, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
         case 2: fft_stage_p<C, 2, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
         case 3: fft_stage_p<C, 3, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
         case 4: fft_stage_p<C, 4, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;

@@ -236,7 +236,7 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
     }
     // plane FFT kernels keep two n2*n3 planes in shared memory
     LocalArgs la{};
-    la.n1 = c->n1; la.n2 = c->n2; la.n3 = c->n3; la.kt = 8;
+    la.n1 = c->n1; la.n2 = c->n2; la.n3 = c->n3;
     if (local_smem_bytes(la, true) > 227 * 1024)
         return fail(c, HPSI_ERR_BAD_ARG, "FFT grid %dx%dx%d: two complex128 n2*n3 planes exceed shared memory", c->n1, c->n2, c->n3);
 
@@ -537,7 +537,7 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
     a.npw = s.npw;
     a.nxs = s.nxs;
-    a.kt = sizeof(C) == 16 ? 8 : 16;
+    local_xpass_shape(&a, sizeof(C));
     a.inv_n = 1.0 / ((double)c->n1 * c->n2 * c->n3);
     a.plane_x = pl;
     a.plane_off = pl + s.nxs;
@@ -848,7 +848,7 @@ static int apply_noalloc_impl(hpsi_ctx* c, KSlot& s, int nb, const double2* psi,
         a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
         a.npw = s.npw;
         a.nxs = s.nxs;
-        a.kt = sizeof(C) == 16 ? 8 : 16;
+        local_xpass_shape(&a, sizeof(C));
         a.inv_n = 1.0 / ((double)c->n1 * c->n2 * c->n3);
         a.plane_x = s.d_plane;
         a.plane_off = s.d_plane + s.nxs;

@@ -54,7 +54,8 @@ struct LocalArgs {
     int n1, n2, n3;
     int npw;
     int nxs;                // x-planes that hold sphere points
-    int kt;                 // x-lines per block in the x pass
+    int kt;                 // z-values per block in the x pass
+    int bb;                 // bands per block in the x pass
     double inv_n;           // 1/(n1*n2*n3): the R2G normalisation
     const int* plane_x;     // [nxs] grid x index of plane p
     const int* plane_off;   // [nxs+1] entry range of plane p
@@ -64,6 +65,8 @@ struct LocalArgs {
 };
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64);
+// choose kt/bb of the x pass for complex size csize (bytes)
+void local_xpass_shape(LocalArgs* a, size_t csize);
 
 template <typename C, typename V>
 cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,

@@ -20,79 +20,97 @@
 #include "fft.cuh"
 #include "kernels.cuh"
 
+// Shared-memory planes use a padded row stride n3p = n3 + 1 (odd) so that
+// both the z-lines (rows) and the y-lines (columns) are read and written by
+// consecutive threads without bank conflicts (both transforms walk lines
+// fastest: LINE_FAST).
 template <typename C>
 __global__ void __launch_bounds__(256) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n2 = a.n2, n3 = a.n3, n23 = n2 * n3;
+    const int n2 = a.n2, n3 = a.n3, n3p = n3 + 1, n23 = n2 * n3, n23p = n2 * n3p;
     C* b0 = reinterpret_cast<C*>(smem_raw);
-    C* b1 = b0 + n23;
-    C* twy = b1 + n23;
+    C* b1 = b0 + n23p;
+    C* twy = b1 + n23p;
     C* twz = twy + n2;
     const int p = blockIdx.x;
     const int b = blockIdx.y;
     for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
     for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
-    for (int t = threadIdx.x; t < n23; t += blockDim.x) b0[t] = cmake<C>(0, 0);
+    for (int t = threadIdx.x; t < n23p; t += blockDim.x) b0[t] = cmake<C>(0, 0);
     __syncthreads();
     const double2* ps = psi + (size_t)b * a.npw;
     const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         int ig = a.ent_ig[e];
-        if (ig >= 0) b0[a.ent_jk[e]] = from_c128<C>(ps[ig]);
+        if (ig >= 0) {
+            int jk = a.ent_jk[e];
+            int j = jk / n3, k = jk - j * n3;
+            b0[j * n3p + k] = from_c128<C>(ps[ig]);
+        }
     }
     __syncthreads();
-    int cur = fft_lines<C, false>(b0, b1, 0, a.Lz, n2, n3, 1, twz, +1);
-    cur = fft_lines<C, true>(b0, b1, cur, a.Ly, n3, 1, n3, twy, +1);
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Lz, n2, n3p, 1, twz, +1);
+    cur = fft_lines<C, true>(b0, b1, cur, a.Ly, n3, 1, n3p, twy, +1);
     const C* res = cur ? b1 : b0;
     C* out = T + ((size_t)b * a.nxs + p) * n23;
-    for (int t = threadIdx.x; t < n23; t += blockDim.x) out[t] = res[t];
+    for (int t = threadIdx.x; t < n23; t += blockDim.x) {
+        int j = t / n3, k = t - j * n3;
+        out[t] = res[j * n3p + k];
+    }
 }
 
+// x pass: a block owns the x-lines of (j, k0..k0+KT) for BB consecutive bands
+// (NL = KT*BB lines, line L = bb*KT + kk, element x at [x*NL + L]); the V tile
+// is loaded once per block.
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
                                               const C* __restrict__ tw_x_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n1 = a.n1, n2 = a.n2, n3 = a.n3, KT = a.kt;
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3, KT = a.kt, BB = a.bb, NL = KT * BB;
     C* b0 = reinterpret_cast<C*>(smem_raw);
-    C* b1 = b0 + n1 * KT;
-    C* twx = b1 + n1 * KT;
+    C* b1 = b0 + n1 * NL;
+    C* twx = b1 + n1 * NL;
     V* vt = reinterpret_cast<V*>(twx + n1);
     const int j = blockIdx.y;
     const int k0 = blockIdx.x * KT;
     const int kt = min(KT, n3 - k0);
+    const int bb0 = blockIdx.z * BB;
+    const int nbb = min(BB, nb - bb0);
     const int nxs = a.nxs;
+    const size_t plane = (size_t)n2 * n3;
     for (int t = threadIdx.x; t < n1; t += blockDim.x) twx[t] = tw_x_g[t];
     for (int t = threadIdx.x; t < n1 * kt; t += blockDim.x) {
         int x = t / kt, kk = t % kt;
         vt[x * KT + kk] = vloc[((size_t)x * n2 + j) * n3 + k0 + kk];
     }
-    const size_t plane = (size_t)n2 * n3;
-    for (int b = 0; b < nb; ++b) {
-        for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) b0[t] = cmake<C>(0, 0);
-        __syncthreads();
-        C* Tb = T + (size_t)b * nxs * plane + (size_t)j * n3 + k0;
-        for (int t = threadIdx.x; t < nxs * kt; t += blockDim.x) {
-            int pp = t / kt, kk = t % kt;
-            b0[a.plane_x[pp] * KT + kk] = Tb[(size_t)pp * plane + kk];
-        }
-        __syncthreads();
-        int cur = fft_lines<C, true>(b0, b1, 0, a.Lx, kt, 1, KT, twx, +1);
-        C* res = cur ? b1 : b0;
-        for (int t = threadIdx.x; t < n1 * kt; t += blockDim.x) {
-            int x = t / kt, kk = t % kt;
-            res[x * KT + kk] = cscale(res[x * KT + kk], (typename Real<C>::type)vt[x * KT + kk]);
-        }
-        __syncthreads();
-        cur = fft_lines<C, true>(b0, b1, cur, a.Lx, kt, 1, KT, twx, -1);
-        res = cur ? b1 : b0;
-        for (int t = threadIdx.x; t < nxs * kt; t += blockDim.x) {
-            int pp = t / kt, kk = t % kt;
-            Tb[(size_t)pp * plane + kk] = res[a.plane_x[pp] * KT + kk];
-        }
-        __syncthreads();
+    for (int t = threadIdx.x; t < n1 * NL; t += blockDim.x) b0[t] = cmake<C>(0, 0);
+    __syncthreads();
+    const int per_plane = nbb * kt;
+    for (int t = threadIdx.x; t < nxs * per_plane; t += blockDim.x) {
+        int pp = t / per_plane, r = t - pp * per_plane;
+        int bb = r / kt, kk = r - bb * kt;
+        const C* src = T + ((size_t)(bb0 + bb) * nxs + pp) * plane + (size_t)j * n3 + k0 + kk;
+        b0[a.plane_x[pp] * NL + bb * KT + kk] = *src;
+    }
+    __syncthreads();
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Lx, NL, 1, NL, twx, +1);
+    C* res = cur ? b1 : b0;
+    for (int t = threadIdx.x; t < n1 * NL; t += blockDim.x) {
+        int x = t / NL, L = t - x * NL;
+        int kk = L % KT;
+        res[t] = cscale(res[t], (typename Real<C>::type)vt[x * KT + kk]);
+    }
+    __syncthreads();
+    cur = fft_lines<C, true>(b0, b1, cur, a.Lx, NL, 1, NL, twx, -1);
+    res = cur ? b1 : b0;
+    for (int t = threadIdx.x; t < nxs * per_plane; t += blockDim.x) {
+        int pp = t / per_plane, r = t - pp * per_plane;
+        int bb = r / kt, kk = r - bb * kt;
+        C* dst = T + ((size_t)(bb0 + bb) * nxs + pp) * plane + (size_t)j * n3 + k0 + kk;
+        *dst = res[a.plane_x[pp] * NL + bb * KT + kk];
     }
 }
 
@@ -102,27 +120,32 @@ __global__ void __launch_bounds__(256) r2g_planes(LocalArgs a, const C* __restri
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n2 = a.n2, n3 = a.n3, n23 = n2 * n3;
+    const int n2 = a.n2, n3 = a.n3, n3p = n3 + 1, n23 = n2 * n3, n23p = n2 * n3p;
     C* b0 = reinterpret_cast<C*>(smem_raw);
-    C* b1 = b0 + n23;
-    C* twy = b1 + n23;
+    C* b1 = b0 + n23p;
+    C* twy = b1 + n23p;
     C* twz = twy + n2;
     const int p = blockIdx.x;
     const int b = blockIdx.y;
     for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
     for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
     const C* in = T + ((size_t)b * a.nxs + p) * n23;
-    for (int t = threadIdx.x; t < n23; t += blockDim.x) b0[t] = in[t];
+    for (int t = threadIdx.x; t < n23; t += blockDim.x) {
+        int j = t / n3, k = t - j * n3;
+        b0[j * n3p + k] = in[t];
+    }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Ly, n3, 1, n3, twy, -1);
-    cur = fft_lines<C, false>(b0, b1, cur, a.Lz, n2, n3, 1, twz, -1);
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Ly, n3, 1, n3p, twy, -1);
+    cur = fft_lines<C, true>(b0, b1, cur, a.Lz, n2, n3p, 1, twz, -1);
     const C* res = cur ? b1 : b0;
     const double2* ps = psi + (size_t)b * a.npw;
     double2* hp = hpsi + (size_t)b * a.npw;
     const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         int ig = a.ent_ig[e] & 0x7fffffff;
-        double2 g = as_c128(res[a.ent_jk[e]]);
+        int jk = a.ent_jk[e];
+        int j = jk / n3, k = jk - j * n3;
+        double2 g = as_c128(res[j * n3p + k]);
         double2 s = ps[ig];
         double kin = kinetic[ig];
         double2 h = hp[ig];
@@ -135,20 +158,36 @@ __global__ void __launch_bounds__(256) r2g_planes(LocalArgs a, const C* __restri
 template <typename C>
 static size_t plane_smem(const LocalArgs& a)
 {
-    return sizeof(C) * (2 * (size_t)a.n2 * a.n3 + a.n2 + a.n3);
+    return sizeof(C) * (2 * (size_t)a.n2 * (a.n3 + 1) + a.n2 + a.n3);
 }
 
 template <typename C, typename V>
 static size_t xpass_smem(const LocalArgs& a)
 {
-    return sizeof(C) * (2 * (size_t)a.n1 * a.kt + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt;
+    const size_t NL = (size_t)a.kt * a.bb;
+    return sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt;
 }
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64)
 {
-    size_t p = fp64 ? plane_smem<double2>(a) : plane_smem<float2>(a);
-    size_t x = fp64 ? xpass_smem<double2, double>(a) : xpass_smem<float2, float>(a);
+    LocalArgs b = a;
+    local_xpass_shape(&b, fp64 ? sizeof(double2) : sizeof(float2));
+    size_t p = fp64 ? plane_smem<double2>(b) : plane_smem<float2>(b);
+    size_t x = fp64 ? xpass_smem<double2, double>(b) : xpass_smem<float2, float>(b);
     return p > x ? p : x;
+}
+
+// x-pass block shape: about 96 KB of line buffers, at most 8 z-values per
+// block, the rest filled with bands.
+void local_xpass_shape(LocalArgs* a, size_t csize)
+{
+    const size_t budget = 96 * 1024;
+    int nlmax = (int)(budget / (2 * (size_t)a->n1 * csize));
+    if (nlmax < 1) nlmax = 1;
+    a->kt = nlmax < 8 ? nlmax : 8;
+    if (a->kt > a->n3) a->kt = a->n3;
+    a->bb = nlmax / a->kt;
+    if (a->bb < 1) a->bb = 1;
 }
 
 template <typename C, typename V>
@@ -165,7 +204,7 @@ cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2
     int h = prof->open(PH_G2R, st);
     g2r_planes<C><<<gp, 256, sp, st>>>(a, psi, T, twy, twz);
     prof->close(h, st);
-    dim3 gx(ceil_div(a.n3, a.kt), a.n2);
+    dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
     x_pass<C, V><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
     prof->close(h, st);
