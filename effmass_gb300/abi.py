@@ -23,11 +23,12 @@ HPSI_ERR_STATE = -6
 HPSI_PREC_FP64 = 0
 HPSI_PREC_FP32 = 1
 HPSI_PREC_TC = 2
+HPSI_PREC_TC_BF16 = 3
 HPSI_DEVICE_PTRS = 0x10
 HPSI_SYNC = 0x20
 HPSI_NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
-PRECISIONS = {"fp64": HPSI_PREC_FP64, "fp32": HPSI_PREC_FP32, "tc": HPSI_PREC_TC}
+PRECISIONS = {"fp64": HPSI_PREC_FP64, "fp32": HPSI_PREC_FP32, "tc": HPSI_PREC_TC, "tc_bf16": HPSI_PREC_TC_BF16}
 
 STATUS_NAMES = {0: "OK", -1: "BAD_ARG", -2: "OOM", -3: "RANGE", -4: "TIMEOUT", -5: "CUDA", -6: "STATE"}
 

@@ -21,6 +21,7 @@
 
 #include "../../include/hpsi_gb300.h"
 #include "kernels.cuh"
+#include "tc_gemm.cuh"
 
 namespace {
 
@@ -46,6 +47,10 @@ struct KSlot {
     bool pr64_grad = false;
     float2* pr32 = nullptr;
     bool pr32_grad = false;
+    // tensor-core operands (built from pr32 on first use of a TC precision)
+    int tc_fmt = -1;               // -1 none, 0 FP16 split, 1 BF16 split
+    unsigned char* tc_mem = nullptr;
+    TcOperand tc_proj, tc_expand;
 };
 
 template <typename T>
@@ -67,7 +72,7 @@ void slot_free(KSlot& s)
 {
     dfree(s.d_kin); dfree(s.d_kvec); dfree(s.d_g); dfree(s.d_q); dfree(s.d_trig); dfree(s.d_ylm);
     dfree(s.d_beta); dfree(s.d_dbeta0); dfree(s.d_sf); dfree(s.d_plane); dfree(s.d_rows); dfree(s.d_lam);
-    dfree(s.pr64); dfree(s.pr32);
+    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem);
     s = KSlot();
 }
 
@@ -94,6 +99,7 @@ struct hpsi_ctx {
     unsigned char* ws = nullptr;
     size_t ws_size = 0;
     Prof prof;
+    int* d_err = nullptr;         // device-side error flag of the bounded waits (tcgen05 GEMMs)
     std::string err;
 };
 
@@ -158,7 +164,7 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     cudaSetDevice(c->dev);
     for (auto& kv : c->slots) slot_free(kv.second);
     dfree(c->d_tables); dfree(c->d_rad_nq); dfree(c->d_rad_dq); dfree(c->d_tau); dfree(c->d_v64); dfree(c->d_v32);
-    dfree(c->d_tw64); dfree(c->d_tw32);
+    dfree(c->d_tw64); dfree(c->d_tw32); dfree(c->d_err);
     if (c->ws) cudaFree(c->ws);
     for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof.pool) cudaEventDestroy(e);
@@ -241,6 +247,8 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
         return fail(c, HPSI_ERR_BAD_ARG, "FFT grid %dx%dx%d: two complex128 n2*n3 planes exceed shared memory", c->n1, c->n2, c->n3);
 
     CUDA_TRY(c, cudaGetDevice(&c->dev));
+    CUDA_TRY(c, dalloc(&c->d_err, (size_t)1));
+    CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
     const size_t N = (size_t)c->n1 * c->n2 * c->n3;
     CUDA_TRY(c, dalloc(&c->d_v64, N));
     CUDA_TRY(c, dalloc(&c->d_v32, N));
@@ -567,13 +575,100 @@ static int check_call(hpsi_ctx* c, int kid, int nb, KSlot** sp, int flags)
     if (!c) return HPSI_ERR_BAD_ARG;
     if (nb < 0) return fail(c, HPSI_ERR_BAD_ARG, "nb < 0");
     int prec = flags & HPSI_PREC_MASK;
-    if (prec != HPSI_PREC_FP64 && prec != HPSI_PREC_FP32 && prec != HPSI_PREC_TC)
+    if (prec != HPSI_PREC_FP64 && prec != HPSI_PREC_FP32 && prec != HPSI_PREC_TC && prec != HPSI_PREC_TC_BF16)
         return fail(c, HPSI_ERR_BAD_ARG, "unknown precision %d", prec);
     KSlot* s = get_slot(c, kid);
     if (!s) return fail(c, HPSI_ERR_STATE, "k-point slot %d is not bound", kid);
     *sp = s;
     cudaError_t e = cudaSetDevice(c->dev);
     if (e) return fail(c, HPSI_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    return HPSI_OK;
+}
+
+// ---- tensor-core nonlocal term ----------------------------------------------
+static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
+{
+    if (s.P == 0 || s.npw == 0) return HPSI_OK;
+    if (s.tc_fmt == fmt && s.tc_mem) return HPSI_OK;
+    int rc;
+    if ((rc = ensure_proj<float2>(c, s, false, st))) return rc;
+    dfree(s.tc_mem);
+    s.tc_fmt = -1;
+    const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(2 * (size_t)s.P);
+    Carver cv;
+    const size_t o1h = cv.take<uint16_t>((size_t)s.P * k1), o1l = cv.take<uint16_t>((size_t)s.P * k1);
+    const size_t o1s = cv.take<float>((size_t)s.P);
+    const size_t o2h = cv.take<uint16_t>((size_t)s.npw * k2), o2l = cv.take<uint16_t>((size_t)s.npw * k2);
+    const size_t o2s = cv.take<float>((size_t)s.npw);
+    const size_t ocm = cv.take<float>((size_t)s.npw);
+    CUDA_TRY(c, dalloc(&s.tc_mem, cv.off));
+    CUDA_TRY(c, cudaMemsetAsync(s.tc_mem + o2h, 0, o2s - o2h, st));  // K padding of Pr^T must read as zero
+    s.tc_proj = TcOperand{s.tc_mem + o1h, s.tc_mem + o1l, reinterpret_cast<float*>(s.tc_mem + o1s), k1};
+    s.tc_expand = TcOperand{s.tc_mem + o2h, s.tc_mem + o2l, reinterpret_cast<float*>(s.tc_mem + o2s), k2};
+    int h = c->prof.open(PH_BUILD, st);
+    CUDA_TRY(c, tc_build_proj_operands(s.pr32, s.P, s.npw, fmt == 0, &s.tc_proj, &s.tc_expand,
+                                       reinterpret_cast<float*>(s.tc_mem + ocm), st));
+    c->prof.close(h, st);
+    s.tc_fmt = fmt;
+    return HPSI_OK;
+}
+
+static size_t tc_ws(const KSlot& s, int nb)
+{
+    const int NB = tc_band_rows(nb);
+    const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(2 * (size_t)s.P);
+    const int ns = tc_proj_splits(s.P, nb, k1);
+    Carver cv;
+    cv.take<uint16_t>((size_t)NB * k1);
+    cv.take<uint16_t>((size_t)NB * k1);
+    cv.take<float>((size_t)NB);
+    cv.take<float>((size_t)ns * s.P * NB);
+    cv.take<float2>((size_t)s.P * nb);
+    cv.take<uint16_t>((size_t)NB * k2);
+    cv.take<uint16_t>((size_t)NB * k2);
+    cv.take<float>((size_t)NB);
+    return cv.off;
+}
+
+static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
+                       cudaStream_t st)
+{
+    if (s.P == 0 || nb == 0) return HPSI_OK;
+    const bool fp16 = s.tc_fmt == 0;
+    const int NB = tc_band_rows(nb);
+    const size_t k1 = s.tc_proj.ldk, k2 = s.tc_expand.ldk;
+    const int ns = tc_proj_splits(s.P, nb, k1);
+    Carver cv;
+    const size_t ob1h = cv.take<uint16_t>((size_t)NB * k1), ob1l = cv.take<uint16_t>((size_t)NB * k1);
+    const size_t ob1s = cv.take<float>((size_t)NB);
+    const size_t opart = cv.take<float>((size_t)ns * s.P * NB);
+    const size_t ow = cv.take<float2>((size_t)s.P * nb);
+    const size_t ob2h = cv.take<uint16_t>((size_t)NB * k2), ob2l = cv.take<uint16_t>((size_t)NB * k2);
+    const size_t ob2s = cv.take<float>((size_t)NB);
+    TcOperand B1{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
+    TcOperand B2{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
+    float2* W = reinterpret_cast<float2*>(ws + ow);
+    int h = c->prof.open(PH_OTHER, st);
+    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &B1, st));
+    c->prof.close(h, st);
+    CUDA_TRY(c, tc_projection(s.tc_proj, s.P, B1, nb, ns, fp16, reinterpret_cast<float*>(ws + opart), s.d_lam, s.P, W,
+                              c->d_err, st, &c->prof));
+    h = c->prof.open(PH_OTHER, st);
+    CUDA_TRY(c, tc_w_operand(W, s.P, nb, fp16, &B2, st));
+    c->prof.close(h, st);
+    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, B2, nb, fp16, hpsi, c->d_err, st, &c->prof));
+    return HPSI_OK;
+}
+
+// After a synchronising call: report a bounded-wait timeout of the tensor-core kernels.
+static int check_device_flag(hpsi_ctx* c)
+{
+    int v = 0;
+    CUDA_TRY(c, cudaMemcpy(&v, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) {
+        cudaMemset(c->d_err, 0, sizeof(int));
+        return fail(c, HPSI_ERR_TIMEOUT, "tensor-core GEMM: a bounded pipeline wait gave up (site %d)", v);
+    }
     return HPSI_OK;
 }
 
@@ -594,8 +689,10 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
     size_t o_psi = dev ? 0 : cv.take<double2>(nel);
     size_t o_hpsi = dev ? 0 : cv.take<double2>(nel);
     size_t o_work = cv.off;
+    const bool tc = prec == HPSI_PREC_TC || prec == HPSI_PREC_TC_BF16;
     size_t wl = local_ws(c, *s, nb, fp64 ? sizeof(double2) : sizeof(float2));
-    size_t wn = fp64 ? nonlocal_ws<double2, double2>(*s, nb, 1) : nonlocal_ws<float2, float2>(*s, nb, 1);
+    size_t wn = fp64 ? nonlocal_ws<double2, double2>(*s, nb, 1)
+                     : (tc ? tc_ws(*s, nb) : nonlocal_ws<float2, float2>(*s, nb, 1));
     if ((rc = ws_reserve(c, o_work + std::max(wl, wn)))) return rc;
     const double2* psi = (const double2*)psi_;
     double2* hpsi = (double2*)hpsi_;
@@ -610,13 +707,20 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
         if ((rc = ensure_proj<double2>(c, *s, false, st))) return rc;
         if ((rc = local_apply<double2, double>(c, *s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st))) return rc;
         if ((rc = nonlocal_apply<double2, double2>(c, *s, nb, psi, hpsi, s->pr64, work, st))) return rc;
+    } else if (tc) {
+        if ((rc = ensure_tc(c, *s, prec == HPSI_PREC_TC ? 0 : 1, st))) return rc;
+        if ((rc = local_apply<float2, float>(c, *s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
+        if ((rc = tc_nonlocal(c, *s, nb, psi, hpsi, work, st))) return rc;
     } else {
         if ((rc = ensure_proj<float2>(c, *s, false, st))) return rc;
         if ((rc = local_apply<float2, float>(c, *s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
         if ((rc = nonlocal_apply<float2, float2>(c, *s, nb, psi, hpsi, s->pr32, work, st))) return rc;
     }
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
-    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (!dev || (flags & HPSI_SYNC)) {
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        if (tc && (rc = check_device_flag(c))) return rc;
+    }
     return HPSI_OK;
 }
 

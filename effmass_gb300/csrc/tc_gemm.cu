@@ -1,0 +1,648 @@
+// tc_gemm.cu — tensor-core (tcgen05) projector GEMMs for the nonlocal term.
+//
+// Both nonlocal GEMMs are cast as real "TN" GEMMs C[m][n] = sum_k A[m][k] B[n][k]
+// with K-major operands:
+//   projection  A = Pr      [P][2*npw]  (interleaved re/im of each projector row)
+//               B = Psi'    [NB][2*npw] rows (psi_r, psi_i) and (psi_i, -psi_r)
+//               C[p][.]     -> W[p][b] = lambda_p (C[p][re b] + i C[p][im b])
+//   expansion   A = Pr^T    [npw][2*P]   (row g: (Pr_r, Pr_i)[p] interleaved)
+//               B = W'      [NB][2*P]    rows (W_r, -W_i) and (W_i, W_r)
+//               C[g][.]     -> hpsi[b][g] += C[g][re b] + i C[g][im b]
+// Band rows are blocked by 128: row (t*256 + c*128 + j) holds band 128t+j, part c
+// (0 = re, 1 = im), so an N tile of 256 holds both parts of 128 bands.
+//
+// Precision: every operand x is split as x*2^s = hi + lo in FP16 (s a per-row
+// power of two that puts the row maximum at ~2^14) or in BF16 (s = 0); the
+// product uses three MMAs hi*hi + hi*lo + lo*hi with FP32 accumulation in
+// TMEM, and the epilogue removes 2^-(s_a + s_b).  FP16 pieces carry 11
+// significand bits each, so hi+lo represents x to ~2^-22; BF16 pieces to ~2^-18.
+//
+// Kernel: one 128 x 256 output tile per CTA (cta_group::1, UMMA M=128, N=256,
+// K=16), 64-deep K stages loaded by TMA (SWIZZLE_128B) into two pipeline
+// stages of A_hi, A_lo, B_hi, B_lo; warp 0 issues TMA, warp 1 owns TMEM and
+// issues the MMAs from one thread, warps 2-5 drain TMEM.  Every mbarrier wait
+// is bounded; on timeout the CTA sets an error flag, drains and frees TMEM.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include "kernels.cuh"
+#include "tc_gemm.cuh"
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
+constexpr int A_TILE = BM * BK * 2;   // bytes of one A piece per stage (16 KB)
+constexpr int B_TILE = BN * BK * 2;   // 32 KB
+constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false after WAIT_LIMIT polls (about a second)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (i > 32) __nanosleep(40);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// SMEM matrix descriptor for a K-major tile written by TMA with SWIZZLE_128B:
+// 8-row x 128-byte swizzle atoms stacked along M/N every 1024 bytes (SBO);
+// LBO is not used by swizzled K-major layouts (encoded as 1).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version of sm_100-class tensor cores
+    d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = F16 (fmt 0) or BF16
+// (fmt 1), both K-major, no negation, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N, uint32_t fmt)
+{
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcSmem {
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+    uint64_t done;
+    uint32_t tmem_base;
+    uint32_t abort_flag;
+};
+
+// Epilogue modes
+//   0: projection partials  part[z][m][n] = C * 2^-(sa[m] + sb[n])   (row-major, ldp = N)
+//   1: expansion            hpsi[b][g] += (C[g][re] + i C[g][im]) * 2^-(sa[g] + sb[b])
+template <int MODE>
+__global__ void __launch_bounds__(192, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                   const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, TcEpilogue ep,
+                   int M, int N, int ktiles_total, int ktiles_per_split, uint32_t idesc, int* err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // 1024-byte aligned tile area
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    TcSmem* sh = reinterpret_cast<TcSmem*>(tiles + STAGES * STAGE_BYTES);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    const int kt0 = blockIdx.z * ktiles_per_split;
+    const int kt1 = min(ktiles_total, kt0 + ktiles_per_split);
+    const int nk = max(0, kt1 - kt0);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->empty[s], 1);
+        }
+        mbar_init(&sh->done, 1);
+        sh->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer
+        int issued = 0;
+        for (int it = 0; it < nk; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (it / STAGES) & 1;
+            if (!mbar_wait(&sh->empty[s], ph ^ 1)) { atomicExch(err, 1); sh->abort_flag = 1; break; }
+            if (*(volatile uint32_t*)&sh->abort_flag) break;
+            unsigned char* st = tiles + s * STAGE_BYTES;
+            mbar_arrive_expect_tx(&sh->full[s], STAGE_BYTES);
+            const int kx = (kt0 + it) * BK;
+            tma_load_2d(st, &tmAh, kx, m0, &sh->full[s]);
+            tma_load_2d(st + A_TILE, &tmAl, kx, m0, &sh->full[s]);
+            tma_load_2d(st + 2 * A_TILE, &tmBh, kx, n0, &sh->full[s]);
+            tma_load_2d(st + 2 * A_TILE + B_TILE, &tmBl, kx, n0, &sh->full[s]);
+            issued = it + 1;
+        }
+        // drain: copies in flight must land before the CTA exits (bounded)
+        for (int it = max(0, issued - STAGES); it < issued; ++it)
+            mbar_wait(&sh->full[it % STAGES], (it / STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        bool ok = true;
+        for (int it = 0; it < nk; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (it / STAGES) & 1;
+            if (!mbar_wait(&sh->full[s], ph)) { atomicExch(err, 2); sh->abort_flag = 1; ok = false; break; }
+            tc_fence_after();
+            const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
+            const uint64_t ah = sdesc_sw128(st), al = sdesc_sw128(st + A_TILE);
+            const uint64_t bh = sdesc_sw128(st + 2 * A_TILE), bl = sdesc_sw128(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t adv = (uint64_t)((kk * 32) >> 4);  // 16 elements = 32 bytes along K
+                const uint32_t first = (it == 0 && kk == 0) ? 0u : 1u;
+                tc_mma(tmem, ah + adv, bh + adv, idesc, first);
+                tc_mma(tmem, ah + adv, bl + adv, idesc, 1u);
+                tc_mma(tmem, al + adv, bh + adv, idesc, 1u);
+            }
+            tc_commit(&sh->empty[s]);  // stage reusable once these MMAs have read it
+        }
+        (void)ok;
+        tc_commit(&sh->done);  // accumulator final (arrives after all prior MMAs)
+    } else if (warp >= 2) {
+        // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
+        const int q = warp & 3;
+        const int row = m0 + q * 32 + lane;
+        bool ok = mbar_wait(&sh->done, 0);
+        tc_fence_after();
+        if (!ok) atomicExch(err, 3);
+        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
+        // warp-uniform decision: tcgen05.ld is a .sync.aligned warp instruction
+        const bool go = __all_sync(0xffffffffu, ok && nk > 0 && !*(volatile uint32_t*)&sh->abort_flag);
+        if (go) {
+            const float sa = (row < M) ? ep.sa_scale[row] : 0.f;
+            if (MODE == 0) {
+                float* out = ep.part + ((size_t)blockIdx.z * M + row) * (size_t)N + n0;
+#pragma unroll 1
+                for (int c0 = 0; c0 < BN; c0 += 32) {
+                    float v[32];
+                    tmem_ld32(tbase + c0, v);
+                    if (row < M) {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) {
+                            const int n = n0 + c0 + i;
+                            if (n < N) out[c0 + i] = v[i] * sa * ep.sb_scale[n];
+                        }
+                    }
+                }
+            } else {
+                // columns [0,128): real parts of bands 128*blockIdx.y + j, [128,256): imaginary
+#pragma unroll 1
+                for (int c0 = 0; c0 < 128; c0 += 32) {
+                    float re[32], im[32];
+                    tmem_ld32(tbase + c0, re);
+                    tmem_ld32(tbase + 128 + c0, im);
+                    if (row < M) {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) {
+                            const int b = blockIdx.y * 128 + c0 + i;
+                            if (b < ep.nb) {
+                                const float f = sa * ep.sb_scale[n0 + c0 + i];
+                                double2* h = ep.hpsi + (size_t)b * ep.ldh + row;
+                                double2 o = *h;
+                                o.x += (double)(re[i] * f);
+                                o.y += (double)(im[i] * f);
+                                *h = o;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// ---------------------------------------------------------------- prep kernels
+template <typename T>
+__device__ __forceinline__ void split_store(float x, T* hi, T* lo);
+template <>
+__device__ __forceinline__ void split_store<__half>(float x, __half* hi, __half* lo)
+{
+    __half h = __float2half_rn(x);
+    *hi = h;
+    *lo = __float2half_rn(x - __half2float(h));
+}
+template <>
+__device__ __forceinline__ void split_store<__nv_bfloat16>(float x, __nv_bfloat16* hi, __nv_bfloat16* lo)
+{
+    __nv_bfloat16 h = __float2bfloat16_rn(x);
+    *hi = h;
+    *lo = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// power-of-two row scale 2^s with max*2^s in [2^13, 2^14] (FP16); 1 for BF16
+__device__ __forceinline__ float row_scale(float mx, bool fp16)
+{
+    if (!fp16 || !(mx > 0.f)) return 1.f;
+    int e;
+    frexpf(mx, &e);  // mx = f * 2^e, f in [0.5, 1)
+    return ldexpf(1.f, 14 - e);
+}
+
+__device__ __forceinline__ float block_max(float v, float* red)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float w = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) w = fmaxf(w, __shfl_xor_sync(0xffffffffu, w, o));
+        if (threadIdx.x == 0) red[0] = w;
+    }
+    __syncthreads();
+    float r = red[0];
+    __syncthreads();
+    return r;
+}
+
+// Projection A: row p of Pr (complex, length npw) -> [hi|lo][p][kpad] interleaved re/im
+template <typename T>
+__global__ void split_rows_kernel(const float2* __restrict__ pr, int npw, size_t ldk, T* hi, T* lo, float* inv_scale,
+                                  bool fp16)
+{
+    __shared__ float red[32];
+    const int p = blockIdx.x;
+    const float2* row = pr + (size_t)p * npw;
+    float mx = 0.f;
+    for (int g = threadIdx.x; g < npw; g += blockDim.x) mx = fmaxf(mx, fmaxf(fabsf(row[g].x), fabsf(row[g].y)));
+    mx = block_max(mx, red);
+    const float sc = row_scale(mx, fp16);
+    if (threadIdx.x == 0) inv_scale[p] = 1.f / sc;
+    T* h = hi + (size_t)p * ldk;
+    T* l = lo + (size_t)p * ldk;
+    for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
+        float x = 0.f;
+        if (k < 2 * (size_t)npw) {
+            float2 v = row[k >> 1];
+            x = (k & 1) ? v.y : v.x;
+        }
+        split_store<T>(x * sc, h + k, l + k);
+    }
+}
+
+// Column maxima of Pr over projectors: cmax[g] = max_p max(|re|, |im|)
+__global__ void col_max_kernel(const float2* __restrict__ pr, int P, int npw, float* cmax)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= npw) return;
+    float mx = 0.f;
+    for (int p = 0; p < P; ++p) {
+        float2 v = pr[(size_t)p * npw + g];
+        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    cmax[g] = mx;
+}
+
+// Expansion A: Pr^T rows g: [hi|lo][g][2p + c], scaled by the row scale of g
+template <typename T>
+__global__ void transpose_split_kernel(const float2* __restrict__ pr, int P, int npw, size_t ldk,
+                                       const float* __restrict__ cmax, T* hi, T* lo, float* inv_scale, bool fp16)
+{
+    __shared__ float2 tile[32][33];
+    const int g0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+    for (int r = ty; r < 32; r += 8) {
+        const int p = p0 + r, g = g0 + tx;
+        tile[r][tx] = (p < P && g < npw) ? pr[(size_t)p * npw + g] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int g = g0 + r;
+        if (g >= npw) continue;
+        const float sc = row_scale(cmax[g], fp16);
+        if (blockIdx.y == 0 && tx == 0) inv_scale[g] = 1.f / sc;
+        const float2 v = tile[tx][r];
+        const int p = p0 + tx;
+        const size_t k = 2 * (size_t)p;
+        if (k + 1 < ldk) {
+            split_store<T>(v.x * sc, hi + (size_t)g * ldk + k, lo + (size_t)g * ldk + k);
+            split_store<T>(v.y * sc, hi + (size_t)g * ldk + k + 1, lo + (size_t)g * ldk + k + 1);
+        }
+    }
+}
+
+// B rows from band data.  src is complex [nb][len] (ld = len) in double2 (psi)
+// or per-column data (W, [len][nb]).  Row layout: t*256 + c*128 + j for band
+// b = 128 t + j.  Projection (FROM_W = false): re row (x_r, x_i), im row (x_i, -x_r);
+// expansion (FROM_W = true): re row (w_r, -w_i), im row (w_i, w_r).
+template <typename T, typename S, bool FROM_W>
+__global__ void band_rows_kernel(const S* __restrict__ src, int nb, int len, size_t ldk, T* hi, T* lo,
+                                 float* inv_scale, bool fp16)
+{
+    __shared__ float red[32];
+    const int b = blockIdx.x;  // band
+    const int t = b / 128, j = b % 128;
+    const size_t rre = (size_t)t * 256 + j, rim = rre + 128;
+    auto get = [&](int i) -> double2 {
+        if (FROM_W) return as_c128(src[(size_t)i * nb + b]);
+        return as_c128(src[(size_t)b * len + i]);
+    };
+    float mx = 0.f;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        double2 v = get(i);
+        mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+    }
+    mx = block_max(mx, red);
+    const float sc = row_scale(mx, fp16);
+    if (threadIdx.x == 0) {
+        inv_scale[rre] = 1.f / sc;
+        inv_scale[rim] = 1.f / sc;
+    }
+    for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
+        float a = 0.f, c = 0.f;
+        if (k < 2 * (size_t)len) {
+            double2 v = get((int)(k >> 1));
+            const double r = v.x * (double)sc, i = v.y * (double)sc;
+            if (!FROM_W) { a = (k & 1) ? (float)i : (float)r; c = (k & 1) ? (float)(-r) : (float)i; }
+            else { a = (k & 1) ? (float)(-i) : (float)r; c = (k & 1) ? (float)r : (float)i; }
+        }
+        split_store<T>(a, hi + rre * ldk + k, lo + rre * ldk + k);
+        split_store<T>(c, hi + rim * ldk + k, lo + rim * ldk + k);
+    }
+}
+
+// rows of bands missing from the last 128-block: zero hi/lo, unit scale
+template <typename T>
+__global__ void zero_rows_kernel(int nb, int nbp, size_t ldk, T* hi, T* lo, float* inv_scale)
+{
+    const int b = nb + blockIdx.x;
+    if (b >= nbp) return;
+    const int t = b / 128, j = b % 128;
+    for (int c = 0; c < 2; ++c) {
+        const size_t r = (size_t)t * 256 + c * 128 + j;
+        if (threadIdx.x == 0) inv_scale[r] = 1.f;
+        for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
+            hi[r * ldk + k] = T(0.f);
+            lo[r * ldk + k] = T(0.f);
+        }
+    }
+}
+
+// W[p][b] = lambda_p * sum_z (C[z][p][re b] + i C[z][p][im b])
+template <typename CW>
+__global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float* __restrict__ part,
+                                   const double* __restrict__ lam, int period, CW* W)
+{
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)P * nb) return;
+    const int p = (int)(idx / nb), b = (int)(idx % nb);
+    const int t = b / 128, j = b % 128;
+    const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
+    double sr = 0.0, si = 0.0;
+    for (int z = 0; z < nsplit; ++z) {
+        const float* row = part + ((size_t)z * P + p) * N;
+        sr += row[cre];
+        si += row[cim];
+    }
+    const double f = lam ? lam[p % period] : 1.0;
+    W[idx] = from_c128<CW>(make_double2(f * sr, f * si));
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// 2-D map over a [rows][ldk] 16-bit matrix, box {64, box_rows}, 128B swizzle
+bool make_map(CUtensorMap* m, const void* base, size_t rows, size_t ldk, int box_rows, bool fp16)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)ldk, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(ldk * 2)};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+size_t tc_round_k(size_t k) { return (k + BK - 1) / BK * BK; }
+int tc_band_rows(int nb) { return (nb + 127) / 128 * 256; }
+
+size_t tc_gemm_smem_bytes() { return (size_t)STAGES * STAGE_BYTES + 1024 + sizeof(TcSmem) + 64; }
+
+cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, TcOperand* proj, TcOperand* expand,
+                                   float* cmax_scratch, cudaStream_t st)
+{
+    if (P == 0 || npw == 0) return cudaSuccess;
+    if (fp16) {
+        split_rows_kernel<__half><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__half*)proj->hi, (__half*)proj->lo,
+                                                     proj->inv_scale, true);
+    } else {
+        split_rows_kernel<__nv_bfloat16><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__nv_bfloat16*)proj->hi,
+                                                            (__nv_bfloat16*)proj->lo, proj->inv_scale, false);
+    }
+    col_max_kernel<<<ceil_div(npw, 256), 256, 0, st>>>(pr, P, npw, cmax_scratch);
+    dim3 g(ceil_div(npw, 32), ceil_div(P, 32));
+    if (fp16)
+        transpose_split_kernel<__half><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, cmax_scratch, (__half*)expand->hi,
+                                                          (__half*)expand->lo, expand->inv_scale, true);
+    else
+        transpose_split_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, cmax_scratch,
+                                                                 (__nv_bfloat16*)expand->hi,
+                                                                 (__nv_bfloat16*)expand->lo, expand->inv_scale, false);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, cudaStream_t st)
+{
+    const int nbp = tc_band_rows(nb) / 2;
+    if (fp16)
+        band_rows_kernel<__half, double2, false><<<nb, 256, 0, st>>>(psi, nb, npw, B->ldk, (__half*)B->hi,
+                                                                    (__half*)B->lo, B->inv_scale, true);
+    else
+        band_rows_kernel<__nv_bfloat16, double2, false><<<nb, 256, 0, st>>>(
+            psi, nb, npw, B->ldk, (__nv_bfloat16*)B->hi, (__nv_bfloat16*)B->lo, B->inv_scale, false);
+    if (nbp > nb) {
+        if (fp16)
+            zero_rows_kernel<__half><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__half*)B->hi, (__half*)B->lo,
+                                                              B->inv_scale);
+        else
+            zero_rows_kernel<__nv_bfloat16><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__nv_bfloat16*)B->hi,
+                                                                     (__nv_bfloat16*)B->lo, B->inv_scale);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, cudaStream_t st)
+{
+    const int nbp = tc_band_rows(nb) / 2;
+    if (fp16)
+        band_rows_kernel<__half, float2, true><<<nb, 256, 0, st>>>(W, nb, P, B->ldk, (__half*)B->hi, (__half*)B->lo,
+                                                                  B->inv_scale, true);
+    else
+        band_rows_kernel<__nv_bfloat16, float2, true><<<nb, 256, 0, st>>>(
+            W, nb, P, B->ldk, (__nv_bfloat16*)B->hi, (__nv_bfloat16*)B->lo, B->inv_scale, false);
+    if (nbp > nb) {
+        if (fp16)
+            zero_rows_kernel<__half><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__half*)B->hi, (__half*)B->lo,
+                                                              B->inv_scale);
+        else
+            zero_rows_kernel<__nv_bfloat16><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__nv_bfloat16*)B->hi,
+                                                                     (__nv_bfloat16*)B->lo, B->inv_scale);
+    }
+    return cudaGetLastError();
+}
+
+int tc_proj_splits(int P, int nb, size_t ldk)
+{
+    const int tiles = ceil_div(P, BM) * (tc_band_rows(nb) / BN);
+    const int ktiles = (int)(ldk / BK);
+    int s = 148 / tiles;
+    if (s < 1) s = 1;
+    if (s > ktiles) s = ktiles;
+    return s;
+}
+
+// A: rows M, B: rows N (= tc_band_rows(nb)); one launch
+static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperand& B, int N, int nsplit, bool fp16,
+                             const TcEpilogue& ep, int* err, cudaStream_t st)
+{
+    CUtensorMap mah, mal, mbh, mbl;
+    if (!make_map(&mah, A.hi, M, A.ldk, BM, fp16) || !make_map(&mal, A.lo, M, A.ldk, BM, fp16) ||
+        !make_map(&mbh, B.hi, N, B.ldk, BN, fp16) || !make_map(&mbl, B.lo, N, B.ldk, BN, fp16))
+        return cudaErrorInvalidValue;
+    const int ktiles = (int)(A.ldk / BK);
+    const int per = ceil_div(ktiles, nsplit);
+    const int nz = ceil_div(ktiles, per);
+    const size_t smem = tc_gemm_smem_bytes();
+    dim3 grid(ceil_div(M, BM), N / BN, nz);
+    const uint32_t idesc = idesc_f16(BM, BN, fp16 ? 0u : 1u);
+    cudaError_t e;
+    if (mode == 0) {
+        if ((e = cudaFuncSetAttribute(tc_gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        tc_gemm_kernel<0><<<grid, 192, smem, st>>>(mah, mal, mbh, mbl, ep, M, N, ktiles, per, idesc, err);
+    } else {
+        if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        tc_gemm_kernel<1><<<grid, 192, smem, st>>>(mah, mal, mbh, mbl, ep, M, N, ktiles, per, idesc, err);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
+                          const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof)
+{
+    const int N = tc_band_rows(nb);
+    TcEpilogue ep{};
+    ep.part = part;
+    ep.sa_scale = A.inv_scale;
+    ep.sb_scale = B.inv_scale;
+    int h = prof->open(PH_PROJ, st);
+    cudaError_t e = launch_tc(0, A, P, B, N, nsplit, fp16, ep, err, st);
+    prof->close(h, st);
+    if (e) return e;
+    const int ktiles = (int)(A.ldk / BK);
+    const int per = ceil_div(ktiles, nsplit);
+    const int nz = ceil_div(ktiles, per);
+    h = prof->open(PH_REDUCE, st);
+    proj_reduce_kernel<float2><<<ceil_div((long)P * nb, 256), 256, 0, st>>>(P, nb, N, nz, part, lam, period, W);
+    prof->close(h, st);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi,
+                         int* err, cudaStream_t st, Prof* prof)
+{
+    const int N = tc_band_rows(nb);
+    TcEpilogue ep{};
+    ep.hpsi = hpsi;
+    ep.ldh = npw;
+    ep.nb = nb;
+    ep.sa_scale = A.inv_scale;
+    ep.sb_scale = B.inv_scale;
+    int h = prof->open(PH_EXPAND, st);
+    cudaError_t e = launch_tc(1, A, npw, B, N, 1, fp16, ep, err, st);
+    prof->close(h, st);
+    return e;
+}

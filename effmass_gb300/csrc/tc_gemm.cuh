@@ -1,0 +1,42 @@
+// tc_gemm.cuh — interface of the tcgen05 projector GEMMs (tc_gemm.cu).
+#pragma once
+
+#include "kernels.cuh"
+
+// One split operand: hi and lo halves ([rows][ldk] FP16 or BF16, ldk a
+// multiple of 64) and the per-row factor that undoes its power-of-two scale.
+struct TcOperand {
+    void* hi = nullptr;
+    void* lo = nullptr;
+    float* inv_scale = nullptr;
+    size_t ldk = 0;
+};
+
+struct TcEpilogue {
+    float* part;               // mode 0: [splits][M][N] partial sums
+    double2* hpsi;             // mode 1: output, [nb][ldh]
+    int ldh;
+    int nb;
+    const float* sa_scale;     // per A row
+    const float* sb_scale;     // per B row
+};
+
+size_t tc_round_k(size_t k);   // K padded to the 64-deep stage
+int tc_band_rows(int nb);      // B rows for nb bands (re/im blocks of 128)
+size_t tc_gemm_smem_bytes();
+int tc_proj_splits(int P, int nb, size_t ldk);
+
+// From the c64 projector matrix Pr[P][npw]: the projection operand [P][2npw]
+// and the expansion operand Pr^T [npw][2P] (expand buffers must be zeroed).
+cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, TcOperand* proj, TcOperand* expand,
+                                   float* cmax_scratch, cudaStream_t st);
+// Band operand of the projection from psi (complex128 [nb][npw]).
+cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, cudaStream_t st);
+// Band operand of the expansion from W (complex64 [P][nb]).
+cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, cudaStream_t st);
+// W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null)
+cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
+                          const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof);
+// hpsi[b][G] += sum_p W[p][b] Pr[p][G]
+cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
+                         cudaStream_t st, Prof* prof);

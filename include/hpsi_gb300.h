@@ -62,7 +62,9 @@ extern "C" {
 /* flags: precision in bits 0-3 */
 #define HPSI_PREC_FP64      0  /* complex128 FFTs, FP64 projector sums: parity path */
 #define HPSI_PREC_FP32      1  /* complex64 FFTs, FP32 projector GEMMs, FP64 phases */
-#define HPSI_PREC_TC        2  /* complex64 FFTs, tcgen05 tensor-core split-BF16 projector GEMMs */
+#define HPSI_PREC_TC        2  /* complex64 FFTs, tcgen05 tensor-core projector GEMMs on split FP16
+                                  (x*2^s = hi + lo per row, 3 products, FP32 accumulation) */
+#define HPSI_PREC_TC_BF16   3  /* as HPSI_PREC_TC with split BF16 (hi + lo, 3 products, no scaling) */
 #define HPSI_PREC_MASK    0xF
 #define HPSI_DEVICE_PTRS  0x10 /* psi/outputs are device pointers (else host memory) */
 #define HPSI_SYNC         0x20 /* synchronise `stream` before returning */
@@ -123,7 +125,8 @@ int hpsi_dim(const hpsi_ctx* ctx, int kid);
 int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
                int flags, void* stream);
 
-/* d{x,y,z}[b] += dH/dk_{x,y,z} psi[b]; NULL outputs are skipped. */
+/* d{x,y,z}[b] += dH/dk_{x,y,z} psi[b]; NULL outputs are skipped.
+ * (The tensor-core precisions use the FP32 GEMMs here.) */
 int hpsi_grad_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi,
                     double* dx, double* dy, double* dz, int flags, void* stream);
 
