@@ -35,7 +35,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--prec", default="fp32", choices=["fp32", "fp64", "tc"])
+    ap.add_argument("--prec", default="tc", choices=["fp32", "fp64", "tc", "tc_bf16"])
     ap.add_argument("--system", default="sc64")
     ap.add_argument("--nb", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -259,7 +259,8 @@ def run_gb300(args, rank, world, local):
         "metric": "H|psi> band-applications/s (mixed precision, rel. err <= 1e-6 vs FP64)",
         "value": value, "unit": "band-apps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "c64/f32", "fp64": "c128/f64", "tc": "c64/f32 + bf16x3 tensor"}[args.prec],
+        "dtype": {"fp32": "c64/f32", "fp64": "c128/f64", "tc": "c64/f32 FFT + fp16x2-split tensor (3 products, f32 acc)",
+                  "tc_bf16": "c64/f32 FFT + bf16x2-split tensor (3 products, f32 acc)"}[args.prec],
         "precision_path": args.prec,
         "data": "synthetic (seeded psi, V_loc, KB projectors of the named shapes)",
         "config": {"workload": f"{args.system}: 64-atom SC diamond, 72^3 grid, Ecut 20 Ha, Gamma",

@@ -21,10 +21,30 @@
 #define HPSI_FFT_MAXR 13
 #define HPSI_FFT_MAXN 512
 
+// Division by a run-time constant d (dividends below 2^31) as a multiply-high
+// and a shift: q = (umulhi(x, mul) + x) >> shr (Granlund-Montgomery).
+struct FastDiv {
+    uint32_t d, mul, shr;
+};
+
+static inline FastDiv make_fastdiv(uint32_t d)
+{
+    FastDiv f{d, 0u, 0u};
+    if (d <= 1) return f;
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    f.shr = l;
+    f.mul = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    return f;
+}
+
+HPSI_D uint32_t fdiv(uint32_t x, const FastDiv& f) { return (__umulhi(x, f.mul) + x) >> f.shr; }
+
 struct FftLen {
     int n;
     int nst;
     int rad[HPSI_FFT_MAXST];
+    FastDiv ns[HPSI_FFT_MAXST];  // divisor by the product of the radices before stage s
 };
 
 // Factor n into stage radices, preferring the composite radices 8 and 9
@@ -45,6 +65,11 @@ static inline bool fft_factor(int n, FftLen* L)
             L->rad[L->nst++] = p;
             m /= p;
         }
+    }
+    int Ns = 1;
+    for (int s = 0; s < L->nst; ++s) {
+        L->ns[s] = make_fastdiv((uint32_t)Ns);
+        Ns *= L->rad[s];
     }
     return m == 1;
 }
@@ -166,66 +191,71 @@ HPSI_D void dft_small(C (&v)[HPSI_FFT_MAXR], const C* tw, int n, int sign)
 
 // One Stockham stage over `nl` lines.  Element e of line L lives at
 // buf[L*ls + e*es].  LINE_FAST selects which index consecutive threads walk:
-// lines (use when ls == 1) or butterflies (use when es == 1), so that shared
-// memory accesses of a warp are contiguous.
+// lines (use when ls == 1, or when the row stride ls is odd) or butterflies
+// (use when es == 1), so that shared-memory accesses of a warp do not
+// collide.  `nlf` divides by nl and `nsf` by Ns without integer division.
 template <typename C, int P, bool LINE_FAST>
-HPSI_D void fft_stage_p(const C* __restrict__ src, C* __restrict__ dst, int n, int Ns, int nl, int ls,
-                        int es, const C* tw, int sign)
+HPSI_D void fft_stage_p(const C* __restrict__ src, C* __restrict__ dst, int n, const FastDiv& nsf, const FastDiv& nlf,
+                        int ls, int es, const C* tw, int sign)
 {
+    const int Ns = (int)nsf.d;
+    const int nl = (int)nlf.d;
     const int nbf = n / P;
     const int total = nl * nbf;
     const int tstep = n / (Ns * P);
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         int L, i;
-        if (LINE_FAST) { L = t % nl; i = t / nl; }
-        else { i = t % nbf; L = t / nbf; }
-        const int k = i % Ns;
+        if (LINE_FAST) { i = (int)fdiv((uint32_t)t, nlf); L = t - i * nl; }
+        else { L = (int)(t / nbf); i = t - L * nbf; }
+        const int hi = (int)fdiv((uint32_t)i, nsf);
+        const int k = i - hi * Ns;
+        const int tj = k * tstep;  // q * tj < n for q < P
         C v[HPSI_FFT_MAXR];
         const C* s = src + (size_t)L * ls;
 #pragma unroll
         for (int q = 0; q < P; ++q) {
             C x = s[(size_t)(i + q * nbf) * es];
-            if (q > 0 && k > 0) x = cmul(x, tw_get(tw, (q * k * tstep) % n, sign));
+            if (q > 0 && k > 0) x = cmul(x, tw_get(tw, q * tj, sign));
             v[q] = x;
         }
         dft_small<C, P>(v, tw, n, sign);
         C* d = dst + (size_t)L * ls;
-        const int base = (i / Ns) * Ns * P + k;
+        const int base = hi * Ns * P + k;
 #pragma unroll
         for (int q = 0; q < P; ++q) d[(size_t)(base + q * Ns) * es] = v[q];
     }
 }
 
 template <typename C, bool LINE_FAST>
-HPSI_D void fft_stage(const C* src, C* dst, int p, int n, int Ns, int nl, int ls, int es, const C* tw, int sign)
+HPSI_D void fft_stage(const C* src, C* dst, int p, int n, const FastDiv& nsf, const FastDiv& nlf, int ls, int es,
+                      const C* tw, int sign)
 {
     switch (p) {
-        case 8: fft_stage_p<C, 8, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 9: fft_stage_p<C, 9, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 2: fft_stage_p<C, 2, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 3: fft_stage_p<C, 3, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 4: fft_stage_p<C, 4, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 5: fft_stage_p<C, 5, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 7: fft_stage_p<C, 7, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 11: fft_stage_p<C, 11, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
-        case 13: fft_stage_p<C, 13, LINE_FAST>(src, dst, n, Ns, nl, ls, es, tw, sign); break;
+        case 8: fft_stage_p<C, 8, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 9: fft_stage_p<C, 9, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 2: fft_stage_p<C, 2, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 3: fft_stage_p<C, 3, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 4: fft_stage_p<C, 4, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 5: fft_stage_p<C, 5, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 7: fft_stage_p<C, 7, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 11: fft_stage_p<C, 11, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+        case 13: fft_stage_p<C, 13, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
         default: break;  // fft_factor admits no other radix
     }
 }
 
-// Full transform of nl lines; data starts in bufs[cur] and the function
-// returns the index (0/1) of the buffer holding the result.
+// Full transform of the nl lines described by nlf; data starts in bufs[cur]
+// and the function returns the index (0/1) of the buffer holding the result.
 template <typename C, bool LINE_FAST>
-HPSI_D int fft_lines(C* buf0, C* buf1, int cur, const FftLen& L, int nl, int ls, int es, const C* tw, int sign)
+HPSI_D int fft_lines(C* buf0, C* buf1, int cur, const FftLen& L, const FastDiv& nlf, int ls, int es, const C* tw,
+                     int sign)
 {
-    int Ns = 1;
     for (int s = 0; s < L.nst; ++s) {
         const int p = L.rad[s];
         C* src = cur ? buf1 : buf0;
         C* dst = cur ? buf0 : buf1;
-        fft_stage<C, LINE_FAST>(src, dst, p, L.n, Ns, nl, ls, es, tw, sign);
+        fft_stage<C, LINE_FAST>(src, dst, p, L.n, L.ns[s], nlf, ls, es, tw, sign);
         __syncthreads();
-        Ns *= p;
         cur ^= 1;
     }
     return cur;

@@ -627,6 +627,7 @@ static size_t tc_ws(const KSlot& s, int nb)
     cv.take<uint16_t>((size_t)NB * k2);
     cv.take<uint16_t>((size_t)NB * k2);
     cv.take<float>((size_t)NB);
+    cv.take<unsigned>((size_t)nb);
     return cv.off;
 }
 
@@ -645,16 +646,17 @@ static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     const size_t ow = cv.take<float2>((size_t)s.P * nb);
     const size_t ob2h = cv.take<uint16_t>((size_t)NB * k2), ob2l = cv.take<uint16_t>((size_t)NB * k2);
     const size_t ob2s = cv.take<float>((size_t)NB);
+    unsigned* rowmax = reinterpret_cast<unsigned*>(ws + cv.take<unsigned>((size_t)nb));
     TcOperand B1{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
     TcOperand B2{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
     float2* W = reinterpret_cast<float2*>(ws + ow);
     int h = c->prof.open(PH_OTHER, st);
-    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &B1, st));
+    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &B1, rowmax, st));
     c->prof.close(h, st);
     CUDA_TRY(c, tc_projection(s.tc_proj, s.P, B1, nb, ns, fp16, reinterpret_cast<float*>(ws + opart), s.d_lam, s.P, W,
                               c->d_err, st, &c->prof));
     h = c->prof.open(PH_OTHER, st);
-    CUDA_TRY(c, tc_w_operand(W, s.P, nb, fp16, &B2, st));
+    CUDA_TRY(c, tc_w_operand(W, s.P, nb, fp16, &B2, rowmax, st));
     c->prof.close(h, st);
     CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, B2, nb, fp16, hpsi, c->d_err, st, &c->prof));
     return HPSI_OK;

@@ -62,6 +62,9 @@ struct LocalArgs {
     const int* ent_ig;      // [npw] caller-order G index; negative = gather only
     const int* ent_jk;      // [npw] j*n3 + k of the entry
     FftLen Lx, Ly, Lz;
+    FastDiv nl_z;           // z-lines of a plane: n2
+    FastDiv nl_y;           // y-lines of a plane: n3
+    FastDiv nl_x;           // x-lines of an x-pass block: kt*bb
 };
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64);

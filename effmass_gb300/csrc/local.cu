@@ -51,8 +51,8 @@ __global__ void __launch_bounds__(256) g2r_planes(LocalArgs a, const double2* __
         }
     }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Lz, n2, n3p, 1, twz, +1);
-    cur = fft_lines<C, true>(b0, b1, cur, a.Ly, n3, 1, n3p, twy, +1);
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Lz, a.nl_z, n3p, 1, twz, +1);
+    cur = fft_lines<C, true>(b0, b1, cur, a.Ly, a.nl_y, 1, n3p, twy, +1);
     const C* res = cur ? b1 : b0;
     C* out = T + ((size_t)b * a.nxs + p) * n23;
     for (int t = threadIdx.x; t < n23; t += blockDim.x) {
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict
         b0[a.plane_x[pp] * NL + bb * KT + kk] = *src;
     }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Lx, NL, 1, NL, twx, +1);
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Lx, a.nl_x, 1, NL, twx, +1);
     C* res = cur ? b1 : b0;
     for (int t = threadIdx.x; t < n1 * NL; t += blockDim.x) {
         int x = t / NL, L = t - x * NL;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict
         res[t] = cscale(res[t], (typename Real<C>::type)vt[x * KT + kk]);
     }
     __syncthreads();
-    cur = fft_lines<C, true>(b0, b1, cur, a.Lx, NL, 1, NL, twx, -1);
+    cur = fft_lines<C, true>(b0, b1, cur, a.Lx, a.nl_x, 1, NL, twx, -1);
     res = cur ? b1 : b0;
     for (int t = threadIdx.x; t < nxs * per_plane; t += blockDim.x) {
         int pp = t / per_plane, r = t - pp * per_plane;
@@ -135,8 +135,8 @@ __global__ void __launch_bounds__(256) r2g_planes(LocalArgs a, const C* __restri
         b0[j * n3p + k] = in[t];
     }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Ly, n3, 1, n3p, twy, -1);
-    cur = fft_lines<C, true>(b0, b1, cur, a.Lz, n2, n3p, 1, twz, -1);
+    int cur = fft_lines<C, true>(b0, b1, 0, a.Ly, a.nl_y, 1, n3p, twy, -1);
+    cur = fft_lines<C, true>(b0, b1, cur, a.Lz, a.nl_z, n3p, 1, twz, -1);
     const C* res = cur ? b1 : b0;
     const double2* ps = psi + (size_t)b * a.npw;
     double2* hp = hpsi + (size_t)b * a.npw;
@@ -188,6 +188,9 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
     if (a->kt > a->n3) a->kt = a->n3;
     a->bb = nlmax / a->kt;
     if (a->bb < 1) a->bb = 1;
+    a->nl_z = make_fastdiv((uint32_t)a->n2);
+    a->nl_y = make_fastdiv((uint32_t)a->n3);
+    a->nl_x = make_fastdiv((uint32_t)(a->kt * a->bb));
 }
 
 template <typename C, typename V>

@@ -393,44 +393,68 @@ __global__ void transpose_split_kernel(const float2* __restrict__ pr, int P, int
     }
 }
 
-// B rows from band data.  src is complex [nb][len] (ld = len) in double2 (psi)
-// or per-column data (W, [len][nb]).  Row layout: t*256 + c*128 + j for band
-// b = 128 t + j.  Projection (FROM_W = false): re row (x_r, x_i), im row (x_i, -x_r);
-// expansion (FROM_W = true): re row (w_r, -w_i), im row (w_i, w_r).
-template <typename T, typename S, bool FROM_W>
-__global__ void band_rows_kernel(const S* __restrict__ src, int nb, int len, size_t ldk, T* hi, T* lo,
-                                 float* inv_scale, bool fp16)
+// B rows from band data.  src is complex [nb][len] (psi, FROM_W = false) or
+// [len][nb] (W, FROM_W = true).  Row layout: t*256 + c*128 + j for band
+// b = 128 t + j.  Projection: re row (x_r, x_i), im row (x_i, -x_r);
+// expansion: re row (w_r, -w_i), im row (w_i, w_r).  Two passes: the band
+// maxima (atomicMax on the float bits, non-negative) then the split writes.
+template <typename S, bool FROM_W>
+__device__ __forceinline__ double2 band_get(const S* src, int nb, int len, int b, int i)
 {
-    __shared__ float red[32];
-    const int b = blockIdx.x;  // band
-    const int t = b / 128, j = b % 128;
-    const size_t rre = (size_t)t * 256 + j, rim = rre + 128;
-    auto get = [&](int i) -> double2 {
-        if (FROM_W) return as_c128(src[(size_t)i * nb + b]);
-        return as_c128(src[(size_t)b * len + i]);
-    };
+    if (FROM_W) return as_c128(src[(size_t)i * nb + b]);
+    return as_c128(src[(size_t)b * len + i]);
+}
+
+template <typename S, bool FROM_W>
+__global__ void band_max_kernel(const S* __restrict__ src, int nb, int len, unsigned* rowmax)
+{
+    const int b = blockIdx.y;
     float mx = 0.f;
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
-        double2 v = get(i);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        double2 v = band_get<S, FROM_W>(src, nb, len, b, i);
         mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
     }
-    mx = block_max(mx, red);
-    const float sc = row_scale(mx, fp16);
-    if (threadIdx.x == 0) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(rowmax + b, __float_as_uint(mx));
+}
+
+template <typename T, typename S, bool FROM_W>
+__global__ void band_write_kernel(const S* __restrict__ src, int nb, int len, size_t ldk, T* hi, T* lo,
+                                  float* inv_scale, const unsigned* __restrict__ rowmax, bool fp16)
+{
+    const int b = blockIdx.y;
+    const int t = b / 128, j = b % 128;
+    const size_t rre = (size_t)t * 256 + j, rim = rre + 128;
+    const float sc = row_scale(__uint_as_float(rowmax[b]), fp16);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         inv_scale[rre] = 1.f / sc;
         inv_scale[rim] = 1.f / sc;
     }
-    for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
-        float a = 0.f, c = 0.f;
-        if (k < 2 * (size_t)len) {
-            double2 v = get((int)(k >> 1));
-            const double r = v.x * (double)sc, i = v.y * (double)sc;
-            if (!FROM_W) { a = (k & 1) ? (float)i : (float)r; c = (k & 1) ? (float)(-r) : (float)i; }
-            else { a = (k & 1) ? (float)(-i) : (float)r; c = (k & 1) ? (float)r : (float)i; }
-        }
-        split_store<T>(a, hi + rre * ldk + k, lo + rre * ldk + k);
-        split_store<T>(c, hi + rim * ldk + k, lo + rim * ldk + k);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // complex element -> k = 2i, 2i+1
+    if ((size_t)(2 * i) >= ldk) return;
+    float a0 = 0.f, a1 = 0.f, c0 = 0.f, c1 = 0.f;
+    if (i < len) {
+        const double2 v = band_get<S, FROM_W>(src, nb, len, b, i);
+        const float r = (float)(v.x * (double)sc), m = (float)(v.y * (double)sc);
+        if (!FROM_W) { a0 = r; a1 = m; c0 = m; c1 = -r; }
+        else { a0 = r; a1 = -m; c0 = m; c1 = r; }
     }
+    const size_t k = 2 * (size_t)i;
+    split_store<T>(a0, hi + rre * ldk + k, lo + rre * ldk + k);
+    split_store<T>(a1, hi + rre * ldk + k + 1, lo + rre * ldk + k + 1);
+    split_store<T>(c0, hi + rim * ldk + k, lo + rim * ldk + k);
+    split_store<T>(c1, hi + rim * ldk + k + 1, lo + rim * ldk + k + 1);
+}
+
+template <typename T, typename S, bool FROM_W>
+static void band_rows(const S* src, int nb, int len, size_t ldk, T* hi, T* lo, float* inv_scale, unsigned* rowmax,
+                      bool fp16, cudaStream_t st)
+{
+    cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * nb, st);
+    const int chunks = min(64, ceil_div(len, 256 * 4));
+    band_max_kernel<S, FROM_W><<<dim3(chunks, nb), 256, 0, st>>>(src, nb, len, rowmax);
+    band_write_kernel<T, S, FROM_W><<<dim3(ceil_div((long)(ldk / 2), 256), nb), 256, 0, st>>>(
+        src, nb, len, ldk, hi, lo, inv_scale, rowmax, fp16);
 }
 
 // rows of bands missing from the last 128-block: zero hi/lo, unit scale
@@ -533,15 +557,16 @@ cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, 
     return cudaGetLastError();
 }
 
-cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, cudaStream_t st)
+cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, unsigned* rowmax,
+                            cudaStream_t st)
 {
     const int nbp = tc_band_rows(nb) / 2;
     if (fp16)
-        band_rows_kernel<__half, double2, false><<<nb, 256, 0, st>>>(psi, nb, npw, B->ldk, (__half*)B->hi,
-                                                                    (__half*)B->lo, B->inv_scale, true);
+        band_rows<__half, double2, false>(psi, nb, npw, B->ldk, (__half*)B->hi, (__half*)B->lo, B->inv_scale, rowmax,
+                                          true, st);
     else
-        band_rows_kernel<__nv_bfloat16, double2, false><<<nb, 256, 0, st>>>(
-            psi, nb, npw, B->ldk, (__nv_bfloat16*)B->hi, (__nv_bfloat16*)B->lo, B->inv_scale, false);
+        band_rows<__nv_bfloat16, double2, false>(psi, nb, npw, B->ldk, (__nv_bfloat16*)B->hi,
+                                                 (__nv_bfloat16*)B->lo, B->inv_scale, rowmax, false, st);
     if (nbp > nb) {
         if (fp16)
             zero_rows_kernel<__half><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__half*)B->hi, (__half*)B->lo,
@@ -553,15 +578,15 @@ cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOp
     return cudaGetLastError();
 }
 
-cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, cudaStream_t st)
+cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, unsigned* rowmax, cudaStream_t st)
 {
     const int nbp = tc_band_rows(nb) / 2;
     if (fp16)
-        band_rows_kernel<__half, float2, true><<<nb, 256, 0, st>>>(W, nb, P, B->ldk, (__half*)B->hi, (__half*)B->lo,
-                                                                  B->inv_scale, true);
+        band_rows<__half, float2, true>(W, nb, P, B->ldk, (__half*)B->hi, (__half*)B->lo, B->inv_scale, rowmax, true,
+                                        st);
     else
-        band_rows_kernel<__nv_bfloat16, float2, true><<<nb, 256, 0, st>>>(
-            W, nb, P, B->ldk, (__nv_bfloat16*)B->hi, (__nv_bfloat16*)B->lo, B->inv_scale, false);
+        band_rows<__nv_bfloat16, float2, true>(W, nb, P, B->ldk, (__nv_bfloat16*)B->hi, (__nv_bfloat16*)B->lo,
+                                               B->inv_scale, rowmax, false, st);
     if (nbp > nb) {
         if (fp16)
             zero_rows_kernel<__half><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__half*)B->hi, (__half*)B->lo,

@@ -30,10 +30,11 @@ int tc_proj_splits(int P, int nb, size_t ldk);
 // and the expansion operand Pr^T [npw][2P] (expand buffers must be zeroed).
 cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, TcOperand* proj, TcOperand* expand,
                                    float* cmax_scratch, cudaStream_t st);
-// Band operand of the projection from psi (complex128 [nb][npw]).
-cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, cudaStream_t st);
+// Band operand of the projection from psi (complex128 [nb][npw]); rowmax: nb scratch words.
+cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, unsigned* rowmax,
+                            cudaStream_t st);
 // Band operand of the expansion from W (complex64 [P][nb]).
-cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, cudaStream_t st);
+cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, unsigned* rowmax, cudaStream_t st);
 // W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null)
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                           const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof);
