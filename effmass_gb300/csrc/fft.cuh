@@ -226,7 +226,9 @@ HPSI_D void fft_stage_p(const C* __restrict__ src, C* __restrict__ dst, int n, c
     }
 }
 
-template <typename C, bool LINE_FAST>
+// Radices compiled into a stage: the narrow set {2,3,4,5,8,9} covers the
+// usual 2^a 3^b 5^c grids with few registers; WIDE adds 7, 11 and 13.
+template <typename C, bool LINE_FAST, bool WIDE>
 HPSI_D void fft_stage(const C* src, C* dst, int p, int n, const FastDiv& nsf, const FastDiv& nlf, int ls, int es,
                       const C* tw, int sign)
 {
@@ -237,16 +239,30 @@ HPSI_D void fft_stage(const C* src, C* dst, int p, int n, const FastDiv& nsf, co
         case 3: fft_stage_p<C, 3, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
         case 4: fft_stage_p<C, 4, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
         case 5: fft_stage_p<C, 5, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
-        case 7: fft_stage_p<C, 7, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
-        case 11: fft_stage_p<C, 11, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
-        case 13: fft_stage_p<C, 13, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
-        default: break;  // fft_factor admits no other radix
+        default:
+            if constexpr (WIDE) {
+                switch (p) {
+                    case 7: fft_stage_p<C, 7, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+                    case 11: fft_stage_p<C, 11, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+                    case 13: fft_stage_p<C, 13, LINE_FAST>(src, dst, n, nsf, nlf, ls, es, tw, sign); break;
+                    default: break;
+                }
+            }
+            break;  // fft_factor admits no other radix; the host picks WIDE when 7, 11 or 13 occur
     }
+}
+
+// true if a length needs the wide radix set
+static inline bool fft_needs_wide(const FftLen& L)
+{
+    for (int s = 0; s < L.nst; ++s)
+        if (L.rad[s] == 7 || L.rad[s] == 11 || L.rad[s] == 13) return true;
+    return false;
 }
 
 // Full transform of the nl lines described by nlf; data starts in bufs[cur]
 // and the function returns the index (0/1) of the buffer holding the result.
-template <typename C, bool LINE_FAST>
+template <typename C, bool LINE_FAST, bool WIDE>
 HPSI_D int fft_lines(C* buf0, C* buf1, int cur, const FftLen& L, const FastDiv& nlf, int ls, int es, const C* tw,
                      int sign)
 {
@@ -254,7 +270,7 @@ HPSI_D int fft_lines(C* buf0, C* buf1, int cur, const FftLen& L, const FastDiv& 
         const int p = L.rad[s];
         C* src = cur ? buf1 : buf0;
         C* dst = cur ? buf0 : buf1;
-        fft_stage<C, LINE_FAST>(src, dst, p, L.n, L.ns[s], nlf, ls, es, tw, sign);
+        fft_stage<C, LINE_FAST, WIDE>(src, dst, p, L.n, L.ns[s], nlf, ls, es, tw, sign);
         __syncthreads();
         cur ^= 1;
     }

@@ -20,12 +20,19 @@
 #include "fft.cuh"
 #include "kernels.cuh"
 
+// Launch shape per precision: complex64 kernels run 512-thread plane blocks
+// (two per SM) and four x-pass blocks per SM; complex128 kernels keep the
+// register budget of one block per SM.
+template <typename C> struct Cfg;
+template <> struct Cfg<float2> { static constexpr int plane_threads = 512, plane_min = 2, x_min = 4; };
+template <> struct Cfg<double2> { static constexpr int plane_threads = 256, plane_min = 1, x_min = 1; };
+
 // Shared-memory planes use a padded row stride n3p = n3 + 1 (odd) so that
 // both the z-lines (rows) and the y-lines (columns) are read and written by
 // consecutive threads without bank conflicts (both transforms walk lines
 // fastest: LINE_FAST).
-template <typename C>
-__global__ void __launch_bounds__(256) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
+template <typename C, bool WIDE>
+__global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -51,8 +58,8 @@ __global__ void __launch_bounds__(256) g2r_planes(LocalArgs a, const double2* __
         }
     }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Lz, a.nl_z, n3p, 1, twz, +1);
-    cur = fft_lines<C, true>(b0, b1, cur, a.Ly, a.nl_y, 1, n3p, twy, +1);
+    int cur = fft_lines<C, true, WIDE>(b0, b1, 0, a.Lz, a.nl_z, n3p, 1, twz, +1);
+    cur = fft_lines<C, true, WIDE>(b0, b1, cur, a.Ly, a.nl_y, 1, n3p, twy, +1);
     const C* res = cur ? b1 : b0;
     C* out = T + ((size_t)b * a.nxs + p) * n23;
     for (int t = threadIdx.x; t < n23; t += blockDim.x) {
@@ -64,8 +71,8 @@ __global__ void __launch_bounds__(256) g2r_planes(LocalArgs a, const double2* __
 // x pass: a block owns the x-lines of (j, k0..k0+KT) for BB consecutive bands
 // (NL = KT*BB lines, line L = bb*KT + kk, element x at [x*NL + L]); the V tile
 // is loaded once per block.
-template <typename C, typename V>
-__global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
+template <typename C, typename V, bool WIDE>
+__global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
                                               const C* __restrict__ tw_x_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -96,7 +103,7 @@ __global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict
         b0[a.plane_x[pp] * NL + bb * KT + kk] = *src;
     }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Lx, a.nl_x, 1, NL, twx, +1);
+    int cur = fft_lines<C, true, WIDE>(b0, b1, 0, a.Lx, a.nl_x, 1, NL, twx, +1);
     C* res = cur ? b1 : b0;
     for (int t = threadIdx.x; t < n1 * NL; t += blockDim.x) {
         int x = t / NL, L = t - x * NL;
@@ -104,7 +111,7 @@ __global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict
         res[t] = cscale(res[t], (typename Real<C>::type)vt[x * KT + kk]);
     }
     __syncthreads();
-    cur = fft_lines<C, true>(b0, b1, cur, a.Lx, a.nl_x, 1, NL, twx, -1);
+    cur = fft_lines<C, true, WIDE>(b0, b1, cur, a.Lx, a.nl_x, 1, NL, twx, -1);
     res = cur ? b1 : b0;
     for (int t = threadIdx.x; t < nxs * per_plane; t += blockDim.x) {
         int pp = t / per_plane, r = t - pp * per_plane;
@@ -114,8 +121,8 @@ __global__ void __launch_bounds__(256) x_pass(LocalArgs a, int nb, C* __restrict
     }
 }
 
-template <typename C>
-__global__ void __launch_bounds__(256) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
+template <typename C, bool WIDE>
+__global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
                                                   double2* __restrict__ hpsi, const double* __restrict__ kinetic,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
@@ -135,8 +142,8 @@ __global__ void __launch_bounds__(256) r2g_planes(LocalArgs a, const C* __restri
         b0[j * n3p + k] = in[t];
     }
     __syncthreads();
-    int cur = fft_lines<C, true>(b0, b1, 0, a.Ly, a.nl_y, 1, n3p, twy, -1);
-    cur = fft_lines<C, true>(b0, b1, cur, a.Lz, a.nl_z, n3p, 1, twz, -1);
+    int cur = fft_lines<C, true, WIDE>(b0, b1, 0, a.Ly, a.nl_y, 1, n3p, twy, -1);
+    cur = fft_lines<C, true, WIDE>(b0, b1, cur, a.Lz, a.nl_z, n3p, 1, twz, -1);
     const C* res = cur ? b1 : b0;
     const double2* ps = psi + (size_t)b * a.npw;
     double2* hp = hpsi + (size_t)b * a.npw;
@@ -177,11 +184,12 @@ size_t local_smem_bytes(const LocalArgs& a, bool fp64)
     return p > x ? p : x;
 }
 
-// x-pass block shape: about 96 KB of line buffers, at most 8 z-values per
-// block, the rest filled with bands.
+// x-pass block shape: about 48 KB of complex64 line buffers (four blocks per
+// SM) or 96 KB of complex128 ones, at most 8 z-values per block, the rest
+// filled with bands.
 void local_xpass_shape(LocalArgs* a, size_t csize)
 {
-    const size_t budget = 96 * 1024;
+    const size_t budget = csize == 8 ? 48 * 1024 : 96 * 1024;
     int nlmax = (int)(budget / (2 * (size_t)a->n1 * csize));
     if (nlmax < 1) nlmax = 1;
     a->kt = nlmax < 8 ? nlmax : 8;
@@ -193,28 +201,39 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
     a->nl_x = make_fastdiv((uint32_t)(a->kt * a->bb));
 }
 
+template <typename C, typename V, bool WIDE>
+static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic,
+                                  C* T, const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st,
+                                  Prof* prof)
+{
+    const size_t sp = plane_smem<C>(a), sx = xpass_smem<C, V>(a);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(g2r_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(r2g_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
+        return e;
+    if (a.nxs == 0 || nb == 0) return cudaSuccess;
+    dim3 gp(a.nxs, nb);
+    int h = prof->open(PH_G2R, st);
+    g2r_planes<C, WIDE><<<gp, Cfg<C>::plane_threads, sp, st>>>(a, psi, T, twy, twz);
+    prof->close(h, st);
+    dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
+    h = prof->open(PH_XPASS, st);
+    x_pass<C, V, WIDE><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    prof->close(h, st);
+    h = prof->open(PH_R2G, st);
+    r2g_planes<C, WIDE><<<gp, Cfg<C>::plane_threads, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
+    prof->close(h, st);
+    return cudaGetLastError();
+}
+
 template <typename C, typename V>
 cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
                          const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof)
 {
-    const size_t sp = plane_smem<C>(a), sx = xpass_smem<C, V>(a);
-    cudaError_t e;
-    if ((e = cudaFuncSetAttribute(g2r_planes<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(r2g_planes<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(x_pass<C, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
-    if (a.nxs == 0 || nb == 0) return cudaSuccess;
-    dim3 gp(a.nxs, nb);
-    int h = prof->open(PH_G2R, st);
-    g2r_planes<C><<<gp, 256, sp, st>>>(a, psi, T, twy, twz);
-    prof->close(h, st);
-    dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
-    h = prof->open(PH_XPASS, st);
-    x_pass<C, V><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
-    prof->close(h, st);
-    h = prof->open(PH_R2G, st);
-    r2g_planes<C><<<gp, 256, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
-    prof->close(h, st);
-    return cudaGetLastError();
+    const bool wide = fft_needs_wide(a.Lx) || fft_needs_wide(a.Ly) || fft_needs_wide(a.Lz);
+    if (wide) return launch_local_t<C, V, true>(a, nb, psi, hpsi, kinetic, T, vloc, twx, twy, twz, st, prof);
+    return launch_local_t<C, V, false>(a, nb, psi, hpsi, kinetic, T, vloc, twx, twy, twz, st, prof);
 }
 
 template cudaError_t launch_local<double2, double>(const LocalArgs&, int, const double2*, double2*, const double*,

@@ -17,7 +17,7 @@ from effmass_gb300 import abi
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-12, "fp32": 1e-6}
+TOL = {"fp64": 1e-12, "fp32": 1e-6, "tc": 1e-6, "tc_bf16": 2e-6}
 
 
 @pytest.fixture(scope="module")
@@ -40,7 +40,7 @@ def H_of():
         v[0].close()
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "tc", "tc_bf16"])
 @pytest.mark.parametrize("case", CASES)
 def test_hpsi_matches_reference(H_of, case, prec):
     H, sysm, kp, psi, href, _ = H_of(case)
@@ -201,13 +201,14 @@ def sc64():
     H.close()
 
 
-def test_full_size_fp32_vs_fp64_and_hermitian(sc64):
+def test_full_size_mixed_vs_fp64_and_hermitian(sc64):
     H, kp, psi = sc64
     h64 = np.zeros_like(psi)
-    h32 = np.zeros_like(psi)
     H.apply(0, psi.shape[0], psi, h64, "fp64")
-    H.apply(0, psi.shape[0], psi, h32, "fp32")
-    assert rel_err(h32, h64) <= 1e-6
+    for prec in ("fp32", "tc", "tc_bf16"):
+        hm = np.zeros_like(psi)
+        H.apply(0, psi.shape[0], psi, hm, prec)
+        assert rel_err(hm, h64) <= TOL[prec], (prec, rel_err(hm, h64))
     M = psi.conj() @ h64.T
     assert np.abs(M - M.conj().T).max() <= 1e-11 * np.abs(M).max()
 
@@ -221,3 +222,22 @@ def test_full_size_linearity(sc64):
     H.apply(0, 4, mix, hm, "fp64")
     H.apply(0, psi.shape[0], psi, h, "fp64")
     assert rel_err(hm, a * h[0:4] + b * h[4:8]) <= 1e-12
+
+
+def test_wide_radix_grid_matches_oracle():
+    """A 14 x 21 x 13 grid needs the radix-7 and radix-13 stages (the wide kernel set)."""
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import Hamiltonian
+    from oracle import oracle as O
+    sysm = S.make_system("tiny")
+    sysm.n1, sysm.n2, sysm.n3 = 14, 21, 13
+    sysm.v_loc = S.local_potential(sysm.lattice, sysm.atom_tau, 14, 21, 13)
+    kp = S.g_sphere(sysm.lattice, (0.1, 0.2, 0.3), sysm.ecut)
+    psi = S.make_bands(kp, 3)
+    ref = O.hpsi(sysm, kp, psi)
+    with Hamiltonian(sysm) as H:
+        H.set_kpoint(0, kp)
+        for prec, tol in (("fp64", 1e-12), ("fp32", 1e-6), ("tc", 1e-6)):
+            out = np.zeros_like(psi)
+            H.at_k(0, precision=prec)(3, psi, out)
+            assert rel_err(out, ref) <= tol, (prec, rel_err(out, ref))
