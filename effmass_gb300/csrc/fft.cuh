@@ -226,6 +226,105 @@ HPSI_D void fft_stage_p(const C* __restrict__ src, C* __restrict__ dst, int n, c
     }
 }
 
+// The same stage with element access through functors: ld(L, e) returns
+// element e of line L, st(L, e, v) stores it.  Lets the first stage of a
+// transform read straight from global memory and the last stage write straight
+// to its destination (with any pointwise factor folded into st).
+template <typename C, int P, bool LINE_FAST, typename LD, typename ST>
+HPSI_D void fft_stage_io(const LD& ld, const ST& st, int n, const FastDiv& nsf, const FastDiv& nlf, const C* tw,
+                         int sign)
+{
+    const int Ns = (int)nsf.d;
+    const int nl = (int)nlf.d;
+    const int nbf = n / P;
+    const int total = nl * nbf;
+    const int tstep = n / (Ns * P);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int L, i;
+        if (LINE_FAST) { i = (int)fdiv((uint32_t)t, nlf); L = t - i * nl; }
+        else { L = (int)(t / nbf); i = t - L * nbf; }
+        const int hi = (int)fdiv((uint32_t)i, nsf);
+        const int k = i - hi * Ns;
+        const int tj = k * tstep;
+        C v[HPSI_FFT_MAXR];
+#pragma unroll
+        for (int q = 0; q < P; ++q) v[q] = ld(L, i + q * nbf);
+#pragma unroll
+        for (int q = 1; q < P; ++q)
+            if (k > 0) v[q] = cmul(v[q], tw_get(tw, q * tj, sign));
+        dft_small<C, P>(v, tw, n, sign);
+        const int base = hi * Ns * P + k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) st(L, base + q * Ns, v[q]);
+    }
+}
+
+// shared-memory line accessor: element e of line L at b[L*ls + e*es]
+template <typename C>
+struct SmemLines {
+    C* b;
+    int ls, es;
+    HPSI_D C operator()(int L, int e) const { return b[L * ls + e * es]; }
+    HPSI_D void operator()(int L, int e, C v) const { b[L * ls + e * es] = v; }
+};
+
+template <typename C, bool LINE_FAST, bool WIDE, typename LD, typename ST>
+HPSI_D void fft_stage_io_p(int p, const LD& ld, const ST& st, int n, const FastDiv& nsf, const FastDiv& nlf,
+                           const C* tw, int sign)
+{
+    switch (p) {
+        case 8: fft_stage_io<C, 8, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+        case 9: fft_stage_io<C, 9, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+        case 2: fft_stage_io<C, 2, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+        case 3: fft_stage_io<C, 3, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+        case 4: fft_stage_io<C, 4, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+        case 5: fft_stage_io<C, 5, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+        default:
+            if constexpr (WIDE) {
+                switch (p) {
+                    case 7: fft_stage_io<C, 7, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+                    case 11: fft_stage_io<C, 11, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+                    case 13: fft_stage_io<C, 13, LINE_FAST>(ld, st, n, nsf, nlf, tw, sign); break;
+                    default: break;
+                }
+            }
+            break;
+    }
+}
+
+// Which buffer the last stage of fft_lines_io reads: 0 = ld, 1 = bufA, 2 = bufB.
+HPSI_HD int fft_last_read(const FftLen& L) { return L.nst <= 1 ? 0 : (((L.nst - 2) % 2 == 0) ? 1 : 2); }
+
+// Transform of nl lines: stage 0 reads through ld, the last stage writes
+// through st, stages in between ping-pong through bufA (written by stages
+// 0, 2, ...) and bufB (stages 1, 3, ...), laid out with line stride ls and
+// element stride es.  ld must not read bufA.  A barrier separates stages; the
+// caller synchronises after the last one.  Returns the buffer that the last
+// stage read (so the caller may direct st to the other one): 0 = ld, 1 = bufA,
+// 2 = bufB.
+template <typename C, bool LINE_FAST, bool WIDE, typename LD, typename ST>
+HPSI_D int fft_lines_io(const LD& ld, const ST& st, C* bufA, C* bufB, const FftLen& L, const FastDiv& nlf, int ls,
+                        int es, const C* tw, int sign)
+{
+    if (L.nst == 0) {
+        for (int t = threadIdx.x; t < (int)nlf.d; t += blockDim.x) st(t, 0, ld(t, 0));
+        return 0;
+    }
+    const SmemLines<C> A{bufA, ls, es}, B{bufB, ls, es};
+    for (int s = 0; s < L.nst; ++s) {
+        const bool first = s == 0, last = s == L.nst - 1;
+        const SmemLines<C>& in = ((s - 1) % 2 == 0) ? A : B;
+        const SmemLines<C>& out = (s % 2 == 0) ? A : B;
+        const int p = L.rad[s];
+        if (first && last) fft_stage_io_p<C, LINE_FAST, WIDE>(p, ld, st, L.n, L.ns[s], nlf, tw, sign);
+        else if (first) fft_stage_io_p<C, LINE_FAST, WIDE>(p, ld, out, L.n, L.ns[s], nlf, tw, sign);
+        else if (last) fft_stage_io_p<C, LINE_FAST, WIDE>(p, in, st, L.n, L.ns[s], nlf, tw, sign);
+        else fft_stage_io_p<C, LINE_FAST, WIDE>(p, in, out, L.n, L.ns[s], nlf, tw, sign);
+        if (!last) __syncthreads();
+    }
+    return L.nst == 1 ? 0 : (((L.nst - 2) % 2 == 0) ? 1 : 2);
+}
+
 // Radices compiled into a stage: the narrow set {2,3,4,5,8,9} covers the
 // usual 2^a 3^b 5^c grids with few registers; WIDE adds 7, 11 and 13.
 template <typename C, bool LINE_FAST, bool WIDE>

@@ -65,6 +65,7 @@ struct LocalArgs {
     FastDiv nl_z;           // z-lines of a plane: n2
     FastDiv nl_y;           // y-lines of a plane: n3
     FastDiv nl_x;           // x-lines of an x-pass block: kt*bb
+    FastDiv kt_f;           // divisor by kt
 };
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64);

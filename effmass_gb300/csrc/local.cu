@@ -30,7 +30,19 @@ template <> struct Cfg<double2> { static constexpr int plane_threads = 256, plan
 // Shared-memory planes use a padded row stride n3p = n3 + 1 (odd) so that
 // both the z-lines (rows) and the y-lines (columns) are read and written by
 // consecutive threads without bank conflicts (both transforms walk lines
-// fastest: LINE_FAST).
+// fastest: LINE_FAST).  The first stage of a transform reads its source
+// directly and the last stage writes its destination directly
+// (fft_lines_io), so a plane costs two barriers per axis.
+
+// global plane of T as y-lines: line = k, element = j
+template <typename C>
+struct PlaneGlobal {
+    C* p;
+    int n3;
+    HPSI_D C operator()(int L, int e) const { return p[e * n3 + L]; }
+    HPSI_D void operator()(int L, int e, C v) const { p[e * n3 + L] = v; }
+};
+
 template <typename C, bool WIDE>
 __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
@@ -58,19 +70,69 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) g2r_
         }
     }
     __syncthreads();
-    int cur = fft_lines<C, true, WIDE>(b0, b1, 0, a.Lz, a.nl_z, n3p, 1, twz, +1);
-    cur = fft_lines<C, true, WIDE>(b0, b1, cur, a.Ly, a.nl_y, 1, n3p, twy, +1);
-    const C* res = cur ? b1 : b0;
-    C* out = T + ((size_t)b * a.nxs + p) * n23;
-    for (int t = threadIdx.x; t < n23; t += blockDim.x) {
-        int j = t / n3, k = t - j * n3;
-        out[t] = res[j * n3p + k];
-    }
+    // z (rows of b0): intermediates in b1 then b0; output to the buffer the last stage does not read
+    const int rz = fft_last_read(a.Lz);
+    C* zo = (rz == 1) ? b0 : b1;
+    fft_lines_io<C, true, WIDE>(SmemLines<C>{b0, n3p, 1}, SmemLines<C>{zo, n3p, 1}, b1, b0, a.Lz, a.nl_z, n3p, 1,
+                                twz, +1);
+    __syncthreads();
+    // y (columns), last stage straight to T
+    C* zother = (zo == b0) ? b1 : b0;
+    fft_lines_io<C, true, WIDE>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{T + ((size_t)b * a.nxs + p) * n23, n3},
+                                zother, zo, a.Ly, a.nl_y, 1, n3p, twy, +1);
 }
 
 // x pass: a block owns the x-lines of (j, k0..k0+KT) for BB consecutive bands
 // (NL = KT*BB lines, line L = bb*KT + kk, element x at [x*NL + L]); the V tile
-// is loaded once per block.
+// is loaded once per block.  The G->r transform reads the sphere planes of T
+// directly (zero for other x) and multiplies by V as it stores; the r->G
+// transform stores the sphere planes back into T.
+template <typename C>
+struct XLoad {
+    const C* T;
+    const int* xpl;      // smem: plane index of x or -1
+    size_t plane;        // n2*n3
+    size_t base;         // j*n3 + k0
+    int nxs, KT, kt, nbb, bb0;
+    FastDiv ktf;
+    HPSI_D C operator()(int L, int x) const
+    {
+        const int bb = (int)fdiv((uint32_t)L, ktf), kk = L - bb * KT;
+        const int pl = xpl[x];
+        if (pl < 0 || bb >= nbb || kk >= kt) return cmake<C>(0, 0);
+        return T[((size_t)(bb0 + bb) * nxs + pl) * plane + base + kk];
+    }
+};
+
+template <typename C, typename V>
+struct XStoreV {
+    C* buf;
+    const V* vt;         // smem V tile [x*KT + kk]
+    int NL, KT;
+    FastDiv ktf;
+    HPSI_D void operator()(int L, int x, C v) const
+    {
+        const int bb = (int)fdiv((uint32_t)L, ktf), kk = L - bb * KT;
+        buf[x * NL + L] = cscale(v, (typename Real<C>::type)vt[x * KT + kk]);
+    }
+};
+
+template <typename C>
+struct XStore {
+    C* T;
+    const int* xpl;
+    size_t plane, base;
+    int nxs, KT, kt, nbb, bb0;
+    FastDiv ktf;
+    HPSI_D void operator()(int L, int x, C v) const
+    {
+        const int bb = (int)fdiv((uint32_t)L, ktf), kk = L - bb * KT;
+        const int pl = xpl[x];
+        if (pl < 0 || bb >= nbb || kk >= kt) return;
+        T[((size_t)(bb0 + bb) * nxs + pl) * plane + base + kk] = v;
+    }
+};
+
 template <typename C, typename V, bool WIDE>
 __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
                                               const C* __restrict__ tw_x_g)
@@ -81,44 +143,32 @@ __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb
     C* b1 = b0 + n1 * NL;
     C* twx = b1 + n1 * NL;
     V* vt = reinterpret_cast<V*>(twx + n1);
+    int* xpl = reinterpret_cast<int*>(vt + n1 * KT);
     const int j = blockIdx.y;
     const int k0 = blockIdx.x * KT;
     const int kt = min(KT, n3 - k0);
     const int bb0 = blockIdx.z * BB;
     const int nbb = min(BB, nb - bb0);
-    const int nxs = a.nxs;
     const size_t plane = (size_t)n2 * n3;
-    for (int t = threadIdx.x; t < n1; t += blockDim.x) twx[t] = tw_x_g[t];
-    for (int t = threadIdx.x; t < n1 * kt; t += blockDim.x) {
-        int x = t / kt, kk = t % kt;
-        vt[x * KT + kk] = vloc[((size_t)x * n2 + j) * n3 + k0 + kk];
-    }
-    for (int t = threadIdx.x; t < n1 * NL; t += blockDim.x) b0[t] = cmake<C>(0, 0);
-    __syncthreads();
-    const int per_plane = nbb * kt;
-    for (int t = threadIdx.x; t < nxs * per_plane; t += blockDim.x) {
-        int pp = t / per_plane, r = t - pp * per_plane;
-        int bb = r / kt, kk = r - bb * kt;
-        const C* src = T + ((size_t)(bb0 + bb) * nxs + pp) * plane + (size_t)j * n3 + k0 + kk;
-        b0[a.plane_x[pp] * NL + bb * KT + kk] = *src;
+    for (int t = threadIdx.x; t < n1; t += blockDim.x) { twx[t] = tw_x_g[t]; xpl[t] = -1; }
+    for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) {
+        int x = t / KT, kk = t % KT;
+        vt[t] = kk < kt ? vloc[((size_t)x * n2 + j) * n3 + k0 + kk] : (V)0;
     }
     __syncthreads();
-    int cur = fft_lines<C, true, WIDE>(b0, b1, 0, a.Lx, a.nl_x, 1, NL, twx, +1);
-    C* res = cur ? b1 : b0;
-    for (int t = threadIdx.x; t < n1 * NL; t += blockDim.x) {
-        int x = t / NL, L = t - x * NL;
-        int kk = L % KT;
-        res[t] = cscale(res[t], (typename Real<C>::type)vt[x * KT + kk]);
-    }
+    for (int t = threadIdx.x; t < a.nxs; t += blockDim.x) xpl[a.plane_x[t]] = t;
     __syncthreads();
-    cur = fft_lines<C, true, WIDE>(b0, b1, cur, a.Lx, a.nl_x, 1, NL, twx, -1);
-    res = cur ? b1 : b0;
-    for (int t = threadIdx.x; t < nxs * per_plane; t += blockDim.x) {
-        int pp = t / per_plane, r = t - pp * per_plane;
-        int bb = r / kt, kk = r - bb * kt;
-        C* dst = T + ((size_t)(bb0 + bb) * nxs + pp) * plane + (size_t)j * n3 + k0 + kk;
-        *dst = res[a.plane_x[pp] * NL + bb * KT + kk];
-    }
+    const size_t base = (size_t)j * n3 + k0;
+    const XLoad<C> ld{T, xpl, plane, base, a.nxs, KT, kt, nbb, bb0, a.kt_f};
+    // G->r, times V, into the buffer the last stage does not read
+    const int r = fft_last_read(a.Lx);
+    C* vo = (r == 1) ? b1 : b0;
+    fft_lines_io<C, true, WIDE>(ld, XStoreV<C, V>{vo, vt, NL, KT, a.kt_f}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
+    __syncthreads();
+    // r->G, back into the sphere planes of T
+    C* vother = (vo == b0) ? b1 : b0;
+    const XStore<C> stT{T, xpl, plane, base, a.nxs, KT, kt, nbb, bb0, a.kt_f};
+    fft_lines_io<C, true, WIDE>(SmemLines<C>{vo, 1, NL}, stT, vother, vo, a.Lx, a.nl_x, 1, NL, twx, -1);
 }
 
 template <typename C, bool WIDE>
@@ -136,15 +186,22 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) r2g_
     const int b = blockIdx.y;
     for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
     for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
-    const C* in = T + ((size_t)b * a.nxs + p) * n23;
-    for (int t = threadIdx.x; t < n23; t += blockDim.x) {
-        int j = t / n3, k = t - j * n3;
-        b0[j * n3p + k] = in[t];
-    }
     __syncthreads();
-    int cur = fft_lines<C, true, WIDE>(b0, b1, 0, a.Ly, a.nl_y, 1, n3p, twy, -1);
-    cur = fft_lines<C, true, WIDE>(b0, b1, cur, a.Lz, a.nl_z, n3p, 1, twz, -1);
-    const C* res = cur ? b1 : b0;
+    // y (columns) straight from T; output into the buffer the last stage does not read
+    const int ry = fft_last_read(a.Ly);
+    C* yo = (ry == 1) ? b1 : b0;
+    fft_lines_io<C, true, WIDE>(PlaneGlobal<C>{const_cast<C*>(T) + ((size_t)b * a.nxs + p) * n23, n3},
+                                SmemLines<C>{yo, 1, n3p}, b0, b1, a.Ly, a.nl_y, 1, n3p, twy, -1);
+    __syncthreads();
+    // z (rows)
+    C* yother = (yo == b0) ? b1 : b0;
+    const int rz = fft_last_read(a.Lz);
+    // intermediates: bufA = yother, bufB = yo; last stage reads yo (rz == 2) or yother (rz == 1) or yo via ld (rz == 0)
+    C* zo = (rz == 1) ? yo : yother;
+    fft_lines_io<C, true, WIDE>(SmemLines<C>{yo, n3p, 1}, SmemLines<C>{zo, n3p, 1}, yother, yo, a.Lz, a.nl_z, n3p, 1,
+                                twz, -1);
+    __syncthreads();
+    const C* res = zo;
     const double2* ps = psi + (size_t)b * a.npw;
     double2* hp = hpsi + (size_t)b * a.npw;
     const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
@@ -172,7 +229,7 @@ template <typename C, typename V>
 static size_t xpass_smem(const LocalArgs& a)
 {
     const size_t NL = (size_t)a.kt * a.bb;
-    return sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt;
+    return sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt + sizeof(int) * a.n1;
 }
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64)
@@ -199,6 +256,7 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
     a->nl_z = make_fastdiv((uint32_t)a->n2);
     a->nl_y = make_fastdiv((uint32_t)a->n3);
     a->nl_x = make_fastdiv((uint32_t)(a->kt * a->bb));
+    a->kt_f = make_fastdiv((uint32_t)a->kt);
 }
 
 template <typename C, typename V, bool WIDE>
