@@ -196,6 +196,21 @@ def run_gb300(args, rank, world, local):
         torch.cuda.synchronize()
         fp64 = nb / (f0.elapsed_time(f1) / reps * 1e-3)
 
+    # dH/dk_{x,y,z}|psi> on the same block (the 64-atom workload asks for it beside H|psi>)
+    from effmass_gb300.hamiltonian import GradHPsi
+    gx, gy, gz = (torch.zeros_like(psi_d) for _ in range(3))
+    gout = GradHPsi(gx, gy, gz)
+    H.grad_apply(0, nb, psi_d, gout, args.prec)
+    torch.cuda.synchronize()
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    for _ in range(args.steps):
+        H.grad_apply(0, nb, psi_d, gout, args.prec)
+    q1.record(stream)
+    torch.cuda.synchronize()
+    grad_value = world * nb / (q0.elapsed_time(q1) / args.steps * 1e-3)
+    del gx, gy, gz, gout
+
     # end to end through the public API with pinned host buffers
     psi_h = torch.from_numpy(psi).pin_memory()
     hpsi_h = torch.zeros_like(psi_h).pin_memory()
@@ -278,6 +293,7 @@ def run_gb300(args, rank, world, local):
                                                                                        psi.nbytes >> 20)},
         "rel_err_vs_fp64": err, "band_energy_max_abs_diff_Ha": de,
         "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
+        "grad_value": grad_value, "grad_unit": "band-apps/s of dH/dk_{x,y,z}|psi> (all three directions)",
         "e2e": e2e, "roofline": roof, "roofline_gemm": roof_gemm, "phases": phases, "gpu_launches": gpu_launches,
         "cpu_baseline": cpu, "clocks": clk,
     }

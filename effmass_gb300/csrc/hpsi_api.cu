@@ -51,6 +51,9 @@ struct KSlot {
     int tc_fmt = -1;               // -1 none, 0 FP16 split, 1 BF16 split
     unsigned char* tc_mem = nullptr;
     TcOperand tc_proj, tc_expand;
+    int tcg_fmt = -1;              // gradient operands (4P-row projection, per-direction expansion)
+    unsigned char* tcg_mem = nullptr;
+    TcOperand tcg_proj, tcg_exp[3];
 };
 
 template <typename T>
@@ -72,7 +75,7 @@ void slot_free(KSlot& s)
 {
     dfree(s.d_kin); dfree(s.d_kvec); dfree(s.d_g); dfree(s.d_q); dfree(s.d_trig); dfree(s.d_ylm);
     dfree(s.d_beta); dfree(s.d_dbeta0); dfree(s.d_sf); dfree(s.d_plane); dfree(s.d_rows); dfree(s.d_lam);
-    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem);
+    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem); dfree(s.tcg_mem);
     s = KSlot();
 }
 
@@ -662,6 +665,100 @@ static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     return HPSI_OK;
 }
 
+static int ensure_tc_grad(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
+{
+    if (s.P == 0 || s.npw == 0) return HPSI_OK;
+    if (s.tcg_fmt == fmt && s.tcg_mem) return HPSI_OK;
+    int rc;
+    if ((rc = ensure_proj<float2>(c, s, true, st))) return rc;
+    dfree(s.tcg_mem);
+    s.tcg_fmt = -1;
+    const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(4 * (size_t)s.P);
+    Carver cv;
+    const size_t o1h = cv.take<uint16_t>((size_t)4 * s.P * k1), o1l = cv.take<uint16_t>((size_t)4 * s.P * k1);
+    const size_t o1s = cv.take<float>((size_t)4 * s.P);
+    size_t oh[3], ol[3], os[3];
+    const size_t z0 = cv.off;
+    for (int a = 0; a < 3; ++a) {
+        oh[a] = cv.take<uint16_t>((size_t)s.npw * k2);
+        ol[a] = cv.take<uint16_t>((size_t)s.npw * k2);
+        os[a] = cv.take<float>((size_t)s.npw);
+    }
+    const size_t z1 = cv.off;
+    const size_t ocm = cv.take<float>((size_t)s.npw);
+    CUDA_TRY(c, dalloc(&s.tcg_mem, cv.off));
+    CUDA_TRY(c, cudaMemsetAsync(s.tcg_mem + z0, 0, z1 - z0, st));  // K padding must read as zero
+    s.tcg_proj = TcOperand{s.tcg_mem + o1h, s.tcg_mem + o1l, reinterpret_cast<float*>(s.tcg_mem + o1s), k1};
+    for (int a = 0; a < 3; ++a)
+        s.tcg_exp[a] = TcOperand{s.tcg_mem + oh[a], s.tcg_mem + ol[a], reinterpret_cast<float*>(s.tcg_mem + os[a]), k2};
+    int h = c->prof.open(PH_BUILD, st);
+    CUDA_TRY(c, tc_build_grad_operands(s.pr32, s.P, s.npw, fmt == 0, &s.tcg_proj, s.tcg_exp,
+                                       reinterpret_cast<float*>(s.tcg_mem + ocm), st));
+    c->prof.close(h, st);
+    s.tcg_fmt = fmt;
+    return HPSI_OK;
+}
+
+static size_t tc_grad_ws(const KSlot& s, int nb)
+{
+    const int NB = tc_band_rows(nb);
+    const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(4 * (size_t)s.P);
+    const int ns = tc_proj_splits(4 * s.P, nb, k1);
+    Carver cv;
+    cv.take<uint16_t>((size_t)NB * k1);
+    cv.take<uint16_t>((size_t)NB * k1);
+    cv.take<float>((size_t)NB);
+    cv.take<float>((size_t)ns * 4 * s.P * NB);
+    cv.take<float2>((size_t)4 * s.P * nb);
+    cv.take<float2>((size_t)2 * s.P * nb);
+    cv.take<uint16_t>((size_t)NB * k2);
+    cv.take<uint16_t>((size_t)NB * k2);
+    cv.take<float>((size_t)NB);
+    cv.take<unsigned>((size_t)nb);
+    return cv.off;
+}
+
+// d_alpha += nonlocal part of dH/dk_alpha psi on the tensor cores (device pointers)
+static int tc_grad_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* d[3], unsigned char* ws,
+                            cudaStream_t st)
+{
+    if (s.P == 0 || nb == 0) return HPSI_OK;
+    const bool fp16 = s.tcg_fmt == 0;
+    const int NB = tc_band_rows(nb), P = s.P, P4 = 4 * s.P;
+    const size_t k1 = s.tcg_proj.ldk, k2 = s.tcg_exp[0].ldk;
+    const int ns = tc_proj_splits(P4, nb, k1);
+    Carver cv;
+    const size_t ob1h = cv.take<uint16_t>((size_t)NB * k1), ob1l = cv.take<uint16_t>((size_t)NB * k1);
+    const size_t ob1s = cv.take<float>((size_t)NB);
+    const size_t opart = cv.take<float>((size_t)ns * P4 * NB);
+    const size_t ow = cv.take<float2>((size_t)P4 * nb);
+    const size_t ow2 = cv.take<float2>((size_t)2 * P * nb);
+    const size_t ob2h = cv.take<uint16_t>((size_t)NB * k2), ob2l = cv.take<uint16_t>((size_t)NB * k2);
+    const size_t ob2s = cv.take<float>((size_t)NB);
+    unsigned* rowmax = reinterpret_cast<unsigned*>(ws + cv.take<unsigned>((size_t)nb));
+    TcOperand B1{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
+    TcOperand B2{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
+    float2* W = reinterpret_cast<float2*>(ws + ow);    // [4P][nb]: <p|psi>, <dp_x|psi>, <dp_y|psi>, <dp_z|psi> (x lambda)
+    float2* W2 = reinterpret_cast<float2*>(ws + ow2);  // [2P][nb]: (<dp_a|psi>, <p|psi>) for one direction
+    int h = c->prof.open(PH_OTHER, st);
+    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &B1, rowmax, st));
+    c->prof.close(h, st);
+    CUDA_TRY(c, tc_projection(s.tcg_proj, P4, B1, nb, ns, fp16, reinterpret_cast<float*>(ws + opart), s.d_lam, P, W,
+                              c->d_err, st, &c->prof));
+    const size_t blk = (size_t)P * nb * sizeof(float2);
+    for (int a = 0; a < 3; ++a) {
+        if (!d[a]) continue;
+        // out_a += sum_p lambda <dp_a|psi> p + lambda <p|psi> dp_a: K = (p block, dp_a block)
+        CUDA_TRY(c, cudaMemcpyAsync(W2, W + (size_t)(1 + a) * P * nb, blk, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(W2 + (size_t)P * nb, W, blk, cudaMemcpyDeviceToDevice, st));
+        h = c->prof.open(PH_OTHER, st);
+        CUDA_TRY(c, tc_w_operand(W2, 2 * P, nb, fp16, &B2, rowmax, st));
+        c->prof.close(h, st);
+        CUDA_TRY(c, tc_expansion(s.tcg_exp[a], s.npw, B2, nb, fp16, d[a], c->d_err, st, &c->prof));
+    }
+    return HPSI_OK;
+}
+
 // After a synchronising call: report a bounded-wait timeout of the tensor-core kernels.
 static int check_device_flag(hpsi_ctx* c)
 {
@@ -793,6 +890,19 @@ static size_t grad_ws(const KSlot& s, int nb)
     return nonlocal_ws<C, Acc>(s, nb, 4);
 }
 
+static int grad_tc(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* d[3], unsigned char* work, int fmt,
+                   cudaStream_t st)
+{
+    const size_t nel = (size_t)nb * s.npw;
+    int h = c->prof.open(PH_OTHER, st);
+    grad_kinetic_kernel<<<ceil_div((long)nel, 256), 256, 0, st>>>(s.npw, nb, s.d_kvec, psi, d[0], d[1], d[2]);
+    c->prof.close(h, st);
+    CUDA_TRY(c, cudaGetLastError());
+    int rc;
+    if ((rc = ensure_tc_grad(c, s, fmt, st))) return rc;
+    return tc_grad_nonlocal(c, s, nb, psi, d, work, st);
+}
+
 extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* dx, double* dy, double* dz,
                                int flags, void* stream)
 {
@@ -802,7 +912,9 @@ extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_,
     if (nb > 0 && !psi_) return fail(c, HPSI_ERR_BAD_ARG, "psi NULL");
     if (nb == 0 || s->npw == 0 || (!dx && !dy && !dz)) return HPSI_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    const bool fp64 = (flags & HPSI_PREC_MASK) == HPSI_PREC_FP64;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool fp64 = prec == HPSI_PREC_FP64;
+    const bool tc = prec == HPSI_PREC_TC || prec == HPSI_PREC_TC_BF16;
     const bool dev = flags & HPSI_DEVICE_PTRS;
     const size_t nel = (size_t)nb * s->npw;
     double* outs[3] = {dx, dy, dz};
@@ -812,7 +924,7 @@ extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_,
     for (int a = 0; a < 3; ++a)
         if (!dev && outs[a]) o_out[a] = cv.take<double2>(nel);
     size_t o_work = cv.off;
-    size_t wn = fp64 ? grad_ws<double2, double2>(*s, nb) : grad_ws<float2, float2>(*s, nb);
+    size_t wn = fp64 ? grad_ws<double2, double2>(*s, nb) : (tc ? tc_grad_ws(*s, nb) : grad_ws<float2, float2>(*s, nb));
     if ((rc = ws_reserve(c, o_work + wn))) return rc;
     const double2* psi = (const double2*)psi_;
     double2* d[3] = {(double2*)dx, (double2*)dy, (double2*)dz};
@@ -826,13 +938,18 @@ extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_,
         }
     }
     unsigned char* work = c->ws + o_work;
-    rc = fp64 ? grad_device<double2, double2>(c, *s, nb, psi, d, work, st)
-              : grad_device<float2, float2>(c, *s, nb, psi, d, work, st);
+    if (tc) rc = grad_tc(c, *s, nb, psi, d, work, prec == HPSI_PREC_TC ? 0 : 1, st);
+    else
+        rc = fp64 ? grad_device<double2, double2>(c, *s, nb, psi, d, work, st)
+                  : grad_device<float2, float2>(c, *s, nb, psi, d, work, st);
     if (rc) return rc;
     if (!dev)
         for (int a = 0; a < 3; ++a)
             if (outs[a]) CUDA_TRY(c, cudaMemcpyAsync(outs[a], d[a], nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
-    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (!dev || (flags & HPSI_SYNC)) {
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        if (tc && (rc = check_device_flag(c))) return rc;
+    }
     return HPSI_OK;
 }
 

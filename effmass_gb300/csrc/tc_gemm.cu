@@ -35,7 +35,7 @@ constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
 constexpr int A_TILE = BM * BK * 2;   // bytes of one A piece per stage (16 KB)
 constexpr int B_TILE = BN * BK * 2;   // 32 KB
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
-constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t TMEM_COLS = 512;  // two 256-column FP32 accumulators, alternating by k-tile
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -216,10 +216,13 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
                 const uint64_t adv = (uint64_t)((kk * 32) >> 4);  // 16 elements = 32 bytes along K
-                const uint32_t first = (it == 0 && kk == 0) ? 0u : 1u;
-                tc_mma(tmem, ah + adv, bh + adv, idesc, first);
-                tc_mma(tmem, ah + adv, bl + adv, idesc, 1u);
-                tc_mma(tmem, al + adv, bh + adv, idesc, 1u);
+                // even k-tiles accumulate into columns [0,256), odd ones into [256,512):
+                // two half-length FP32 accumulation chains, summed by the epilogue
+                const uint32_t acc = tmem + (uint32_t)((it & 1) * BN);
+                const uint32_t first = (it < 2 && kk == 0) ? 0u : 1u;
+                tc_mma(acc, ah + adv, bh + adv, idesc, first);
+                tc_mma(acc, ah + adv, bl + adv, idesc, 1u);
+                tc_mma(acc, al + adv, bh + adv, idesc, 1u);
             }
             tc_commit(&sh->empty[s]);  // stage reusable once these MMAs have read it
         }
@@ -237,12 +240,18 @@ __global__ void __launch_bounds__(192, 1)
         const bool go = __all_sync(0xffffffffu, ok && nk > 0 && !*(volatile uint32_t*)&sh->abort_flag);
         if (go) {
             const float sa = (row < M) ? ep.sa_scale[row] : 0.f;
+            const bool two = nk > 1;  // the odd accumulator holds data only with two or more k-tiles
             if (MODE == 0) {
                 float* out = ep.part + ((size_t)blockIdx.z * M + row) * (size_t)N + n0;
 #pragma unroll 1
                 for (int c0 = 0; c0 < BN; c0 += 32) {
-                    float v[32];
+                    float v[32], w[32];
                     tmem_ld32(tbase + c0, v);
+                    if (two) {
+                        tmem_ld32(tbase + BN + c0, w);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) v[i] += w[i];
+                    }
                     if (row < M) {
 #pragma unroll
                         for (int i = 0; i < 32; ++i) {
@@ -255,9 +264,17 @@ __global__ void __launch_bounds__(192, 1)
                 // columns [0,128): real parts of bands 128*blockIdx.y + j, [128,256): imaginary
 #pragma unroll 1
                 for (int c0 = 0; c0 < 128; c0 += 32) {
-                    float re[32], im[32];
+                    float re[32], im[32], w[32];
                     tmem_ld32(tbase + c0, re);
                     tmem_ld32(tbase + 128 + c0, im);
+                    if (two) {
+                        tmem_ld32(tbase + BN + c0, w);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) re[i] += w[i];
+                        tmem_ld32(tbase + BN + 128 + c0, w);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) im[i] += w[i];
+                    }
                     if (row < M) {
 #pragma unroll
                         for (int i = 0; i < 32; ++i) {
@@ -352,8 +369,10 @@ __global__ void split_rows_kernel(const float2* __restrict__ pr, int npw, size_t
     }
 }
 
-// Column maxima of Pr over projectors: cmax[g] = max_p max(|re|, |im|)
-__global__ void col_max_kernel(const float2* __restrict__ pr, int P, int npw, float* cmax)
+// Column maxima over projectors: cmax[g] = max_p max(|re|, |im|) of pr and,
+// if given, of pr2 (the two row blocks that share one row of the transposed operand)
+__global__ void col_max_kernel(const float2* __restrict__ pr, const float2* __restrict__ pr2, int P, int npw,
+                               float* cmax)
 {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= npw) return;
@@ -361,13 +380,17 @@ __global__ void col_max_kernel(const float2* __restrict__ pr, int P, int npw, fl
     for (int p = 0; p < P; ++p) {
         float2 v = pr[(size_t)p * npw + g];
         mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+        if (pr2) {
+            float2 w = pr2[(size_t)p * npw + g];
+            mx = fmaxf(mx, fmaxf(fabsf(w.x), fabsf(w.y)));
+        }
     }
     cmax[g] = mx;
 }
 
 // Expansion A: Pr^T rows g: [hi|lo][g][2p + c], scaled by the row scale of g
 template <typename T>
-__global__ void transpose_split_kernel(const float2* __restrict__ pr, int P, int npw, size_t ldk,
+__global__ void transpose_split_kernel(const float2* __restrict__ pr, int P, int npw, size_t ldk, size_t koff,
                                        const float* __restrict__ cmax, T* hi, T* lo, float* inv_scale, bool fp16)
 {
     __shared__ float2 tile[32][33];
@@ -385,7 +408,7 @@ __global__ void transpose_split_kernel(const float2* __restrict__ pr, int P, int
         if (blockIdx.y == 0 && tx == 0) inv_scale[g] = 1.f / sc;
         const float2 v = tile[tx][r];
         const int p = p0 + tx;
-        const size_t k = 2 * (size_t)p;
+        const size_t k = koff + 2 * (size_t)p;
         if (k + 1 < ldk) {
             split_store<T>(v.x * sc, hi + (size_t)g * ldk + k, lo + (size_t)g * ldk + k);
             split_store<T>(v.y * sc, hi + (size_t)g * ldk + k + 1, lo + (size_t)g * ldk + k + 1);
@@ -545,15 +568,48 @@ cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, 
         split_rows_kernel<__nv_bfloat16><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__nv_bfloat16*)proj->hi,
                                                             (__nv_bfloat16*)proj->lo, proj->inv_scale, false);
     }
-    col_max_kernel<<<ceil_div(npw, 256), 256, 0, st>>>(pr, P, npw, cmax_scratch);
+    col_max_kernel<<<ceil_div(npw, 256), 256, 0, st>>>(pr, nullptr, P, npw, cmax_scratch);
     dim3 g(ceil_div(npw, 32), ceil_div(P, 32));
     if (fp16)
-        transpose_split_kernel<__half><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, cmax_scratch, (__half*)expand->hi,
+        transpose_split_kernel<__half><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, 0, cmax_scratch, (__half*)expand->hi,
                                                           (__half*)expand->lo, expand->inv_scale, true);
     else
-        transpose_split_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, cmax_scratch,
+        transpose_split_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, 0, cmax_scratch,
                                                                  (__nv_bfloat16*)expand->hi,
                                                                  (__nv_bfloat16*)expand->lo, expand->inv_scale, false);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_build_grad_operands(const float2* pr4, int P, int npw, bool fp16, TcOperand* proj4, TcOperand* exp3,
+                                   float* cmax_scratch, cudaStream_t st)
+{
+    if (P == 0 || npw == 0) return cudaSuccess;
+    const int P4 = 4 * P;
+    if (fp16)
+        split_rows_kernel<__half><<<P4, 256, 0, st>>>(pr4, npw, proj4->ldk, (__half*)proj4->hi, (__half*)proj4->lo,
+                                                      proj4->inv_scale, true);
+    else
+        split_rows_kernel<__nv_bfloat16><<<P4, 256, 0, st>>>(pr4, npw, proj4->ldk, (__nv_bfloat16*)proj4->hi,
+                                                             (__nv_bfloat16*)proj4->lo, proj4->inv_scale, false);
+    const size_t PN = (size_t)P * npw;
+    dim3 g(ceil_div(npw, 32), ceil_div(P, 32));
+    for (int a = 0; a < 3; ++a) {
+        // row g of the alpha operand: (Pr[p][g], p < P) then (dPr_alpha[p][g], p < P), one row scale
+        const float2* dpa = pr4 + (size_t)(1 + a) * PN;
+        TcOperand* E = &exp3[a];
+        col_max_kernel<<<ceil_div(npw, 256), 256, 0, st>>>(pr4, dpa, P, npw, cmax_scratch);
+        for (int blk = 0; blk < 2; ++blk) {
+            const float2* src = blk == 0 ? pr4 : dpa;
+            const size_t koff = blk == 0 ? 0 : 2 * (size_t)P;
+            if (fp16)
+                transpose_split_kernel<__half><<<g, 256, 0, st>>>(src, P, npw, E->ldk, koff, cmax_scratch,
+                                                                  (__half*)E->hi, (__half*)E->lo, E->inv_scale, true);
+            else
+                transpose_split_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(src, P, npw, E->ldk, koff, cmax_scratch,
+                                                                         (__nv_bfloat16*)E->hi, (__nv_bfloat16*)E->lo,
+                                                                         E->inv_scale, false);
+        }
+    }
     return cudaGetLastError();
 }
 
@@ -598,14 +654,26 @@ cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B
     return cudaGetLastError();
 }
 
+// Split-K of the projection: at most 48 k-tiles per CTA (short FP32
+// accumulation chains: with the two alternating accumulators at most 24
+// k-tiles, 288 MMAs, add into one accumulator), rounded up so that the CTAs
+// fill whole waves of the 148 SMs the kernel plans for.
 int tc_proj_splits(int P, int nb, size_t ldk)
 {
     const int tiles = ceil_div(P, BM) * (tc_band_rows(nb) / BN);
     const int ktiles = (int)(ldk / BK);
-    int s = 148 / tiles;
-    if (s < 1) s = 1;
-    if (s > ktiles) s = ktiles;
-    return s;
+    int s = ceil_div(ktiles, 48);
+    if (tiles * s < 148) s = ceil_div(148, tiles);
+    // cost model: waves x k-tiles per split, plus the partial-sum reduction
+    int best = s;
+    double best_cost = 1e300;
+    for (int c = s; c <= 2 * s && c <= ktiles; ++c) {
+        const double cost = (double)ceil_div(tiles * c, 148) * ceil_div(ktiles, c) + c / 8.0;
+        if (cost < best_cost) { best = c; best_cost = cost; }
+    }
+    if (best > ktiles) best = ktiles;
+    if (best < 1) best = 1;
+    return best;
 }
 
 // A: rows M, B: rows N (= tc_band_rows(nb)); one launch

@@ -30,6 +30,11 @@ int tc_proj_splits(int P, int nb, size_t ldk);
 // and the expansion operand Pr^T [npw][2P] (expand buffers must be zeroed).
 cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, TcOperand* proj, TcOperand* expand,
                                    float* cmax_scratch, cudaStream_t st);
+// Gradient operands from the stacked c64 matrices [4P][npw] (Pr, dPr_x, dPr_y,
+// dPr_z): the projection operand [4P][2npw] and, per direction alpha, the
+// expansion operand [npw][4P] = (Pr^T | dPr_alpha^T) (buffers must be zeroed).
+cudaError_t tc_build_grad_operands(const float2* pr4, int P, int npw, bool fp16, TcOperand* proj4, TcOperand* exp3,
+                                   float* cmax_scratch, cudaStream_t st);
 // Band operand of the projection from psi (complex128 [nb][npw]); rowmax: nb scratch words.
 cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, unsigned* rowmax,
                             cudaStream_t st);

@@ -50,7 +50,7 @@ def test_hpsi_matches_reference(H_of, case, prec):
     assert rel_err(out, href) <= TOL[prec], (case, prec, rel_err(out, href))
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "tc", "tc_bf16"])
 @pytest.mark.parametrize("case", CASES)
 def test_grad_matches_reference(H_of, case, prec):
     from effmass_gb300.hamiltonian import GradHPsi
@@ -211,6 +211,17 @@ def test_full_size_mixed_vs_fp64_and_hermitian(sc64):
         assert rel_err(hm, h64) <= TOL[prec], (prec, rel_err(hm, h64))
     M = psi.conj() @ h64.T
     assert np.abs(M - M.conj().T).max() <= 1e-11 * np.abs(M).max()
+
+
+def test_full_size_grad_mixed_vs_fp64(sc64):
+    from effmass_gb300.hamiltonian import GradHPsi
+    H, kp, psi = sc64
+    g64 = np.zeros((3,) + psi.shape, dtype=np.complex128)
+    H.gradient().at_k(0, precision="fp64")(psi, GradHPsi(g64[0], g64[1], g64[2]), n_bands=psi.shape[0])
+    for prec in ("fp32", "tc"):
+        g = np.zeros_like(g64)
+        H.gradient().at_k(0, precision=prec)(psi, GradHPsi(g[0], g[1], g[2]), n_bands=psi.shape[0])
+        assert rel_err(g, g64) <= TOL[prec], (prec, rel_err(g, g64))
 
 
 def test_full_size_linearity(sc64):
