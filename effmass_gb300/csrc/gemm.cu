@@ -216,6 +216,8 @@ template cudaError_t launch_proj_gemm<float2, float2, float2>(int, int, int, con
                                                               size_t, float2*, int, cudaStream_t);
 template cudaError_t launch_proj_gemm<float2, double2, float2>(int, int, int, const float2*, size_t, const double2*,
                                                                size_t, float2*, int, cudaStream_t);
+template cudaError_t launch_proj_gemm<double2, double2, float2>(int, int, int, const double2*, size_t, const double2*,
+                                                                size_t, float2*, int, cudaStream_t);
 template cudaError_t launch_reduce_splits<double2, double2>(int, int, int, const double2*, const double*, int,
                                                             double2*, size_t, cudaStream_t);
 template cudaError_t launch_reduce_splits<float2, float2>(int, int, int, const float2*, const double*, int, float2*,

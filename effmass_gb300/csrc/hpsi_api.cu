@@ -771,58 +771,6 @@ static int check_device_flag(hpsi_ctx* c)
     return HPSI_OK;
 }
 
-extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* hpsi_, int flags, void* stream)
-{
-    KSlot* s = nullptr;
-    int rc = check_call(c, kid, nb, &s, flags);
-    if (rc) return rc;
-    if (nb > 0 && (!psi_ || !hpsi_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/hpsi NULL");
-    if (nb == 0 || s->npw == 0) return HPSI_OK;
-    cudaStream_t st = (cudaStream_t)stream;
-    const int prec = flags & HPSI_PREC_MASK;
-    const bool dev = flags & HPSI_DEVICE_PTRS;
-    const bool fp64 = prec == HPSI_PREC_FP64;
-    const size_t nel = (size_t)nb * s->npw;
-    // workspace: [staging psi, hpsi] [max(local, nonlocal)]
-    Carver cv;
-    size_t o_psi = dev ? 0 : cv.take<double2>(nel);
-    size_t o_hpsi = dev ? 0 : cv.take<double2>(nel);
-    size_t o_work = cv.off;
-    const bool tc = prec == HPSI_PREC_TC || prec == HPSI_PREC_TC_BF16;
-    size_t wl = local_ws(c, *s, nb, fp64 ? sizeof(double2) : sizeof(float2));
-    size_t wn = fp64 ? nonlocal_ws<double2, double2>(*s, nb, 1)
-                     : (tc ? tc_ws(*s, nb) : nonlocal_ws<float2, float2>(*s, nb, 1));
-    if ((rc = ws_reserve(c, o_work + std::max(wl, wn)))) return rc;
-    const double2* psi = (const double2*)psi_;
-    double2* hpsi = (double2*)hpsi_;
-    if (!dev) {
-        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
-        hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
-        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
-    }
-    unsigned char* work = c->ws + o_work;
-    if (fp64) {
-        if ((rc = ensure_proj<double2>(c, *s, false, st))) return rc;
-        if ((rc = local_apply<double2, double>(c, *s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st))) return rc;
-        if ((rc = nonlocal_apply<double2, double2>(c, *s, nb, psi, hpsi, s->pr64, work, st))) return rc;
-    } else if (tc) {
-        if ((rc = ensure_tc(c, *s, prec == HPSI_PREC_TC ? 0 : 1, st))) return rc;
-        if ((rc = local_apply<float2, float>(c, *s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
-        if ((rc = tc_nonlocal(c, *s, nb, psi, hpsi, work, st))) return rc;
-    } else {
-        if ((rc = ensure_proj<float2>(c, *s, false, st))) return rc;
-        if ((rc = local_apply<float2, float>(c, *s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
-        if ((rc = nonlocal_apply<float2, float2>(c, *s, nb, psi, hpsi, s->pr32, work, st))) return rc;
-    }
-    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
-    if (!dev || (flags & HPSI_SYNC)) {
-        CUDA_TRY(c, cudaStreamSynchronize(st));
-        if (tc && (rc = check_device_flag(c))) return rc;
-    }
-    return HPSI_OK;
-}
-
 __global__ void grad_kinetic_kernel(int npw, int nb, const double* __restrict__ kvec, const double2* __restrict__ psi,
                                     double2* dx, double2* dy, double2* dz)
 {
@@ -903,6 +851,143 @@ static int grad_tc(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* d
     return tc_grad_nonlocal(c, s, nb, psi, d, work, st);
 }
 
+
+static bool is_tc(int prec) { return prec == HPSI_PREC_TC || prec == HPSI_PREC_TC_BF16; }
+
+// Build, once, what a precision needs on slot s (projector matrices, tensor-core
+// operands; with grad also the derivative operands).  Allocates.
+static int prepare_slot(hpsi_ctx* c, KSlot& s, int prec, bool grad, cudaStream_t st)
+{
+    int rc;
+    if (prec == HPSI_PREC_FP64) return ensure_proj<double2>(c, s, grad, st);
+    if (is_tc(prec)) {
+        if ((rc = ensure_tc(c, s, prec == HPSI_PREC_TC ? 0 : 1, st))) return rc;
+        if (grad && (rc = ensure_tc_grad(c, s, prec == HPSI_PREC_TC ? 0 : 1, st))) return rc;
+        return HPSI_OK;
+    }
+    return ensure_proj<float2>(c, s, grad, st);
+}
+
+// workspace of one H|psi> on device pointers
+static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec)
+{
+    const bool fp64 = prec == HPSI_PREC_FP64;
+    size_t wl = local_ws(c, s, nb, fp64 ? sizeof(double2) : sizeof(float2));
+    size_t wn = fp64 ? nonlocal_ws<double2, double2>(s, nb, 1)
+                     : (is_tc(prec) ? tc_ws(s, nb) : nonlocal_ws<float2, float2>(s, nb, 1));
+    return std::max(wl, wn);
+}
+
+// hpsi += H psi on device pointers with an explicit workspace (prepare_slot first)
+static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, int prec, unsigned char* work,
+                     cudaStream_t st)
+{
+    int rc;
+    if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
+    if (prec == HPSI_PREC_FP64) {
+        if ((rc = local_apply<double2, double>(c, s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st))) return rc;
+        return nonlocal_apply<double2, double2>(c, s, nb, psi, hpsi, s.pr64, work, st);
+    }
+    if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
+    if (is_tc(prec)) return tc_nonlocal(c, s, nb, psi, hpsi, work, st);
+    return nonlocal_apply<float2, float2>(c, s, nb, psi, hpsi, s.pr32, work, st);
+}
+
+static size_t grad_ws_bytes(const KSlot& s, int nb, int prec)
+{
+    if (prec == HPSI_PREC_FP64) return grad_ws<double2, double2>(s, nb);
+    return is_tc(prec) ? tc_grad_ws(s, nb) : grad_ws<float2, float2>(s, nb);
+}
+
+// d_a += dH/dk_a psi on device pointers (NULL d_a skipped)
+static int grad_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* d[3], int prec, unsigned char* work,
+                    cudaStream_t st)
+{
+    int rc;
+    if ((rc = prepare_slot(c, s, prec, true, st))) return rc;
+    if (is_tc(prec)) return grad_tc(c, s, nb, psi, d, work, prec == HPSI_PREC_TC ? 0 : 1, st);
+    return prec == HPSI_PREC_FP64 ? grad_device<double2, double2>(c, s, nb, psi, d, work, st)
+                                  : grad_device<float2, float2>(c, s, nb, psi, d, work, st);
+}
+
+// velocity workspace: G_a (3 nb npw complex128), psi^H G partials, then the gradient workspace
+static size_t vel_ws_bytes(const KSlot& s, int nb, int prec)
+{
+    const int nsv = split_for(nb, nb, s.npw);
+    Carver cv;
+    cv.take<double2>((size_t)3 * nb * s.npw);
+    cv.take<double2>((size_t)nsv * nb * nb);
+    return cv.off + grad_ws_bytes(s, nb, prec);
+}
+
+// m[a][i][j] = sum_G conj(psi_i) (dH_a psi_j), overwritten, device pointers
+static int velocity_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* m, int prec, unsigned char* ws,
+                        cudaStream_t st)
+{
+    const size_t nel = (size_t)nb * s.npw;
+    const int nsv = split_for(nb, nb, s.npw);
+    Carver cv;
+    const size_t o_g = cv.take<double2>(3 * nel);
+    const size_t o_vp = cv.take<double2>((size_t)nsv * nb * nb);
+    double2* g = reinterpret_cast<double2*>(ws + o_g);
+    CUDA_TRY(c, cudaMemsetAsync(g, 0, 3 * nel * sizeof(double2), st));
+    double2* d[3] = {g, g + nel, g + 2 * nel};
+    int rc = grad_dev(c, s, nb, psi, d, prec, ws + cv.off, st);
+    if (rc) return rc;
+    for (int a = 0; a < 3; ++a) {
+        int h = c->prof.open(PH_OTHER, st);
+        if (prec == HPSI_PREC_FP64) {
+            double2* vp = reinterpret_cast<double2*>(ws + o_vp);
+            CUDA_TRY(c, (launch_proj_gemm<double2, double2, double2>(nb, nb, s.npw, psi, (size_t)s.npw, d[a],
+                                                                     (size_t)s.npw, vp, nsv, st)));
+            CUDA_TRY(c, (launch_reduce_splits<double2, double2>(nb, nb, nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
+                                                                (size_t)nb, st)));
+        } else {
+            // FP32 products of the FP64 inputs, FP64 split-K reduction
+            float2* vp = reinterpret_cast<float2*>(ws + o_vp);
+            CUDA_TRY(c, (launch_proj_gemm<double2, double2, float2>(nb, nb, s.npw, psi, (size_t)s.npw, d[a],
+                                                                    (size_t)s.npw, vp, nsv, st)));
+            CUDA_TRY(c, (launch_reduce_splits<float2, double2>(nb, nb, nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
+                                                               (size_t)nb, st)));
+        }
+        c->prof.close(h, st);
+    }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* hpsi_, int flags, void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (nb > 0 && (!psi_ || !hpsi_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/hpsi NULL");
+    if (nb == 0 || s->npw == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t nel = (size_t)nb * s->npw;
+    Carver cv;
+    size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_hpsi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_work = cv.off;
+    if ((rc = ws_reserve(c, o_work + apply_ws_bytes(c, *s, nb, prec)))) return rc;
+    const double2* psi = (const double2*)psi_;
+    double2* hpsi = (double2*)hpsi_;
+    if (!dev) {
+        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
+        hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+    }
+    if ((rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st))) return rc;
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) {
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
+    }
+    return HPSI_OK;
+}
+
 extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* dx, double* dy, double* dz,
                                int flags, void* stream)
 {
@@ -913,8 +998,6 @@ extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_,
     if (nb == 0 || s->npw == 0 || (!dx && !dy && !dz)) return HPSI_OK;
     cudaStream_t st = (cudaStream_t)stream;
     const int prec = flags & HPSI_PREC_MASK;
-    const bool fp64 = prec == HPSI_PREC_FP64;
-    const bool tc = prec == HPSI_PREC_TC || prec == HPSI_PREC_TC_BF16;
     const bool dev = flags & HPSI_DEVICE_PTRS;
     const size_t nel = (size_t)nb * s->npw;
     double* outs[3] = {dx, dy, dz};
@@ -924,8 +1007,7 @@ extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_,
     for (int a = 0; a < 3; ++a)
         if (!dev && outs[a]) o_out[a] = cv.take<double2>(nel);
     size_t o_work = cv.off;
-    size_t wn = fp64 ? grad_ws<double2, double2>(*s, nb) : (tc ? tc_grad_ws(*s, nb) : grad_ws<float2, float2>(*s, nb));
-    if ((rc = ws_reserve(c, o_work + wn))) return rc;
+    if ((rc = ws_reserve(c, o_work + grad_ws_bytes(*s, nb, prec)))) return rc;
     const double2* psi = (const double2*)psi_;
     double2* d[3] = {(double2*)dx, (double2*)dy, (double2*)dz};
     if (!dev) {
@@ -937,18 +1019,13 @@ extern "C" int hpsi_grad_apply(hpsi_ctx* c, int kid, int nb, const double* psi_,
             CUDA_TRY(c, cudaMemcpyAsync(d[a], outs[a], nel * sizeof(double2), cudaMemcpyHostToDevice, st));
         }
     }
-    unsigned char* work = c->ws + o_work;
-    if (tc) rc = grad_tc(c, *s, nb, psi, d, work, prec == HPSI_PREC_TC ? 0 : 1, st);
-    else
-        rc = fp64 ? grad_device<double2, double2>(c, *s, nb, psi, d, work, st)
-                  : grad_device<float2, float2>(c, *s, nb, psi, d, work, st);
-    if (rc) return rc;
+    if ((rc = grad_dev(c, *s, nb, psi, d, prec, c->ws + o_work, st))) return rc;
     if (!dev)
         for (int a = 0; a < 3; ++a)
             if (outs[a]) CUDA_TRY(c, cudaMemcpyAsync(outs[a], d[a], nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
     if (!dev || (flags & HPSI_SYNC)) {
         CUDA_TRY(c, cudaStreamSynchronize(st));
-        if (tc && (rc = check_device_flag(c))) return rc;
+        if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
     }
     return HPSI_OK;
 }
@@ -962,19 +1039,20 @@ extern "C" int hpsi_velocity_matrix(hpsi_ctx* c, int kid, int nb, const double* 
     if (nb > 0 && (!psi_ || !m_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/m NULL");
     if (nb == 0) return HPSI_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    const bool fp64 = (flags & HPSI_PREC_MASK) == HPSI_PREC_FP64;
+    const int prec = flags & HPSI_PREC_MASK;
     const bool dev = flags & HPSI_DEVICE_PTRS;
     const size_t nel = (size_t)nb * s->npw;
     const size_t nm = (size_t)3 * nb * nb;
+    if (s->npw == 0) {
+        if (dev) CUDA_TRY(c, cudaMemsetAsync(m_, 0, nm * sizeof(double2), st));
+        else std::memset(m_, 0, nm * sizeof(double2));
+        return HPSI_OK;
+    }
     Carver cv;
     size_t o_psi = dev ? 0 : cv.take<double2>(nel);
     size_t o_m = dev ? 0 : cv.take<double2>(nm);
-    size_t o_g = cv.take<double2>(3 * nel);
-    const int nsv = split_for(nb, nb, s->npw);
-    size_t o_vp = cv.take<double2>((size_t)nsv * nb * nb);
     size_t o_work = cv.off;
-    size_t wn = fp64 ? grad_ws<double2, double2>(*s, nb) : grad_ws<float2, float2>(*s, nb);
-    if ((rc = ws_reserve(c, o_work + wn))) return rc;
+    if ((rc = ws_reserve(c, o_work + vel_ws_bytes(*s, nb, prec)))) return rc;
     const double2* psi = (const double2*)psi_;
     double2* m = (double2*)m_;
     if (!dev) {
@@ -982,25 +1060,12 @@ extern "C" int hpsi_velocity_matrix(hpsi_ctx* c, int kid, int nb, const double* 
         m = reinterpret_cast<double2*>(c->ws + o_m);
         CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
     }
-    double2* g = reinterpret_cast<double2*>(c->ws + o_g);
-    CUDA_TRY(c, cudaMemsetAsync(g, 0, 3 * nel * sizeof(double2), st));
-    double2* d[3] = {g, g + nel, g + 2 * nel};
-    unsigned char* work = c->ws + o_work;
-    rc = fp64 ? grad_device<double2, double2>(c, *s, nb, psi, d, work, st)
-              : grad_device<float2, float2>(c, *s, nb, psi, d, work, st);
-    if (rc) return rc;
-    double2* vp = reinterpret_cast<double2*>(c->ws + o_vp);
-    for (int a = 0; a < 3; ++a) {
-        // m[a][i][j] = sum_G conj(psi_i) (dH_a psi_j)
-        int h = c->prof.open(PH_OTHER, st);
-        CUDA_TRY(c, (launch_proj_gemm<double2, double2, double2>(nb, nb, s->npw, psi, (size_t)s->npw, d[a],
-                                                                 (size_t)s->npw, vp, nsv, st)));
-        CUDA_TRY(c, (launch_reduce_splits<double2, double2>(nb, nb, nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
-                                                            (size_t)nb, st)));
-        c->prof.close(h, st);
-    }
+    if ((rc = velocity_dev(c, *s, nb, psi, m, prec, c->ws + o_work, st))) return rc;
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(m_, m, nm * sizeof(double2), cudaMemcpyDeviceToHost, st));
-    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (!dev || (flags & HPSI_SYNC)) {
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
+    }
     return HPSI_OK;
 }
 
@@ -1145,5 +1210,367 @@ extern "C" int hpsi_apply_noalloc(hpsi_ctx* c, int kid, int nb, const double* ps
                                                            st);
     if (rc) return rc;
     if (flags & HPSI_SYNC) CUDA_TRY(c, cudaStreamSynchronize(st));
+    return HPSI_OK;
+}
+
+// ===========================================================================
+// Serving: a device-resident request loop with continuous batching.
+//
+// The systems (contexts) keep V_loc, the projector tables and the projector
+// matrices of their bound k-points resident in HBM.  Clients submit requests
+// (each a list of k-point jobs: psi in, hpsi accumulated, optional velocity
+// matrix) from any thread.  One scheduler thread admits requests in arrival
+// order whenever a lane (CUDA stream) is free and the request's buffers fit in
+// the device arena (the HBM budget), queues its copies and kernels on that
+// lane's stream, and retires it when the lane's completion event fires —
+// so requests that arrive while others run are admitted as soon as a slot and
+// memory free up, and the work of different requests overlaps on the device.
+// All CUDA calls are issued from the scheduler thread.
+// ===========================================================================
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+
+namespace {
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// first-fit allocator over [0, size) in 256-byte units
+struct Arena {
+    size_t size = 0;
+    std::map<size_t, size_t> free_;  // offset -> length
+    void init(size_t n) { size = n; free_.clear(); free_[0] = n; }
+    bool alloc(size_t n, size_t* off)
+    {
+        n = (n + 255) / 256 * 256;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *off = it->first;
+                size_t rest = it->second - n, o = it->first + n;
+                free_.erase(it);
+                if (rest) free_[o] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t n)
+    {
+        n = (n + 255) / 256 * 256;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+        }
+    }
+    size_t in_use() const
+    {
+        size_t f = 0;
+        for (auto& kv : free_) f += kv.second;
+        return size - f;
+    }
+};
+
+struct SrvReq {
+    long long ticket = 0;
+    std::vector<hpsi_job> jobs;
+    size_t bytes = 0, off = 0;
+    int lane = -1;
+    int status = HPSI_OK;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    bool done = false;
+    std::string err;
+};
+
+}  // namespace
+
+struct hpsi_server {
+    std::vector<hpsi_ctx*> sys;
+    int prec = HPSI_PREC_TC;
+    int dev = 0;
+    unsigned char* arena_mem = nullptr;
+    Arena arena;
+    std::vector<cudaStream_t> lanes;
+    std::vector<cudaEvent_t> lane_ev;
+    std::vector<SrvReq*> lane_req;
+    std::mutex mu;
+    std::condition_variable cv_done, cv_work;
+    std::deque<SrvReq*> queue;
+    std::map<long long, SrvReq*> reqs;
+    long long next_ticket = 1;
+    bool stop = false;
+    std::thread th;
+    size_t peak_in_use = 0;
+    long long completed = 0;
+    std::string err;
+};
+
+static int srv_fail(hpsi_server* s, int code, const std::string& m)
+{
+    if (s) s->err = m;
+    else g_last_error = m;
+    return code;
+}
+
+// device bytes a request holds while it runs
+static int srv_request_bytes(hpsi_server* S, const std::vector<hpsi_job>& jobs, size_t* bytes, std::string* why)
+{
+    size_t psi_max = 0, m_max = 0, ws_max = 0;
+    for (const hpsi_job& j : jobs) {
+        if (j.system < 0 || j.system >= (int)S->sys.size()) { *why = "job system index out of range"; return HPSI_ERR_BAD_ARG; }
+        hpsi_ctx* c = S->sys[j.system];
+        auto it = c->slots.find(j.kid);
+        if (it == c->slots.end() || !it->second.valid) { *why = "job k-point slot not bound"; return HPSI_ERR_STATE; }
+        if (j.nb < 0 || (j.nb > 0 && (!j.psi || !j.hpsi))) { *why = "job psi/hpsi NULL or nb < 0"; return HPSI_ERR_BAD_ARG; }
+        const KSlot& s = it->second;
+        const size_t nel = (size_t)j.nb * s.npw;
+        psi_max = std::max(psi_max, nel * sizeof(double2));
+        ws_max = std::max(ws_max, apply_ws_bytes(c, s, j.nb, S->prec));
+        if (j.vel) {
+            m_max = std::max(m_max, (size_t)3 * j.nb * j.nb * sizeof(double2));
+            ws_max = std::max(ws_max, vel_ws_bytes(s, j.nb, S->prec));
+        }
+    }
+    Carver cv;
+    cv.take<unsigned char>(psi_max);
+    cv.take<unsigned char>(psi_max);
+    cv.take<unsigned char>(m_max);
+    cv.take<unsigned char>(ws_max);
+    *bytes = cv.off;
+    return HPSI_OK;
+}
+
+// queue a request's work on its lane (scheduler thread)
+static int srv_issue(hpsi_server* S, SrvReq* r)
+{
+    cudaStream_t st = S->lanes[r->lane];
+    size_t psi_max = 0, m_max = 0;
+    for (const hpsi_job& j : r->jobs) {
+        const KSlot& s = S->sys[j.system]->slots[j.kid];
+        psi_max = std::max(psi_max, (size_t)j.nb * s.npw * sizeof(double2));
+        if (j.vel) m_max = std::max(m_max, (size_t)3 * j.nb * j.nb * sizeof(double2));
+    }
+    Carver cv;
+    unsigned char* base = S->arena_mem + r->off;
+    double2* psi = reinterpret_cast<double2*>(base + cv.take<unsigned char>(psi_max));
+    double2* hpsi = reinterpret_cast<double2*>(base + cv.take<unsigned char>(psi_max));
+    double2* m = reinterpret_cast<double2*>(base + cv.take<unsigned char>(m_max));
+    unsigned char* ws = base + cv.take<unsigned char>(0);
+    for (const hpsi_job& j : r->jobs) {
+        if (j.nb == 0) continue;
+        hpsi_ctx* c = S->sys[j.system];
+        KSlot& s = c->slots[j.kid];
+        const size_t nel = (size_t)j.nb * s.npw;
+        if (s.npw == 0) continue;
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(psi, j.psi, nel * sizeof(double2), cudaMemcpyHostToDevice, st)) ||
+            (e = cudaMemcpyAsync(hpsi, j.hpsi, nel * sizeof(double2), cudaMemcpyHostToDevice, st))) {
+            r->err = cudaGetErrorString(e);
+            return HPSI_ERR_CUDA;
+        }
+        int rc = apply_dev(c, s, j.nb, psi, hpsi, S->prec, ws, st);
+        if (!rc && j.vel) rc = velocity_dev(c, s, j.nb, psi, m, S->prec, ws, st);
+        if (rc) { r->err = c->err; return rc; }
+        if ((e = cudaMemcpyAsync(j.hpsi, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st))) {
+            r->err = cudaGetErrorString(e);
+            return HPSI_ERR_CUDA;
+        }
+        if (j.vel && (e = cudaMemcpyAsync(j.vel, m, (size_t)3 * j.nb * j.nb * sizeof(double2), cudaMemcpyDeviceToHost, st))) {
+            r->err = cudaGetErrorString(e);
+            return HPSI_ERR_CUDA;
+        }
+    }
+    return HPSI_OK;
+}
+
+static void srv_loop(hpsi_server* S)
+{
+    cudaSetDevice(S->dev);
+    std::unique_lock<std::mutex> lk(S->mu);
+    while (!S->stop) {
+        bool progress = false;
+        // admit in arrival order while a lane is free and memory fits
+        while (!S->queue.empty()) {
+            int lane = -1;
+            for (int i = 0; i < (int)S->lanes.size(); ++i)
+                if (!S->lane_req[i]) { lane = i; break; }
+            if (lane < 0) break;
+            SrvReq* r = S->queue.front();
+            size_t off = 0;
+            if (!S->arena.alloc(r->bytes, &off)) break;  // head waits for memory
+            S->queue.pop_front();
+            r->off = off;
+            r->lane = lane;
+            r->t_admit = now_ms();
+            S->lane_req[lane] = r;
+            S->peak_in_use = std::max(S->peak_in_use, S->arena.in_use());
+            lk.unlock();
+            r->status = srv_issue(S, r);
+            cudaEventRecord(S->lane_ev[lane], S->lanes[lane]);
+            lk.lock();
+            progress = true;
+        }
+        // retire finished lanes
+        for (int i = 0; i < (int)S->lanes.size(); ++i) {
+            SrvReq* r = S->lane_req[i];
+            if (!r) continue;
+            cudaError_t q = cudaEventQuery(S->lane_ev[i]);
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess && r->status == HPSI_OK) { r->status = HPSI_ERR_CUDA; r->err = cudaGetErrorString(q); }
+            r->t_done = now_ms();
+            r->done = true;
+            S->arena.release(r->off, r->bytes);
+            S->lane_req[i] = nullptr;
+            S->completed++;
+            progress = true;
+        }
+        if (progress) S->cv_done.notify_all();
+        else S->cv_work.wait_for(lk, std::chrono::microseconds(50));
+    }
+}
+
+extern "C" int hpsi_server_create(hpsi_ctx* const* systems, int n_systems, const hpsi_server_config* cfg,
+                                  hpsi_server** out)
+{
+    if (!out) return HPSI_ERR_BAD_ARG;
+    *out = nullptr;
+    if (!systems || n_systems <= 0 || !cfg) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: no systems / config");
+    const int prec = cfg->precision & HPSI_PREC_MASK;
+    if (prec < HPSI_PREC_FP64 || prec > HPSI_PREC_TC_BF16) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: precision");
+    if (cfg->lanes < 1 || cfg->lanes > 64) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: lanes must be 1..64");
+    if (!(cfg->device_budget_bytes > 0)) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: device budget");
+    hpsi_server* S = new hpsi_server();
+    S->prec = prec;
+    S->dev = systems[0]->dev;
+    for (int i = 0; i < n_systems; ++i) {
+        if (!systems[i] || systems[i]->dev != S->dev) {
+            delete S;
+            return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: systems must live on one device");
+        }
+        S->sys.push_back(systems[i]);
+    }
+    cudaSetDevice(S->dev);
+    // make every bound k-point resident in this precision (projector matrices and
+    // operands, with the gradient ones where the tables allow)
+    for (hpsi_ctx* c : S->sys)
+        for (auto& kv : c->slots) {
+            if (!kv.second.valid) continue;
+            int rc = prepare_slot(c, kv.second, prec, c->have_dbeta, 0);
+            if (rc) {
+                std::string m = "server: preparing k-point slot: " + c->err;
+                delete S;
+                return srv_fail(nullptr, rc, m);
+            }
+        }
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMalloc((void**)&S->arena_mem, cfg->device_budget_bytes) != cudaSuccess) {
+        delete S;
+        return srv_fail(nullptr, HPSI_ERR_OOM, "server: cannot allocate the device budget");
+    }
+    S->arena.init(cfg->device_budget_bytes);
+    for (int i = 0; i < cfg->lanes; ++i) {
+        cudaStream_t st;
+        cudaEvent_t ev;
+        cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        S->lanes.push_back(st);
+        S->lane_ev.push_back(ev);
+        S->lane_req.push_back(nullptr);
+    }
+    S->th = std::thread(srv_loop, S);
+    *out = S;
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_server_submit(hpsi_server* S, const hpsi_job* jobs, int n_jobs, long long* ticket)
+{
+    if (!S || !ticket || n_jobs < 0 || (n_jobs > 0 && !jobs)) return HPSI_ERR_BAD_ARG;
+    SrvReq* r = new SrvReq();
+    r->jobs.assign(jobs, jobs + n_jobs);
+    std::lock_guard<std::mutex> lk(S->mu);
+    std::string why;
+    int rc = srv_request_bytes(S, r->jobs, &r->bytes, &why);
+    if (rc) { delete r; return srv_fail(S, rc, "server submit: " + why); }
+    if (r->bytes > S->arena.size) {
+        delete r;
+        return srv_fail(S, HPSI_ERR_OOM, "server submit: request needs more than the whole device budget");
+    }
+    r->ticket = S->next_ticket++;
+    r->t_submit = now_ms();
+    S->queue.push_back(r);
+    S->reqs[r->ticket] = r;
+    *ticket = r->ticket;
+    S->cv_work.notify_one();
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_server_wait(hpsi_server* S, long long ticket, double timeout_s, hpsi_request_times* times)
+{
+    if (!S) return HPSI_ERR_BAD_ARG;
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return srv_fail(S, HPSI_ERR_BAD_ARG, "server wait: unknown ticket");
+    SrvReq* r = it->second;
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    while (!r->done) {
+        if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !r->done)
+            return srv_fail(S, HPSI_ERR_TIMEOUT, "server wait: timed out");
+    }
+    if (times) {
+        times->queue_ms = r->t_admit - r->t_submit;
+        times->run_ms = r->t_done - r->t_admit;
+        times->total_ms = r->t_done - r->t_submit;
+    }
+    int rc = r->status;
+    if (rc) S->err = "server request: " + r->err;
+    S->reqs.erase(it);
+    delete r;
+    return rc;
+}
+
+extern "C" int hpsi_server_stats(hpsi_server* S, hpsi_server_statistics* out)
+{
+    if (!S || !out) return HPSI_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(S->mu);
+    out->completed = S->completed;
+    out->queued = (long long)S->queue.size();
+    long long run = 0;
+    for (auto* r : S->lane_req) run += r ? 1 : 0;
+    out->running = run;
+    out->budget_bytes = (double)S->arena.size;
+    out->peak_bytes = (double)S->peak_in_use;
+    return HPSI_OK;
+}
+
+extern "C" const char* hpsi_server_last_error(const hpsi_server* S)
+{
+    if (!S) return g_last_error.c_str();
+    return S->err.c_str();
+}
+
+extern "C" int hpsi_server_destroy(hpsi_server* S)
+{
+    if (!S) return HPSI_ERR_BAD_ARG;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+        S->cv_work.notify_all();
+    }
+    if (S->th.joinable()) S->th.join();
+    cudaSetDevice(S->dev);
+    for (auto st : S->lanes) cudaStreamSynchronize(st);
+    for (auto st : S->lanes) cudaStreamDestroy(st);
+    for (auto ev : S->lane_ev) cudaEventDestroy(ev);
+    for (auto& kv : S->reqs) delete kv.second;
+    if (S->arena_mem) cudaFree(S->arena_mem);
+    delete S;
     return HPSI_OK;
 }

@@ -163,6 +163,44 @@ int hpsi_apply_noalloc(hpsi_ctx* ctx, int kid, int nb, const double* psi, double
 int hpsi_profile(hpsi_ctx* ctx, int enable);
 int hpsi_profile_read(hpsi_ctx* ctx, double* ms, long long* launches);
 
+/* ---- Serving: a device-resident request loop with continuous batching ------
+ * Systems (contexts with their bound k-points) stay resident in HBM; requests
+ * are lists of k-point jobs submitted from any host thread.  One scheduler
+ * thread admits requests in arrival order when a lane (CUDA stream) is free and
+ * the request's buffers fit in the device budget, runs them concurrently on the
+ * lanes and retires them as their lanes finish.  psi/hpsi/vel of a job are host
+ * memory (pinned memory gives asynchronous copies) and must stay valid until
+ * hpsi_server_wait returns; hpsi accumulates (+=) as in hpsi_apply, vel (if not
+ * NULL) receives the [3][nb][nb] velocity matrix.  While a server runs, its
+ * contexts must not be used directly.  No counterpart in the reference. */
+typedef struct hpsi_server hpsi_server;
+typedef struct hpsi_job {
+    int system;               /* index into the server's systems */
+    int kid;                  /* bound k-point slot of that system */
+    int nb;
+    const double* psi;        /* [nb][npw] complex */
+    double* hpsi;             /* [nb][npw] complex, accumulated */
+    double* vel;              /* [3][nb][nb] complex or NULL */
+} hpsi_job;
+typedef struct hpsi_server_config {
+    int lanes;                /* concurrent requests (CUDA streams), 1..64 */
+    double device_budget_bytes; /* arena for in-flight request buffers and workspaces */
+    int precision;            /* HPSI_PREC_* for every request */
+} hpsi_server_config;
+typedef struct hpsi_request_times {
+    double queue_ms, run_ms, total_ms;  /* submit->admit, admit->done, submit->done */
+} hpsi_request_times;
+typedef struct hpsi_server_statistics {
+    long long completed, queued, running;
+    double budget_bytes, peak_bytes;
+} hpsi_server_statistics;
+int hpsi_server_create(hpsi_ctx* const* systems, int n_systems, const hpsi_server_config* cfg, hpsi_server** out);
+int hpsi_server_submit(hpsi_server* srv, const hpsi_job* jobs, int n_jobs, long long* ticket);
+int hpsi_server_wait(hpsi_server* srv, long long ticket, double timeout_s, hpsi_request_times* times);
+int hpsi_server_stats(hpsi_server* srv, hpsi_server_statistics* out);
+int hpsi_server_destroy(hpsi_server* srv);
+const char* hpsi_server_last_error(const hpsi_server* srv);
+
 /* Message of the last failed call on ctx (never NULL); with ctx == NULL the
  * message of the calling thread's last failed hpsi_ctx_create. */
 const char* hpsi_last_error(const hpsi_ctx* ctx);
