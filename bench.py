@@ -40,6 +40,10 @@ def parse():
     ap.add_argument("--nb", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--serving-requests", type=int, default=600,
+                    help="requests of the served Poisson stream (0 skips serving)")
+    ap.add_argument("--serving-rate", type=float, default=200.0)
+    ap.add_argument("--serving-lanes", type=int, default=4)
     return ap.parse_args()
 
 
@@ -271,6 +275,10 @@ def run_gb300(args, rank, world, local):
                      "note": "algorithmic flops 8*P*npw*nb; the split operands issue 3x that on the tensor pipe"}
     phases = {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps} for k, v in prof.items() if v[1]}
 
+    serving = None
+    if args.serving_requests > 0:
+        serving = run_serving(args, H, kp)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import cpu_baseline
@@ -295,13 +303,110 @@ def run_gb300(args, rank, world, local):
         "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "grad_value": grad_value, "grad_unit": "band-apps/s of dH/dk_{x,y,z}|psi> (all three directions)",
         "e2e": e2e, "roofline": roof, "roofline_gemm": roof_gemm, "phases": phases, "gpu_launches": gpu_launches,
-        "cpu_baseline": cpu, "clocks": clk,
+        "cpu_baseline": cpu, "clocks": clk, "serving": serving,
     }
     if rank == 0:
         print(json.dumps(out))
     H.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_serving(args, H_sc64, kp_sc64):
+    """Served stream: Poisson arrivals of requests mixing the 2-, 8- and 64-atom
+    cells (6:3:1), each 1-16 k-points x 8-128 bands of H|psi> plus the velocity
+    matrix, through the library's serving loop.  Returns the summary dict."""
+    import threading
+    import numpy as np
+    import torch
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import Hamiltonian
+    from effmass_gb300.serving import Job, Server, pinned_empty
+
+    rng = np.random.default_rng(2024)
+    pools = []
+    # the 64-atom cell (already resident: Gamma), the 8-atom cell on a 4^3 MP
+    # grid (16 of its k-points bound) and the 2-atom cell on 6^3 (16 bound)
+    made = []
+    for name, grid, nk in (("fcc2", 6, 16), ("sc8", 4, 16)):
+        sysm = S.make_system(name)
+        H = Hamiltonian(sysm)
+        kpts = S.mp_grid(grid)[:nk]
+        kps = []
+        for i, k in enumerate(kpts):
+            kp = S.g_sphere(sysm.lattice, k, sysm.ecut)
+            H.set_kpoint(i, kp)
+            kps.append(kp)
+        made.append(H)
+        pools.append((H, kps))
+    pools.append((H_sc64, [kp_sc64]))
+    hams = [p[0] for p in pools]
+    # pinned inputs (128 bands per bound k-point) and shared output buffers
+    bufs = []
+    for H, kps in pools:
+        ins, outs, vels = [], [], []
+        for kp in kps:
+            a = pinned_empty((128, kp.npw))
+            a[...] = S.make_bands(kp, 128, seed=int(rng.integers(1 << 30)))
+            ins.append(a)
+            outs.append(pinned_empty((128, kp.npw)))
+            vels.append(pinned_empty((3 * 128 * 128,)))
+        bufs.append((ins, outs, vels))
+    n = args.serving_requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serving_rate, size=n))
+    kinds = rng.choice(3, size=n, p=[0.6, 0.3, 0.1])
+    plans = []
+    for i in range(n):
+        si = int(kinds[i])
+        nkr = int(rng.integers(1, 17))
+        ks = rng.integers(0, len(pools[si][1]), size=nkr)
+        nb = int(rng.integers(8, 129))
+        plans.append((si, [int(k) for k in ks], nb))
+    band_apps = sum(len(p[1]) * p[2] for p in plans)
+    with Server(hams, lanes=args.serving_lanes, budget_gb=48, precision=args.prec) as srv:
+        # warm-up: one request per system
+        for si in range(3):
+            ins, outs, vels = bufs[si]
+            srv.wait(srv.submit([Job(si, 0, ins[0][:8], outs[0][:8], vels[0][: 3 * 64].reshape(3, 8, 8))]))
+        tickets = [None] * n
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, (si, ks, nb) in enumerate(plans):
+                delay = t0 + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ins, outs, vels = bufs[si]
+                jobs = [Job(si, k, ins[k][:nb], outs[k][:nb], vels[k][: 3 * nb * nb].reshape(3, nb, nb)) for k in ks]
+                tickets[i] = srv.submit(jobs)
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        times = []
+        for i in range(n):
+            while tickets[i] is None:
+                time.sleep(0.0005)
+            times.append(srv.wait(tickets[i]))
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    for H in made:
+        H.close()
+    tot = np.array([t["total_ms"] for t in times])
+    que = np.array([t["queue_ms"] for t in times])
+    by_kind = {}
+    for name, kd in (("fcc2", 0), ("sc8", 1), ("sc64", 2)):
+        sel = tot[kinds == kd]
+        if sel.size:
+            by_kind[name] = {"requests": int(sel.size), "p50_ms": float(np.percentile(sel, 50)),
+                             "p99_ms": float(np.percentile(sel, 99))}
+    return {"requests": n, "rate_req_per_s": args.serving_rate, "lanes": args.serving_lanes,
+            "precision": args.prec, "band_apps": int(band_apps), "wall_s": wall,
+            "throughput_band_apps_per_s": band_apps / wall, "throughput_req_per_s": n / wall,
+            "p50_ms": float(np.percentile(tot, 50)), "p99_ms": float(np.percentile(tot, 99)),
+            "max_ms": float(tot.max()), "mean_queue_ms": float(que.mean()), "by_cell": by_kind,
+            "peak_device_bytes": st["peak_bytes"],
+            "mix": "2-, 8-, 64-atom cells 6:3:1; 1-16 k-points (16/16/1 bound) x 8-128 bands; H|psi> + velocity"}
 
 
 def run_reference(args, rank, world, local):

@@ -56,13 +56,17 @@ def _bind(L):
     L._srv_bound = True
 
 
+class _PinnedArray(np.ndarray):
+    """ndarray view of page-locked memory that keeps its owning tensor alive."""
+
+
 def pinned_empty(shape, dtype=np.complex128):
     """A page-locked host array (through torch) for asynchronous copies."""
     import torch
     tdt = {np.complex128: torch.complex128, np.float64: torch.float64}[np.dtype(dtype).type]
     t = torch.empty(tuple(shape), dtype=tdt).pin_memory()
-    arr = t.numpy()
-    arr._pin_owner = t  # noqa: keep the tensor alive with the view  # type: ignore[attr-defined]
+    arr = t.numpy().view(_PinnedArray)
+    arr._owner = t
     return arr
 
 
