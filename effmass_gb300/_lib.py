@@ -17,7 +17,9 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhpsi_gb3
 EXPORTS = ["hpsi_abi_version", "hpsi_ctx_create", "hpsi_ctx_destroy", "hpsi_set_kpoint", "hpsi_dim",
            "hpsi_apply", "hpsi_grad_apply", "hpsi_velocity_matrix", "hpsi_profile", "hpsi_profile_read",
            "hpsi_apply_noalloc", "hpsi_server_create", "hpsi_server_submit", "hpsi_server_wait",
-           "hpsi_server_stats", "hpsi_server_destroy", "hpsi_server_last_error", "hpsi_last_error"]
+           "hpsi_server_stats", "hpsi_server_destroy", "hpsi_server_last_error", "hpsi_batch_create",
+           "hpsi_batch_buffers", "hpsi_batch_offset", "hpsi_batch_run", "hpsi_batch_apply", "hpsi_batch_info",
+           "hpsi_batch_destroy", "hpsi_batch_last_error", "hpsi_last_error"]
 
 _lib = None
 
@@ -54,7 +56,7 @@ def load():
     L.hpsi_last_error.argtypes = [ctxp]
     L.hpsi_last_error.restype = C.c_char_p
     for name in EXPORTS:
-        if name not in ("hpsi_last_error", "hpsi_server_last_error"):
+        if not name.endswith("last_error"):
             getattr(L, name).restype = C.c_int
     if L.hpsi_abi_version() != 1:
         raise RuntimeError("libhpsi_gb300.so ABI version mismatch")

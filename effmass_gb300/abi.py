@@ -26,6 +26,8 @@ HPSI_PREC_TC = 2
 HPSI_PREC_TC_BF16 = 3
 HPSI_DEVICE_PTRS = 0x10
 HPSI_SYNC = 0x20
+HPSI_BATCH_NO_GRAPH = 0x100
+HPSI_BATCH_NO_TUNE = 0x200
 HPSI_NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
 PRECISIONS = {"fp64": HPSI_PREC_FP64, "fp32": HPSI_PREC_FP32, "tc": HPSI_PREC_TC, "tc_bf16": HPSI_PREC_TC_BF16}
@@ -131,3 +133,7 @@ def package_dir() -> str:
 
 def repo_root() -> str:
     return os.path.dirname(package_dir())
+
+
+class HpsiBatchItem(C.Structure):
+    _fields_ = [("ctx", C.c_void_p), ("kid", C.c_int), ("nb", C.c_int)]

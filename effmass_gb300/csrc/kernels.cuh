@@ -50,6 +50,21 @@ struct Prof {
 };
 
 // ---- local potential (local.cu) -------------------------------------------
+// One k-point (with its block of bands) of a batched local-term launch; all
+// pointers on the device.
+struct LocalItem {
+    const int* plane_x;     // [nxs]
+    const int* plane_off;   // [nxs+1]
+    const int* ent_ig;      // [npw]
+    const int* ent_jk;      // [npw]
+    const double* kinetic;  // [npw]
+    const double2* psi;     // [nb][npw]
+    double2* hpsi;          // [nb][npw], accumulated
+    size_t t_off;           // first element of the item's T block [nb][nxs][n2][n3]
+    int npw, nxs, nb;
+    int band0;              // first band of the item in the batch's band numbering
+};
+
 struct LocalArgs {
     int n1, n2, n3;
     int npw;
@@ -66,6 +81,12 @@ struct LocalArgs {
     FastDiv nl_y;           // y-lines of a plane: n3
     FastDiv nl_x;           // x-lines of an x-pass block: kt*bb
     FastDiv kt_f;           // divisor by kt
+    // batched launches (items == null for one k-point): the plane kernels run
+    // blockIdx.y over all bands of the batch, the x pass blockIdx.z over xblk
+    const LocalItem* items;
+    const int* band_item;   // [bands] item of each batch band
+    const int2* xblk;       // [x-pass band blocks] (item, first band within the item)
+    int plane_threads;      // block size of the plane kernels (0: default)
 };
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64);
@@ -75,6 +96,13 @@ void local_xpass_shape(LocalArgs* a, size_t csize);
 template <typename C, typename V>
 cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
                          const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof);
+// x-pass line buffer bytes of a given (kt, bb) shape
+size_t local_xpass_smem(const LocalArgs& a, bool fp64);
+// Batched local term over the items of a.items: nbands = all bands of the
+// batch, max_nxs = largest nxs, nxblk = x-pass band blocks (a.kt, a.bb set).
+template <typename C, typename V>
+cudaError_t launch_local_batch(const LocalArgs& a, int nbands, int max_nxs, int nxblk, C* T, const V* vloc,
+                               const C* twx, const C* twy, const C* twz, cudaStream_t st);
 
 // ---- projector build (projectors.cu) --------------------------------------
 // Per G: spherical coordinates, trig, Y_lm and its angular gradients.
@@ -144,3 +172,23 @@ cudaError_t launch_expand_gemm(int M, int N, int K, const C* W, size_t ldw, cons
 // out[i] = from_c128(in[i])
 template <typename C>
 cudaError_t launch_convert(size_t n, const double2* in, C* out, cudaStream_t st);
+
+// ---- ragged batched SIMT GEMMs (bgemm.cu) ----------------------------------
+// One k-point of a batched nonlocal launch; all pointers on the device.
+struct BGemmItem {
+    const void* pr;        // [P][npw] projector matrix (complex C of the launch)
+    const double2* psi;    // [nb][npw]
+    double2* hpsi;         // [nb][npw], accumulated
+    const double* lam;     // [P]
+    size_t part_off;       // first element of the item's partials [nsplit][P][nb]
+    int nb, npw;
+};
+
+int bgemm_tile_count();
+void bgemm_tile_shape(int tile, int* tm, int* tn);
+template <typename C, typename Acc>
+cudaError_t launch_bproj(int P, const BGemmItem* items, int n_items, int nb_max, int nsplit, int tile, Acc* part,
+                         cudaStream_t st);
+template <typename C, typename Acc>
+cudaError_t launch_bexp(int P, const BGemmItem* items, int n_items, int nb_max, int npw_max, int nsplit, int tile,
+                        const Acc* part, cudaStream_t st);

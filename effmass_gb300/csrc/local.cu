@@ -54,17 +54,28 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) g2r_
     C* twy = b1 + n23p;
     C* twz = twy + n2;
     const int p = blockIdx.x;
-    const int b = blockIdx.y;
+    int b = blockIdx.y;
+    int npw = a.npw, nxs = a.nxs;
+    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk;
+    if (a.items) {  // batched: the band's item (uniform per block, before any barrier)
+        const LocalItem I = a.items[a.band_item[b]];
+        if (p >= I.nxs) return;
+        b -= I.band0;
+        npw = I.npw; nxs = I.nxs;
+        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk;
+        psi = I.psi;
+        T += I.t_off;
+    }
     for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
     for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
     for (int t = threadIdx.x; t < n23p; t += blockDim.x) b0[t] = cmake<C>(0, 0);
     __syncthreads();
-    const double2* ps = psi + (size_t)b * a.npw;
-    const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
+    const double2* ps = psi + (size_t)b * npw;
+    const int e0 = plane_off[p], e1 = plane_off[p + 1];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        int ig = a.ent_ig[e];
+        int ig = ent_ig[e];
         if (ig >= 0) {
-            int jk = a.ent_jk[e];
+            int jk = ent_jk[e];
             int j = jk / n3, k = jk - j * n3;
             b0[j * n3p + k] = from_c128<C>(ps[ig]);
         }
@@ -78,7 +89,7 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) g2r_
     __syncthreads();
     // y (columns), last stage straight to T
     C* zother = (zo == b0) ? b1 : b0;
-    fft_lines_io<C, true, WIDE>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{T + ((size_t)b * a.nxs + p) * n23, n3},
+    fft_lines_io<C, true, WIDE>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{T + ((size_t)b * nxs + p) * n23, n3},
                                 zother, zo, a.Ly, a.nl_y, 1, n3p, twy, +1);
 }
 
@@ -147,7 +158,18 @@ __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb
     const int j = blockIdx.y;
     const int k0 = blockIdx.x * KT;
     const int kt = min(KT, n3 - k0);
-    const int bb0 = blockIdx.z * BB;
+    int bb0 = blockIdx.z * BB;
+    int nxs = a.nxs;
+    const int* plane_x = a.plane_x;
+    if (a.items) {  // batched: (item, first band) of this band block
+        const int2 xb = a.xblk[blockIdx.z];
+        const LocalItem I = a.items[xb.x];
+        bb0 = xb.y;
+        nb = I.nb;
+        nxs = I.nxs;
+        plane_x = I.plane_x;
+        T += I.t_off;
+    }
     const int nbb = min(BB, nb - bb0);
     const size_t plane = (size_t)n2 * n3;
     for (int t = threadIdx.x; t < n1; t += blockDim.x) { twx[t] = tw_x_g[t]; xpl[t] = -1; }
@@ -156,10 +178,10 @@ __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb
         vt[t] = kk < kt ? vloc[((size_t)x * n2 + j) * n3 + k0 + kk] : (V)0;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < a.nxs; t += blockDim.x) xpl[a.plane_x[t]] = t;
+    for (int t = threadIdx.x; t < nxs; t += blockDim.x) xpl[plane_x[t]] = t;
     __syncthreads();
     const size_t base = (size_t)j * n3 + k0;
-    const XLoad<C> ld{T, xpl, plane, base, a.nxs, KT, kt, nbb, bb0, a.kt_f};
+    const XLoad<C> ld{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
     // G->r, times V, into the buffer the last stage does not read
     const int r = fft_last_read(a.Lx);
     C* vo = (r == 1) ? b1 : b0;
@@ -167,7 +189,7 @@ __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb
     __syncthreads();
     // r->G, back into the sphere planes of T
     C* vother = (vo == b0) ? b1 : b0;
-    const XStore<C> stT{T, xpl, plane, base, a.nxs, KT, kt, nbb, bb0, a.kt_f};
+    const XStore<C> stT{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
     fft_lines_io<C, true, WIDE>(SmemLines<C>{vo, 1, NL}, stT, vother, vo, a.Lx, a.nl_x, 1, NL, twx, -1);
 }
 
@@ -183,14 +205,25 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) r2g_
     C* twy = b1 + n23p;
     C* twz = twy + n2;
     const int p = blockIdx.x;
-    const int b = blockIdx.y;
+    int b = blockIdx.y;
+    int npw = a.npw, nxs = a.nxs;
+    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk;
+    if (a.items) {  // batched: the band's item (uniform per block, before any barrier)
+        const LocalItem I = a.items[a.band_item[b]];
+        if (p >= I.nxs) return;
+        b -= I.band0;
+        npw = I.npw; nxs = I.nxs;
+        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk;
+        psi = I.psi; hpsi = I.hpsi; kinetic = I.kinetic;
+        T += I.t_off;
+    }
     for (int t = threadIdx.x; t < n2; t += blockDim.x) twy[t] = tw_y_g[t];
     for (int t = threadIdx.x; t < n3; t += blockDim.x) twz[t] = tw_z_g[t];
     __syncthreads();
     // y (columns) straight from T; output into the buffer the last stage does not read
     const int ry = fft_last_read(a.Ly);
     C* yo = (ry == 1) ? b1 : b0;
-    fft_lines_io<C, true, WIDE>(PlaneGlobal<C>{const_cast<C*>(T) + ((size_t)b * a.nxs + p) * n23, n3},
+    fft_lines_io<C, true, WIDE>(PlaneGlobal<C>{const_cast<C*>(T) + ((size_t)b * nxs + p) * n23, n3},
                                 SmemLines<C>{yo, 1, n3p}, b0, b1, a.Ly, a.nl_y, 1, n3p, twy, -1);
     __syncthreads();
     // z (rows)
@@ -202,12 +235,12 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) r2g_
                                 twz, -1);
     __syncthreads();
     const C* res = zo;
-    const double2* ps = psi + (size_t)b * a.npw;
-    double2* hp = hpsi + (size_t)b * a.npw;
-    const int e0 = a.plane_off[p], e1 = a.plane_off[p + 1];
+    const double2* ps = psi + (size_t)b * npw;
+    double2* hp = hpsi + (size_t)b * npw;
+    const int e0 = plane_off[p], e1 = plane_off[p + 1];
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        int ig = a.ent_ig[e] & 0x7fffffff;
-        int jk = a.ent_jk[e];
+        int ig = ent_ig[e] & 0x7fffffff;
+        int jk = ent_jk[e];
         int j = jk / n3, k = jk - j * n3;
         double2 g = as_c128(res[j * n3p + k]);
         double2 s = ps[ig];
@@ -272,17 +305,54 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
         return e;
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
     dim3 gp(a.nxs, nb);
+    const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     int h = prof->open(PH_G2R, st);
-    g2r_planes<C, WIDE><<<gp, Cfg<C>::plane_threads, sp, st>>>(a, psi, T, twy, twz);
+    g2r_planes<C, WIDE><<<gp, pt, sp, st>>>(a, psi, T, twy, twz);
     prof->close(h, st);
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
     x_pass<C, V, WIDE><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
     prof->close(h, st);
     h = prof->open(PH_R2G, st);
-    r2g_planes<C, WIDE><<<gp, Cfg<C>::plane_threads, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
+    r2g_planes<C, WIDE><<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
     prof->close(h, st);
     return cudaGetLastError();
+}
+
+template <typename C, typename V, bool WIDE>
+static cudaError_t launch_local_batch_t(const LocalArgs& a, int nbands, int max_nxs, int nxblk, C* T, const V* vloc,
+                                        const C* twx, const C* twy, const C* twz, cudaStream_t st)
+{
+    const size_t sp = plane_smem<C>(a), sx = xpass_smem<C, V>(a);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(g2r_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(r2g_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
+        return e;
+    if (max_nxs == 0 || nbands == 0 || nxblk == 0) return cudaSuccess;
+    const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
+    dim3 gp(max_nxs, nbands);
+    g2r_planes<C, WIDE><<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
+    dim3 gx(ceil_div(a.n3, a.kt), a.n2, nxblk);
+    x_pass<C, V, WIDE><<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
+    r2g_planes<C, WIDE><<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
+    return cudaGetLastError();
+}
+
+template <typename C, typename V>
+cudaError_t launch_local_batch(const LocalArgs& a, int nbands, int max_nxs, int nxblk, C* T, const V* vloc,
+                               const C* twx, const C* twy, const C* twz, cudaStream_t st)
+{
+    if (!a.items) return cudaErrorInvalidValue;
+    if (a.plane_threads > Cfg<C>::plane_threads || a.plane_threads % 32) return cudaErrorInvalidValue;
+    const bool wide = fft_needs_wide(a.Lx) || fft_needs_wide(a.Ly) || fft_needs_wide(a.Lz);
+    if (wide) return launch_local_batch_t<C, V, true>(a, nbands, max_nxs, nxblk, T, vloc, twx, twy, twz, st);
+    return launch_local_batch_t<C, V, false>(a, nbands, max_nxs, nxblk, T, vloc, twx, twy, twz, st);
+}
+
+size_t local_xpass_smem(const LocalArgs& a, bool fp64)
+{
+    return fp64 ? xpass_smem<double2, double>(a) : xpass_smem<float2, float>(a);
 }
 
 template <typename C, typename V>
@@ -300,3 +370,7 @@ template cudaError_t launch_local<double2, double>(const LocalArgs&, int, const 
 template cudaError_t launch_local<float2, float>(const LocalArgs&, int, const double2*, double2*, const double*,
                                                  float2*, const float*, const float2*, const float2*, const float2*,
                                                  cudaStream_t, Prof*);
+template cudaError_t launch_local_batch<double2, double>(const LocalArgs&, int, int, int, double2*, const double*,
+                                                         const double2*, const double2*, const double2*, cudaStream_t);
+template cudaError_t launch_local_batch<float2, float>(const LocalArgs&, int, int, int, float2*, const float*,
+                                                       const float2*, const float2*, const float2*, cudaStream_t);

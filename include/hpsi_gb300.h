@@ -201,6 +201,46 @@ int hpsi_server_stats(hpsi_server* srv, hpsi_server_statistics* out);
 int hpsi_server_destroy(hpsi_server* srv);
 const char* hpsi_server_last_error(const hpsi_server* srv);
 
+/* ---- Batched k-points: many (context, k-point, bands) items in one plan ----
+ * A plan fixes a list of items (different k-points with ragged npw and band
+ * counts, possibly of several contexts/cells) and keeps their psi and hpsi
+ * resident on the device, packed item after item, each [nb][npw] band-major.
+ * Per cell, each phase is one launch over all of the cell's items (scatter +
+ * z/y FFT planes, x FFT/V/x FFT, y/z FFT planes + gather + kinetic, the ragged
+ * projection GEMM, the expansion GEMM with the fused split-K reduction); the
+ * cells run as parallel branches, the projections beside the FFTs, and the
+ * whole sequence is captured in one CUDA graph.  At creation a tuner times the
+ * candidate FFT block shapes, GEMM tiles and split-K counts on the plan's own
+ * buffers and keeps the fastest (results are cached per shape for the
+ * process).  Precisions: HPSI_PREC_FP64 or HPSI_PREC_FP32.  The items' slots
+ * must stay bound: rebinding one makes later runs fail with HPSI_ERR_STATE;
+ * destroy plans before their contexts.  The reference has no batched call: it
+ * applies Callable::operator() per k-point and band
+ * (src/H_psi/hamiltonian_callable.cpp:94-356). */
+#define HPSI_BATCH_NO_GRAPH 0x100  /* run the launches eagerly instead of a graph */
+#define HPSI_BATCH_NO_TUNE  0x200  /* built-in tile choices, no timing at creation */
+typedef struct hpsi_batch hpsi_batch;
+typedef struct hpsi_batch_item {
+    hpsi_ctx* ctx;
+    int kid;                  /* bound k-point slot of ctx */
+    int nb;                   /* bands (0 allowed) */
+} hpsi_batch_item;
+int hpsi_batch_create(const hpsi_batch_item* items, int n_items, int flags, hpsi_batch** out);
+/* Device buffers of the plan: psi and hpsi, n_complex complex<double> each. */
+int hpsi_batch_buffers(hpsi_batch* b, double** psi, double** hpsi, size_t* n_complex);
+/* Offset (in complex values) of item i in the packed buffers. */
+int hpsi_batch_offset(const hpsi_batch* b, int item, size_t* offset);
+/* hpsi_buffer += H psi_buffer for every item, queued on stream. */
+int hpsi_batch_run(hpsi_batch* b, void* stream);
+/* Copies psi and hpsi (packed, host or device per HPSI_DEVICE_PTRS) into the
+ * plan's buffers, runs, and copies hpsi back (hpsi += H psi, as hpsi_apply). */
+int hpsi_batch_apply(hpsi_batch* b, const double* psi, double* hpsi, int flags, void* stream);
+/* The tuned choices as a JSON text; returns the length it needs (buf may be
+ * NULL). */
+int hpsi_batch_info(const hpsi_batch* b, char* buf, size_t len);
+int hpsi_batch_destroy(hpsi_batch* b);
+const char* hpsi_batch_last_error(const hpsi_batch* b);
+
 /* Message of the last failed call on ctx (never NULL); with ctx == NULL the
  * message of the calling thread's last failed hpsi_ctx_create. */
 const char* hpsi_last_error(const hpsi_ctx* ctx);

@@ -54,6 +54,9 @@ def test_struct_layout_matches_c():
       printf("%zu %zu %zu %zu\n", sizeof(hpsi_species), offsetof(hpsi_species,dq), offsetof(hpsi_species,beta_q), offsetof(hpsi_species,dbeta_q));
       printf("%zu %zu %zu %zu %zu\n", sizeof(hpsi_system), offsetof(hpsi_system,lattice), offsetof(hpsi_system,omega), offsetof(hpsi_system,species), offsetof(hpsi_system,atom_tau));
       printf("%zu %zu %zu %zu\n", sizeof(hpsi_kpoint), offsetof(hpsi_kpoint,k_frac), offsetof(hpsi_kpoint,g_idx), offsetof(hpsi_kpoint,kinetic));
+      printf("%zu %zu %zu\n", sizeof(hpsi_batch_item), offsetof(hpsi_batch_item,kid), offsetof(hpsi_batch_item,nb));
+      printf("%zu %zu %zu\n", sizeof(hpsi_job), offsetof(hpsi_job,psi), offsetof(hpsi_job,vel));
+      printf("%zu %zu %zu\n", sizeof(hpsi_server_config), offsetof(hpsi_server_config,device_budget_bytes), offsetof(hpsi_server_config,precision));
       return 0; }
     """
     with tempfile.TemporaryDirectory() as td:
@@ -66,6 +69,43 @@ def test_struct_layout_matches_c():
     assert got[0] == [C.sizeof(S), S.dq.offset, S.beta_q.offset, S.dbeta_q.offset]
     assert got[1] == [C.sizeof(Y), Y.lattice.offset, Y.omega.offset, Y.species.offset, Y.atom_tau.offset]
     assert got[2] == [C.sizeof(K), K.k_frac.offset, K.g_idx.offset, K.kinetic.offset]
+    from effmass_gb300.serving import HpsiJob, HpsiServerConfig
+    B = abi.HpsiBatchItem
+    assert got[3] == [C.sizeof(B), B.kid.offset, B.nb.offset]
+    assert got[4] == [C.sizeof(HpsiJob), HpsiJob.psi.offset, HpsiJob.vel.offset]
+    assert got[5] == [C.sizeof(HpsiServerConfig), HpsiServerConfig.device_budget_bytes.offset,
+                      HpsiServerConfig.precision.offset]
+
+
+def test_cpp_wrapper_header_compiles():
+    """include/hpsi_gb300.hpp (the Callable-style C++ mirror) is valid C++20 against the C header."""
+    src = r"""
+    #include "hpsi_gb300.hpp"
+    #include <complex>
+    #include <span>
+    void use(hpsi::Hamiltonian& H, std::span<const std::complex<double>> psi, std::span<std::complex<double>> out) {
+        auto op = H.at_k(0);
+        op(psi, out);
+        (void)op.dim();
+    }
+    int main() { return 0; }
+    """
+    with tempfile.TemporaryDirectory() as td:
+        cfile = os.path.join(td, "w.cpp")
+        open(cfile, "w").write(src)
+        r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-I", os.path.dirname(HEADER), cfile],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_batch_rejects_bad_arguments_before_device_use(lib):
+    h = C.c_void_p()
+    lib.hpsi_batch_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+    assert lib.hpsi_batch_create(None, 0, 0, C.byref(h)) == abi.HPSI_ERR_BAD_ARG
+    assert not h.value
+    items = (abi.HpsiBatchItem * 1)(abi.HpsiBatchItem(None, 0, 4))
+    assert lib.hpsi_batch_create(C.cast(items, C.c_void_p), 1, abi.HPSI_PREC_TC, C.byref(h)) == abi.HPSI_ERR_BAD_ARG
+    assert lib.hpsi_batch_create(C.cast(items, C.c_void_p), 1, 0, C.byref(h)) == abi.HPSI_ERR_BAD_ARG
 
 
 def _has_gpu():
