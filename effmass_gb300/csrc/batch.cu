@@ -7,8 +7,8 @@
 // items of one cell (one hpsi_ctx) share every launch:
 //   side stream : ragged projection GEMM over all items (split-K partials)
 //   main stream : g2r planes -> x pass -> r2g planes over all items' bands,
-//                 then (after the projection) the ragged expansion GEMM with
-//                 the split-K reduction and lambda fused into its W-tile load.
+//                 then (after the projection) the split-K reduction with
+//                 lambda and the ragged expansion GEMM.
 // Cells are independent branches.  The sequence is captured once into a CUDA
 // graph, so a run is one graph launch whatever the number of k-points.
 //
@@ -53,6 +53,7 @@ struct Group {
     BGemmItem* d_gitems = nullptr;
     void* T = nullptr;
     void* part = nullptr;
+    void* W = nullptr;       // reduced projections [P][nbands] (complex of the precision)
     int max_split = 1;
     LocalArgs la{};
     Tune tune;
@@ -119,6 +120,7 @@ static void batch_free(hpsi_batch* b)
         dfree(g.d_litems); dfree(g.d_band_item); dfree(g.d_xblk); dfree(g.d_gitems);
         if (g.T) cudaFree(g.T);
         if (g.part) cudaFree(g.part);
+        if (g.W) cudaFree(g.W);
         if (g.s_main) cudaStreamDestroy(g.s_main);
         if (g.s_side) cudaStreamDestroy(g.s_side);
         if (g.ev_proj) cudaEventDestroy(g.ev_proj);
@@ -181,9 +183,9 @@ static cudaError_t launch_group_exp(const hpsi_batch* b, const Group& g, int til
 {
     if (fp64(b))
         return launch_bexp<double2, double2>(g.P, g.d_gitems, (int)g.gitems.size(), g.nb_max, g.npw_max, nsplit,
-                                             tile, (const double2*)g.part, st);
+                                             tile, (const double2*)g.part, (double2*)g.W, st);
     return launch_bexp<float2, float2>(g.P, g.d_gitems, (int)g.gitems.size(), g.nb_max, g.npw_max, nsplit, tile,
-                                       (const float2*)g.part, st);
+                                       (const float2*)g.part, (float2*)g.W, st);
 }
 
 // mean milliseconds of fn over reps launches on st (after one untimed launch)
@@ -282,7 +284,7 @@ static int tune_group(hpsi_batch* b, Group& g)
     }
     t.proj_ms = best;
     if ((rc = upload_gitems(b, g, t.nsplit))) return rc;
-    // expansion tile at the chosen split, on the partials of the chosen projection
+    // expansion tile (with the split reduction) at the chosen split, on the partials of the chosen projection
     BCUDA(b, launch_group_proj(b, g, t.proj_tile, t.nsplit, st));
     best = 1e30;
     for (int tile = 0; tile < bgemm_tile_count(); ++tile) {
@@ -377,6 +379,7 @@ static int build_group(hpsi_batch* b, Group& g)
         gi.psi = li.psi;
         gi.hpsi = li.hpsi;
         gi.lam = s.d_lam;
+        gi.w_off = (size_t)g.P * g.nbands;
         gi.nb = it.nb;
         gi.npw = s.npw;
         g.gitems.push_back(gi);
@@ -404,6 +407,7 @@ static int build_group(hpsi_batch* b, Group& g)
         for (int ns : kSplits)
             if ((size_t)ns * g.P * g.nbands * cs <= kPartBudget) g.max_split = ns;
         BCUDA(b, cudaMalloc(&g.part, (size_t)g.max_split * g.P * g.nbands * cs));
+        BCUDA(b, cudaMalloc(&g.W, (size_t)g.P * g.nbands * cs));
     }
     // local arguments shared by every launch of the cell
     LocalArgs& a = g.la;

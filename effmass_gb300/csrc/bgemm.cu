@@ -7,9 +7,9 @@
 // written for item i (a k-point with its bands) as two GEMMs over the
 // projector matrix Pr_i[P][npw_i]:
 //   projection  part_i[s][P][nb_i] = conj(Pr_i) psi_i^T over the s-th K chunk
-//   expansion   hpsi_i[nb_i][G]   += (lambda . sum_s part_i[s])^T Pr_i
-// The split-K reduction and the lambda scale are fused into the expansion's
-// W-tile load (FP64 sum in split order, as in the unbatched path).
+//   reduction   W_i[P][nb_i]       = lambda . sum_s part_i[s]  (FP64 sum in split order,
+//                                   as in the unbatched path)
+//   expansion   hpsi_i[nb_i][G]   += W_i^T Pr_i
 //
 // Tiles: a 16 x 16 thread grid owning TM x TN outputs each at stride 16, so
 // the tile is (16 TM) x (16 TN) and shared-memory reads of a warp are
@@ -90,11 +90,31 @@ __global__ void __launch_bounds__(256) bproj_kernel(int P, const BGemmItem* __re
     }
 }
 
-// hpsi_i[n][g] += sum_m W[m][n] Pr_i[m][g], W[m][n] = lam[m] * sum_s part_i[s][m][n].
-// Block tile: (16 TM) bands x (16 TN) G.
-template <typename C, typename Acc, int TM, int TN>
-__global__ void __launch_bounds__(256) bexp_kernel(int P, const BGemmItem* __restrict__ items, int nsplit,
-                                                   const Acc* __restrict__ part)
+// W_i[m][n] = lam[m] * sum_s part_i[s][m][n] (FP64 sum in split order), one
+// thread per (m, n); grid (ceil(P nb_max / 256), items).
+template <typename C, typename Acc>
+__global__ void __launch_bounds__(256) bred_kernel(int P, const BGemmItem* __restrict__ items, int nsplit,
+                                                   const Acc* __restrict__ part, C* __restrict__ W)
+{
+    const BGemmItem I = items[blockIdx.y];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= P * I.nb) return;
+    const Acc* pw = part + I.part_off + idx;
+    const size_t split_stride = (size_t)P * I.nb;
+    double sr = 0.0, si = 0.0;
+    for (int s = 0; s < nsplit; ++s) {
+        const double2 v = as_c128(pw[s * split_stride]);
+        sr += v.x;
+        si += v.y;
+    }
+    const double l = I.lam[idx / I.nb];
+    W[I.w_off + idx] = from_c128<C>(make_double2(l * sr, l * si));
+}
+
+// hpsi_i[n][g] += sum_m W_i[m][n] Pr_i[m][g].  Block tile: (16 TM) bands x (16 TN) G.
+template <typename C, int TM, int TN>
+__global__ void __launch_bounds__(256) bexp_kernel(int P, const BGemmItem* __restrict__ items,
+                                                   const C* __restrict__ W)
 {
     using R = typename Real<C>::type;
     constexpr int BB = 16 * TM, BG = 16 * TN;
@@ -104,8 +124,7 @@ __global__ void __launch_bounds__(256) bexp_kernel(int P, const BGemmItem* __res
     const int g0 = blockIdx.x * BG, n0 = blockIdx.y * BB;
     if (n0 >= I.nb || g0 >= I.npw) return;  // uniform
     const C* A = static_cast<const C*>(I.pr);
-    const Acc* pw = part + I.part_off;
-    const size_t split_stride = (size_t)P * I.nb;
+    const C* Wi = W + I.w_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     R ar[TM][TN], ai[TM][TN];
 #pragma unroll
@@ -115,18 +134,7 @@ __global__ void __launch_bounds__(256) bexp_kernel(int P, const BGemmItem* __res
     for (int m0 = 0; m0 < P; m0 += KS) {
         for (int e = threadIdx.x; e < KS * BB; e += 256) {
             const int mm = e / BB, c = e % BB, m = m0 + mm, n = n0 + c;
-            double2 w = make_double2(0.0, 0.0);
-            if (m < P && n < I.nb) {
-                for (int s = 0; s < nsplit; ++s) {
-                    const double2 v = as_c128(pw[s * split_stride + (size_t)m * I.nb + n]);
-                    w.x += v.x;
-                    w.y += v.y;
-                }
-                const double l = I.lam[m];
-                w.x *= l;
-                w.y *= l;
-            }
-            Ws[mm][c] = from_c128<C>(w);
+            Ws[mm][c] = (m < P && n < I.nb) ? Wi[(size_t)m * I.nb + n] : cmake<C>(0, 0);
         }
         for (int e = threadIdx.x; e < KS * BG; e += 256) {
             const int mm = e / BG, c = e % BG, m = m0 + mm, g = g0 + c;
@@ -178,10 +186,10 @@ void proj_launch(dim3 g, int P, const BGemmItem* items, int nsplit, Acc* part, c
     bproj_kernel<C, Acc, kTiles[T][0], kTiles[T][1]><<<g, 256, 0, st>>>(P, items, nsplit, part);
 }
 
-template <typename C, typename Acc, int T>
-void exp_launch(dim3 g, int P, const BGemmItem* items, int nsplit, const Acc* part, cudaStream_t st)
+template <typename C, int T>
+void exp_launch(dim3 g, int P, const BGemmItem* items, const C* W, cudaStream_t st)
 {
-    bexp_kernel<C, Acc, kTiles[T][0], kTiles[T][1]><<<g, 256, 0, st>>>(P, items, nsplit, part);
+    bexp_kernel<C, kTiles[T][0], kTiles[T][1]><<<g, 256, 0, st>>>(P, items, W);
 }
 
 }  // namespace
@@ -214,18 +222,19 @@ cudaError_t launch_bproj(int P, const BGemmItem* items, int n_items, int nb_max,
 
 template <typename C, typename Acc>
 cudaError_t launch_bexp(int P, const BGemmItem* items, int n_items, int nb_max, int npw_max, int nsplit, int tile,
-                        const Acc* part, cudaStream_t st)
+                        const Acc* part, C* W, cudaStream_t st)
 {
     if (tile < 0 || tile >= kNumTiles || nsplit < 1) return cudaErrorInvalidValue;
     if (P == 0 || n_items == 0 || nb_max == 0 || npw_max == 0) return cudaSuccess;
+    bred_kernel<C, Acc><<<dim3(ceil_div((long)P * nb_max, 256), n_items), 256, 0, st>>>(P, items, nsplit, part, W);
     dim3 g(ceil_div(npw_max, 16 * kTiles[tile][1]), ceil_div(nb_max, 16 * kTiles[tile][0]), n_items);
     switch (tile) {
-        case 0: exp_launch<C, Acc, 0>(g, P, items, nsplit, part, st); break;
-        case 1: exp_launch<C, Acc, 1>(g, P, items, nsplit, part, st); break;
-        case 2: exp_launch<C, Acc, 2>(g, P, items, nsplit, part, st); break;
-        case 3: exp_launch<C, Acc, 3>(g, P, items, nsplit, part, st); break;
-        case 4: exp_launch<C, Acc, 4>(g, P, items, nsplit, part, st); break;
-        default: exp_launch<C, Acc, 5>(g, P, items, nsplit, part, st); break;
+        case 0: exp_launch<C, 0>(g, P, items, W, st); break;
+        case 1: exp_launch<C, 1>(g, P, items, W, st); break;
+        case 2: exp_launch<C, 2>(g, P, items, W, st); break;
+        case 3: exp_launch<C, 3>(g, P, items, W, st); break;
+        case 4: exp_launch<C, 4>(g, P, items, W, st); break;
+        default: exp_launch<C, 5>(g, P, items, W, st); break;
     }
     return cudaGetLastError();
 }
@@ -233,6 +242,6 @@ cudaError_t launch_bexp(int P, const BGemmItem* items, int n_items, int nb_max, 
 template cudaError_t launch_bproj<double2, double2>(int, const BGemmItem*, int, int, int, int, double2*, cudaStream_t);
 template cudaError_t launch_bproj<float2, float2>(int, const BGemmItem*, int, int, int, int, float2*, cudaStream_t);
 template cudaError_t launch_bexp<double2, double2>(int, const BGemmItem*, int, int, int, int, int, const double2*,
-                                                   cudaStream_t);
+                                                   double2*, cudaStream_t);
 template cudaError_t launch_bexp<float2, float2>(int, const BGemmItem*, int, int, int, int, int, const float2*,
-                                                 cudaStream_t);
+                                                 float2*, cudaStream_t);

@@ -181,6 +181,7 @@ struct BGemmItem {
     double2* hpsi;         // [nb][npw], accumulated
     const double* lam;     // [P]
     size_t part_off;       // first element of the item's partials [nsplit][P][nb]
+    size_t w_off;          // first element of the item's reduced W [P][nb]
     int nb, npw;
 };
 
@@ -191,4 +192,4 @@ cudaError_t launch_bproj(int P, const BGemmItem* items, int n_items, int nb_max,
                          cudaStream_t st);
 template <typename C, typename Acc>
 cudaError_t launch_bexp(int P, const BGemmItem* items, int n_items, int nb_max, int npw_max, int nsplit, int tile,
-                        const Acc* part, cudaStream_t st);
+                        const Acc* part, C* W, cudaStream_t st);

@@ -207,7 +207,7 @@ const char* hpsi_server_last_error(const hpsi_server* srv);
  * resident on the device, packed item after item, each [nb][npw] band-major.
  * Per cell, each phase is one launch over all of the cell's items (scatter +
  * z/y FFT planes, x FFT/V/x FFT, y/z FFT planes + gather + kinetic, the ragged
- * projection GEMM, the expansion GEMM with the fused split-K reduction); the
+ * projection GEMM, the split-K reduction with lambda, the expansion GEMM); the
  * cells run as parallel branches, the projections beside the FFTs, and the
  * whole sequence is captured in one CUDA graph.  At creation a tuner times the
  * candidate FFT block shapes, GEMM tiles and split-K counts on the plan's own
