@@ -26,6 +26,7 @@ struct KSlot {
     double* d_dbeta0 = nullptr;
     double2* d_sf = nullptr;
     int nxs = 0;
+    bool aliased = false;          // two G-vectors map to one grid point (the scatter keeps the last)
     int* d_plane = nullptr;    // plane_x[nxs], plane_off[nxs+1], ent_ig[npw], ent_jk[npw]
     int P = 0;
     ProjRow* d_rows = nullptr;

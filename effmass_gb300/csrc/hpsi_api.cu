@@ -254,12 +254,14 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
     for (int p = 0; p < nxs; ++p) plane_off[p + 1] += plane_off[p];
     std::vector<int> fill(plane_off.begin(), plane_off.end() - 1);
     std::vector<int> ent_ig(npw), ent_jk(npw);
+    bool aliased = false;
     for (int ig = 0; ig < npw; ++ig) {
         int p = plane_of_x[gi[ig]];
         int e = fill[p]++;
         bool scatter = last[(long)gi[ig] * n[1] * n[2] + jk[ig]] == ig;
         ent_ig[e] = scatter ? ig : (int)((unsigned)ig | 0x80000000u);
         ent_jk[e] = jk[ig];
+        aliased = aliased || !scatter;
     }
 
     // --- projector rows
@@ -285,6 +287,7 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
     s.npw = npw;
     for (int d = 0; d < 3; ++d) s.kf[d] = kp->k_frac[d];
     s.nxs = nxs;
+    s.aliased = aliased;
     s.P = (int)rows.size();
     if (npw > 0) {
         const int nlm = (c->lmax + 1) * (c->lmax + 1);
@@ -369,7 +372,7 @@ static int split_for(int M, int N, int K)
 // hpsi_out[nb][npw] += nonlocal(psi) using projector matrix pr (complex C)
 template <typename C, typename Acc>
 static int nonlocal_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, const C* pr,
-                          unsigned char* ws, cudaStream_t st)
+                          unsigned char* ws, cudaStream_t st, double* e_nl = nullptr)
 {
     if (s.P == 0 || nb == 0) return HPSI_OK;
     const int ns = split_for(s.P, nb, s.npw);
@@ -381,6 +384,7 @@ static int nonlocal_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, dou
     int h = c->prof.open(PH_PROJ, st);
     CUDA_TRY(c, (launch_proj_gemm<C, double2, Acc>(s.P, nb, s.npw, pr, (size_t)s.npw, psi, (size_t)s.npw, part, ns, st)));
     c->prof.close(h, st);
+    if (e_nl) CUDA_TRY(c, launch_nl_energy<Acc>(s.P, nb, ns, part, s.d_lam, e_nl, st));
     h = c->prof.open(PH_REDUCE, st);
     CUDA_TRY(c, (launch_reduce_splits<Acc, C>(s.P, nb, ns, part, s.d_lam, s.P, W, (size_t)nb, st)));
     c->prof.close(h, st);
@@ -411,7 +415,7 @@ static int chunk_bands(const KSlot& s, const hpsi_ctx* c, int nb, size_t csize)
 
 template <typename C, typename V>
 static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
-                       const V* vloc, const C* tw, cudaStream_t st)
+                       const V* vloc, const C* tw, cudaStream_t st, double* epart = nullptr)
 {
     if (nb == 0 || s.npw == 0) return HPSI_OK;
     const int* pl = s.d_plane;
@@ -430,6 +434,9 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     C* T = reinterpret_cast<C*>(ws);
     for (int b0 = 0; b0 < nb; b0 += ch) {
         int nbc = std::min(ch, nb - b0);
+        a.epart = epart;
+        a.e_band0 = b0;
+        a.v64e = epart ? c->d_v64 : nullptr;
         CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
                                         tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
     }
@@ -487,11 +494,24 @@ static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
     return HPSI_OK;
 }
 
-static size_t tc_ws(const KSlot& s, int nb)
+// Split count of the tensor-core projection.  With band energies the FP32
+// accumulation chains in TMEM are kept to kEnergyChain k-tiles per split (the
+// partials are summed in FP64): the tensor cores' FP32 accumulation drifts
+// over long chains, which the band energies would show at the 1e-8 Ha level.
+constexpr int kEnergyChain = 4;
+static int tc_splits(const KSlot& s, int nb, bool energy)
+{
+    const size_t k1 = tc_round_k(2 * (size_t)s.npw);
+    const int ns = tc_proj_splits(s.P, nb, k1);
+    if (!energy) return ns;
+    return std::max(ns, ceil_div((long)(k1 / 64), kEnergyChain));
+}
+
+static size_t tc_ws(const KSlot& s, int nb, bool energy = false)
 {
     const int NB = tc_band_rows(nb);
     const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(2 * (size_t)s.P);
-    const int ns = tc_proj_splits(s.P, nb, k1);
+    const int ns = tc_splits(s, nb, energy);
     Carver cv;
     cv.take<uint16_t>((size_t)NB * k1);
     cv.take<uint16_t>((size_t)NB * k1);
@@ -506,13 +526,13 @@ static size_t tc_ws(const KSlot& s, int nb)
 }
 
 static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
-                       cudaStream_t st)
+                       cudaStream_t st, double* e_nl = nullptr)
 {
     if (s.P == 0 || nb == 0) return HPSI_OK;
     const bool fp16 = s.tc_fmt == 0;
     const int NB = tc_band_rows(nb);
     const size_t k1 = s.tc_proj.ldk, k2 = s.tc_expand.ldk;
-    const int ns = tc_proj_splits(s.P, nb, k1);
+    const int ns = tc_splits(s, nb, e_nl != nullptr);
     Carver cv;
     const size_t ob1h = cv.take<uint16_t>((size_t)NB * k1), ob1l = cv.take<uint16_t>((size_t)NB * k1);
     const size_t ob1s = cv.take<float>((size_t)NB);
@@ -529,6 +549,9 @@ static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     c->prof.close(h, st);
     CUDA_TRY(c, tc_projection(s.tc_proj, s.P, B1, nb, ns, fp16, reinterpret_cast<float*>(ws + opart), s.d_lam, s.P, W,
                               c->d_err, st, &c->prof));
+    if (e_nl)
+        CUDA_TRY(c, tc_proj_energy(s.tc_proj, s.P, nb, ns, reinterpret_cast<const float*>(ws + opart), s.d_lam, e_nl,
+                                   st));
     h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_w_operand(W, s.P, nb, fp16, &B2, rowmax, st));
     c->prof.close(h, st);
@@ -738,28 +761,84 @@ int prepare_slot(hpsi_ctx* c, KSlot& s, int prec, bool grad, cudaStream_t st)
 }
 
 // workspace of one H|psi> on device pointers
-static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec)
+static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec, bool energy = false)
 {
     const bool fp64 = prec == HPSI_PREC_FP64;
     size_t wl = local_ws(c, s, nb, fp64 ? sizeof(double2) : sizeof(float2));
     size_t wn = fp64 ? nonlocal_ws<double2, double2>(s, nb, 1)
-                     : (is_tc(prec) ? tc_ws(s, nb) : nonlocal_ws<float2, float2>(s, nb, 1));
+                     : (is_tc(prec) ? tc_ws(s, nb, energy) : nonlocal_ws<float2, float2>(s, nb, 1));
     return std::max(wl, wn);
 }
 
 // hpsi += H psi on device pointers with an explicit workspace (prepare_slot first)
 static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, int prec, unsigned char* work,
-                     cudaStream_t st)
+                     cudaStream_t st, double* epart = nullptr, double* e_nl = nullptr)
 {
     int rc;
     if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
     if (prec == HPSI_PREC_FP64) {
-        if ((rc = local_apply<double2, double>(c, s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st))) return rc;
-        return nonlocal_apply<double2, double2>(c, s, nb, psi, hpsi, s.pr64, work, st);
+        if ((rc = local_apply<double2, double>(c, s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st, epart))) return rc;
+        return nonlocal_apply<double2, double2>(c, s, nb, psi, hpsi, s.pr64, work, st, e_nl);
     }
-    if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st))) return rc;
-    if (is_tc(prec)) return tc_nonlocal(c, s, nb, psi, hpsi, work, st);
-    return nonlocal_apply<float2, float2>(c, s, nb, psi, hpsi, s.pr32, work, st);
+    if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart))) return rc;
+    if (is_tc(prec)) return tc_nonlocal(c, s, nb, psi, hpsi, work, st, e_nl);
+    return nonlocal_apply<float2, float2>(c, s, nb, psi, hpsi, s.pr32, work, st, e_nl);
+}
+
+// Band energies beside H|psi>: scratch layout in front of the apply workspace
+struct EnergyWs {
+    size_t kn, loc, enl, epart, dots, work;
+    int nslots;
+};
+
+static EnergyWs energy_layout(const hpsi_ctx* c, int nb, int prec)
+{
+    LocalArgs a{};
+    a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
+    local_xpass_shape(&a, prec == HPSI_PREC_FP64 ? sizeof(double2) : sizeof(float2));
+    EnergyWs w;
+    w.nslots = local_energy_slots(a);
+    Carver cv;
+    w.kn = cv.take<double>(2 * (size_t)nb);
+    w.loc = cv.take<double>(2 * (size_t)nb);
+    w.enl = cv.take<double>((size_t)nb);
+    w.epart = cv.take<double>((size_t)nb * w.nslots * 2);
+    w.dots = cv.take<double>(2 * (size_t)nb);
+    w.work = cv.off;
+    return w;
+}
+
+// hpsi += H psi and e[b] = <psi_b|H|psi_b> with FP64 reductions, device pointers
+static int energies_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, double* e, int prec,
+                        unsigned char* ws, cudaStream_t st)
+{
+    int rc;
+    if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
+    const EnergyWs w = energy_layout(c, nb, prec);
+    double* kn = reinterpret_cast<double*>(ws + w.kn);
+    double* loc = reinterpret_cast<double*>(ws + w.loc);
+    double* enl = reinterpret_cast<double*>(ws + w.enl);
+    double* epart = reinterpret_cast<double*>(ws + w.epart);
+    double* dots = reinterpret_cast<double*>(ws + w.dots);
+    if (s.aliased) {
+        // two G-vectors share a grid point: the Parseval identity does not hold,
+        // so the energy is the Rayleigh quotient of the computed H|psi>
+        CUDA_TRY(c, launch_band_dot(s.npw, nb, psi, hpsi, dots, st));
+        if ((rc = apply_dev(c, s, nb, psi, hpsi, prec, ws + w.work, st))) return rc;
+        CUDA_TRY(c, launch_band_dot(s.npw, nb, psi, hpsi, dots + nb, st));
+        CUDA_TRY(c, launch_band_sub(nb, dots + nb, dots, e, st));
+        return HPSI_OK;
+    }
+    const int* ent_ig = s.d_plane + 2 * s.nxs + 1;
+    int h = c->prof.open(PH_OTHER, st);
+    CUDA_TRY(c, launch_kin_norm(s.npw, nb, psi, s.d_kin, ent_ig, kn, st));
+    c->prof.close(h, st);
+    if ((rc = apply_dev(c, s, nb, psi, hpsi, prec, ws + w.work, st, epart, enl))) return rc;
+    h = c->prof.open(PH_OTHER, st);
+    CUDA_TRY(c, launch_local_sums(nb, w.nslots, epart, loc, st));
+    CUDA_TRY(c, launch_energy_combine(nb, kn, loc, s.P > 0 ? enl : nullptr, e, st));
+    c->prof.close(h, st);
+    return HPSI_OK;
 }
 
 static size_t grad_ws_bytes(const KSlot& s, int nb, int prec)
@@ -850,6 +929,52 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
     }
     if ((rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st))) return rc;
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) {
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
+    }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_apply_energies(hpsi_ctx* c, int kid, int nb, const double* psi_, double* hpsi_, double* eout,
+                                   int flags, void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (nb > 0 && (!psi_ || !hpsi_ || !eout)) return fail(c, HPSI_ERR_BAD_ARG, "psi/hpsi/e NULL");
+    if (nb == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    if (s->npw == 0) {
+        if (dev) CUDA_TRY(c, cudaMemsetAsync(eout, 0, nb * sizeof(double), st));
+        else memset(eout, 0, nb * sizeof(double));
+        return HPSI_OK;
+    }
+    const size_t nel = (size_t)nb * s->npw;
+    Carver cv;
+    size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_hpsi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_e = dev ? 0 : cv.take<double>((size_t)nb);
+    size_t o_work = cv.off;
+    const EnergyWs w = energy_layout(c, nb, prec);
+    if ((rc = ws_reserve(c, o_work + w.work + apply_ws_bytes(c, *s, nb, prec, true)))) return rc;
+    const double2* psi = (const double2*)psi_;
+    double2* hpsi = (double2*)hpsi_;
+    double* e = eout;
+    if (!dev) {
+        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
+        hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
+        e = reinterpret_cast<double*>(c->ws + o_e);
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+    }
+    if ((rc = energies_dev(c, *s, nb, psi, hpsi, e, prec, c->ws + o_work, st))) return rc;
+    if (!dev) {
+        CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(c, cudaMemcpyAsync(eout, e, nb * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
     if (!dev || (flags & HPSI_SYNC)) {
         CUDA_TRY(c, cudaStreamSynchronize(st));
         if (is_tc(prec) && (rc = check_device_flag(c))) return rc;

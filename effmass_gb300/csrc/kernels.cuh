@@ -87,7 +87,15 @@ struct LocalArgs {
     const int* band_item;   // [bands] item of each batch band
     const int2* xblk;       // [x-pass band blocks] (item, first band within the item)
     int plane_threads;      // block size of the plane kernels (0: default)
+    // band energies (null: off): the x pass adds, per band and (j, k-tile)
+    // block, FP64 sums of V|psi(r)|^2 and |psi(r)|^2 of the G->r transform at
+    // epart[((e_band0 + band) * nslots + slot) * 2 + {0, 1}]
+    double* epart;
+    int e_band0;
+    const double* v64e;     // FP64 V(r) for those sums (null: the launch's own V)
 };
+// (j, k-tile) blocks of the x pass: the energy slots per band
+inline int local_energy_slots(const LocalArgs& a) { return ((a.n3 + a.kt - 1) / a.kt) * a.n2; }
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64);
 // choose kt/bb of the x pass for complex size csize (bytes)
@@ -193,3 +201,20 @@ cudaError_t launch_bproj(int P, const BGemmItem* items, int n_items, int nb_max,
 template <typename C, typename Acc>
 cudaError_t launch_bexp(int P, const BGemmItem* items, int n_items, int nb_max, int npw_max, int nsplit, int tile,
                         const Acc* part, C* W, cudaStream_t st);
+
+// ---- FP64 band-energy reductions (energy.cu) -------------------------------
+// out[2b] = sum_G kinetic |psi_b|^2, out[2b+1] = sum over scattered G of |psi_b|^2
+cudaError_t launch_kin_norm(int npw, int nb, const double2* psi, const double* kinetic, const int* ent_ig, double* out,
+                            cudaStream_t st);
+// out[2b], out[2b+1] = the x pass's V|psi(r)|^2 and |psi(r)|^2 sums of band b
+cudaError_t launch_local_sums(int nb, int nslots, const double* epart, double* out, cudaStream_t st);
+// out[b] = sum_p lam_p |sum_s part[s][p][b]|^2 (SIMT projection partials)
+template <typename Acc>
+cudaError_t launch_nl_energy(int P, int nb, int nsplit, const Acc* part, const double* lam, double* out,
+                             cudaStream_t st);
+// e[b] = kinetic + S1/S0 * norm + nonlocal (enl may be null)
+cudaError_t launch_energy_combine(int nb, const double* kn, const double* loc, const double* enl, double* e,
+                                  cudaStream_t st);
+// d[b] = Re <psi_b|h_b>;  e[b] = after[b] - before[b]
+cudaError_t launch_band_dot(int npw, int nb, const double2* psi, const double2* h, double* d, cudaStream_t st);
+cudaError_t launch_band_sub(int nb, const double* after, const double* before, double* e, cudaStream_t st);

@@ -44,7 +44,7 @@ struct PlaneGlobal {
 };
 
 template <typename C, bool WIDE>
-__global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
+__global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -144,8 +144,8 @@ struct XStore {
     }
 };
 
-template <typename C, typename V, bool WIDE>
-__global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
+template <typename C, typename V, bool WIDE, bool ENERGY>
+__global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::x_min) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
                                               const C* __restrict__ tw_x_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -185,8 +185,44 @@ __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb
     // G->r, times V, into the buffer the last stage does not read
     const int r = fft_last_read(a.Lx);
     C* vo = (r == 1) ? b1 : b0;
-    fft_lines_io<C, true, WIDE>(ld, XStoreV<C, V>{vo, vt, NL, KT, a.kt_f}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
-    __syncthreads();
+    if constexpr (!ENERGY) {
+        fft_lines_io<C, true, WIDE>(ld, XStoreV<C, V>{vo, vt, NL, KT, a.kt_f}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
+        __syncthreads();
+    } else {
+        // psi(r) unscaled; per line the FP64 sums of V|psi|^2 and |psi|^2, then psi <- V psi
+        fft_lines_io<C, true, WIDE>(ld, SmemLines<C>{vo, 1, NL}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
+        __syncthreads();
+        double* sums = reinterpret_cast<double*>(
+            (reinterpret_cast<uintptr_t>(xpl + n1) + 7) & ~static_cast<uintptr_t>(7));
+        for (int L = threadIdx.x; L < NL; L += blockDim.x) {
+            const int kk = L - (L / KT) * KT;
+            double s1 = 0.0, s0 = 0.0;
+            for (int x = 0; x < n1; ++x) {
+                const C v = vo[x * NL + L];
+                const V w = vt[x * KT + kk];
+                const double wv = a.v64e ? a.v64e[((size_t)x * n2 + j) * n3 + k0 + kk] : (double)w;
+                const double m = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+                s0 += m;
+                s1 += wv * m;
+                vo[x * NL + L] = cscale(v, (typename Real<C>::type)w);
+            }
+            sums[2 * L] = s1;
+            sums[2 * L + 1] = s0;
+        }
+        __syncthreads();
+        const int nslots = gridDim.x * gridDim.y, slot = blockIdx.y * gridDim.x + blockIdx.x;
+        for (int bb = threadIdx.x; bb < nbb; bb += blockDim.x) {
+            double s1 = 0.0, s0 = 0.0;
+            for (int kk = 0; kk < kt; ++kk) {
+                s1 += sums[2 * (bb * KT + kk)];
+                s0 += sums[2 * (bb * KT + kk) + 1];
+            }
+            double* e = a.epart + ((size_t)(a.e_band0 + bb0 + bb) * nslots + slot) * 2;
+            e[0] = s1;
+            e[1] = s0;
+        }
+        __syncthreads();
+    }
     // r->G, back into the sphere planes of T
     C* vother = (vo == b0) ? b1 : b0;
     const XStore<C> stT{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
@@ -194,7 +230,7 @@ __global__ void __launch_bounds__(256, Cfg<C>::x_min) x_pass(LocalArgs a, int nb
 }
 
 template <typename C, bool WIDE>
-__global__ void __launch_bounds__(Cfg<C>::plane_threads, Cfg<C>::plane_min) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
+__global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
                                                   double2* __restrict__ hpsi, const double* __restrict__ kinetic,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
@@ -262,7 +298,9 @@ template <typename C, typename V>
 static size_t xpass_smem(const LocalArgs& a)
 {
     const size_t NL = (size_t)a.kt * a.bb;
-    return sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt + sizeof(int) * a.n1;
+    size_t b = sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt + sizeof(int) * a.n1;
+    if (a.epart) b = (b + 7) / 8 * 8 + 2 * sizeof(double) * NL;  // per-line energy sums
+    return b;
 }
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64)
@@ -301,7 +339,9 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(g2r_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
     if ((e = cudaFuncSetAttribute(r2g_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
+    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
+        return e;
+    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
         return e;
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
     dim3 gp(a.nxs, nb);
@@ -311,7 +351,8 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     prof->close(h, st);
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
-    x_pass<C, V, WIDE><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    if (a.epart) x_pass<C, V, WIDE, true><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    else x_pass<C, V, WIDE, false><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
     prof->close(h, st);
     h = prof->open(PH_R2G, st);
     r2g_planes<C, WIDE><<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
@@ -327,14 +368,14 @@ static cudaError_t launch_local_batch_t(const LocalArgs& a, int nbands, int max_
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(g2r_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
     if ((e = cudaFuncSetAttribute(r2g_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
+    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
         return e;
     if (max_nxs == 0 || nbands == 0 || nxblk == 0) return cudaSuccess;
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     dim3 gp(max_nxs, nbands);
     g2r_planes<C, WIDE><<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, nxblk);
-    x_pass<C, V, WIDE><<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
+    x_pass<C, V, WIDE, false><<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
     r2g_planes<C, WIDE><<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
     return cudaGetLastError();
 }
@@ -343,7 +384,7 @@ template <typename C, typename V>
 cudaError_t launch_local_batch(const LocalArgs& a, int nbands, int max_nxs, int nxblk, C* T, const V* vloc,
                                const C* twx, const C* twy, const C* twz, cudaStream_t st)
 {
-    if (!a.items) return cudaErrorInvalidValue;
+    if (!a.items || a.epart) return cudaErrorInvalidValue;
     if (a.plane_threads > Cfg<C>::plane_threads || a.plane_threads % 32) return cudaErrorInvalidValue;
     const bool wide = fft_needs_wide(a.Lx) || fft_needs_wide(a.Ly) || fft_needs_wide(a.Lz);
     if (wide) return launch_local_batch_t<C, V, true>(a, nbands, max_nxs, nxblk, T, vloc, twx, twy, twz, st);

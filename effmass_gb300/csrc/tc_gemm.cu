@@ -724,6 +724,44 @@ cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb,
     return cudaGetLastError();
 }
 
+// out[b] = sum_p lam_p |sum_z (C[z][p][re b] + i C[z][p][im b])|^2 from the projection partials
+__global__ void __launch_bounds__(256) tc_energy_kernel(int P, int N, int nz, const float* __restrict__ part,
+                                                        const double* __restrict__ lam, double* __restrict__ out)
+{
+    __shared__ double red[32];
+    const int b = blockIdx.x, t = b / 128, j = b % 128;
+    const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
+    double e = 0.0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        double re = 0.0, im = 0.0;
+        for (int z = 0; z < nz; ++z) {
+            const float* row = part + ((size_t)z * P + p) * N;
+            re += row[cre];
+            im += row[cim];
+        }
+        e += lam[p] * (re * re + im * im);
+    }
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        out[b] = s;
+    }
+}
+
+cudaError_t tc_proj_energy(const TcOperand& A, int P, int nb, int nsplit, const float* part, const double* lam,
+                           double* out, cudaStream_t st)
+{
+    if (nb == 0) return cudaSuccess;
+    const int ktiles = (int)(A.ldk / BK);
+    const int per = ceil_div(ktiles, nsplit);
+    const int nz = ceil_div(ktiles, per);
+    tc_energy_kernel<<<nb, 256, 0, st>>>(P, tc_band_rows(nb), nz, part, lam, out);
+    return cudaGetLastError();
+}
+
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi,
                          int* err, cudaStream_t st, Prof* prof)
 {

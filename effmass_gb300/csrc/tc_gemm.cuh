@@ -43,6 +43,9 @@ cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B
 // W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null)
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                           const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof);
+// out[b] = sum_p lam_p |<p|psi_b>|^2 in FP64 from the partials of a tc_projection
+cudaError_t tc_proj_energy(const TcOperand& A, int P, int nb, int nsplit, const float* part, const double* lam,
+                           double* out, cudaStream_t st);
 // hpsi[b][G] += sum_p W[p][b] Pr[p][G]
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
                          cudaStream_t st, Prof* prof);

@@ -151,6 +151,24 @@ class Hamiltonian:
         check(self._lib.hpsi_apply(self._ctx, kid, nb, p, h, self.flags(precision, dev_p), _stream_for(dev_p)),
               self._ctx)
 
+    def apply_energies(self, kid: int, nb: int, psi, hpsi, precision: Optional[str] = None, e=None):
+        """hpsi += H psi and return e[b] = <psi_b|H|psi_b> (FP64 reductions on the device)."""
+        npw = self.dim(kid)
+        p, dev_p = _ptr(psi, npw, nb, "psi")
+        h, dev_h = _ptr(hpsi, npw, nb, "hpsi")
+        if dev_p != dev_h:
+            raise HpsiError(abi.HPSI_ERR_BAD_ARG, "psi and hpsi must both be host or both be device arrays")
+        if e is None:
+            if dev_p:
+                import torch
+                e = torch.zeros(nb, dtype=torch.float64, device=psi.device)
+            else:
+                e = np.zeros(nb, dtype=np.float64)
+        ep = e.data_ptr() if dev_p else e.ctypes.data
+        check(self._lib.hpsi_apply_energies(self._ctx, kid, nb, p, h, ep, self.flags(precision, dev_p),
+                                            _stream_for(dev_p)), self._ctx)
+        return e
+
     def grad_apply(self, kid: int, nb: int, psi, out: GradHPsi, precision: Optional[str] = None):
         npw = self.dim(kid)
         p, dev = _ptr(psi, npw, nb, "psi")

@@ -125,6 +125,19 @@ int hpsi_dim(const hpsi_ctx* ctx, int kid);
 int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
                int flags, void* stream);
 
+/* hpsi += H psi (as hpsi_apply) and e[b] = <psi_b|H|psi_b> (Ha) with FP64
+ * reductions on the device: kinetic energy summed in FP64; local energy
+ * (1/N) sum_r V|psi_b(r)|^2 from the G->r transform of the call, divided by
+ * that transform's own Parseval norm sum_r |psi_b(r)|^2 / (N sum_G |psi_b|^2),
+ * which cancels the gain error of the complex64 FFTs; nonlocal energy
+ * sum_p lambda_p |<p|psi_b>|^2 from the projection's partial sums.  When two
+ * G-vectors of the k-point share a grid point the Rayleigh quotient of the
+ * computed hpsi is returned instead.  e: nb doubles (device memory with
+ * HPSI_DEVICE_PTRS).  The reference forms these Rayleigh quotients on the host
+ * (test/H_psi/test_hpsi_eigen.cpp:92-106); it has no such call. */
+int hpsi_apply_energies(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi, double* e,
+                        int flags, void* stream);
+
 /* d{x,y,z}[b] += dH/dk_{x,y,z} psi[b]; NULL outputs are skipped.
  * (The tensor-core precisions use the FP32 GEMMs here.) */
 int hpsi_grad_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi,
