@@ -44,6 +44,8 @@ def parse():
                     help="requests of the served Poisson stream (0 skips serving)")
     ap.add_argument("--serving-rate", type=float, default=200.0)
     ap.add_argument("--serving-lanes", type=int, default=4)
+    ap.add_argument("--no-kp", action="store_true",
+                    help="skip the k.p workload (64-atom cell, 256 bands, 7 k-points, velocity + FP64 sums)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched k-point workload (fcc2 MP 6^3 x 32 + sc8 MP 4^3 x 48 bands)")
     return ap.parse_args()
@@ -188,6 +190,25 @@ def run_gb300(args, rank, world, local):
     e_mx = torch.einsum("bg,bg->b", psi_d[:nchk].conj(), hmx).real
     e_64 = torch.einsum("bg,bg->b", psi_d[:nchk].conj(), h64).real
     de = float((e_mx - e_64).abs().max())
+    # band energies through hpsi_apply_energies (FP64 reductions on the device,
+    # Parseval-normalised local energy), all nb bands, against its FP64 path
+    e_all = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    h_e = torch.zeros_like(psi_d)
+    H.apply_energies(0, nb, psi_d, h_e, args.prec, e=e_all)
+    e_all64 = H.apply_energies(0, nb, psi_d, torch.zeros_like(psi_d), "fp64")
+    de_api = float((e_all - e_all64).abs().max())
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(args.steps):
+        H.apply_energies(0, nb, psi_d, h_e, args.prec, e=e_all)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    ms_e = g0.elapsed_time(g1) / args.steps
+    energies = {"api": "hpsi_apply_energies (H|psi> + FP64 band energies)", "bands": nb,
+                "max_abs_diff_vs_fp64_Ha": de_api, "value": nb / (ms_e * 1e-3), "unit": "band-apps/s",
+                "ms_per_step": ms_e}
+    del h_e
 
     fp64 = None
     if not args.no_fp64 and args.prec != "fp64":
@@ -283,6 +304,9 @@ def run_gb300(args, rank, world, local):
     batched = None
     if rank == 0 and not args.no_batched:
         batched = run_batched(args)
+    kp_out = None
+    if rank == 0 and not args.no_kp:
+        kp_out = run_kp(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -304,11 +328,12 @@ def run_gb300(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "1 GPU",
                    "l2": "inputs larger than L2 (projector matrix %d MB, psi %d MB)" % (P * npw * csz >> 20,
                                                                                        psi.nbytes >> 20)},
-        "rel_err_vs_fp64": err, "band_energy_max_abs_diff_Ha": de,
+        "rel_err_vs_fp64": err, "band_energy_max_abs_diff_Ha": de_api,
+        "rayleigh_quotient_of_hpsi_max_abs_diff_Ha": de, "band_energies": energies,
         "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "grad_value": grad_value, "grad_unit": "band-apps/s of dH/dk_{x,y,z}|psi> (all three directions)",
         "e2e": e2e, "roofline": roof, "roofline_gemm": roof_gemm, "phases": phases, "gpu_launches": gpu_launches,
-        "cpu_baseline": cpu, "clocks": clk, "serving": serving, "batched": batched,
+        "cpu_baseline": cpu, "clocks": clk, "serving": serving, "batched": batched, "kp": kp_out,
     }
     if rank == 0:
         print(json.dumps(out))
@@ -535,6 +560,75 @@ def run_batched(args):
         "gpu_launches_per_run": 6 * len(cells), "tuned": infos["fp32"], "local_roofline": roof,
         "timing": "CUDA events over %d graph launches on resident buffers (psi %d MB > L2)" % (
             steps, r32["n_complex"] * 16 >> 20),
+    }
+
+
+def run_kp(args):
+    """k.p effective-mass matrix elements: the 64-atom cell with 256 bands at 7
+    k-points (Gamma and Gamma +- delta along x, y, z, delta = 0.01 * 2 pi / a),
+    seeded orthonormal psi and band energies sorted uniform in [-0.5, 0.8] Ha;
+    <psi_m|dH/dk_a|psi_n> for all band pairs on the tensor cores and the FP64
+    sums over energy denominators for the lowest 8 bands."""
+    import numpy as np
+    import torch
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import Hamiltonian, kp_sums
+    nb, n_low = 256, 8
+    sysm = S.make_system("sc64")
+    d = 0.01  # fractional: the reciprocal vectors of the cubic cell are 2 pi / a
+    kpts = [(0.0, 0.0, 0.0)] + [tuple(sg * d if i == ax else 0.0 for i in range(3)) for ax in range(3)
+                                for sg in (1, -1)]
+    H = Hamiltonian(sysm)
+    psis = []
+    for i, k in enumerate(kpts):
+        kp = S.g_sphere(sysm.lattice, k, sysm.ecut)
+        H.set_kpoint(i, kp)
+        psis.append(torch.from_numpy(S.make_bands(kp, nb, seed=700 + i)).cuda())
+    E = torch.from_numpy(np.sort(np.random.default_rng(77).uniform(-0.5, 0.8, nb))).cuda()
+    stream = torch.cuda.current_stream()
+    M = [torch.zeros((3, nb, nb), dtype=torch.complex128, device="cuda") for _ in kpts]
+
+    def run_all(prec):
+        out = []
+        for i in range(len(kpts)):
+            H.velocity_matrix(i, nb, psis[i], out=M[i], precision=prec)
+            out.append(kp_sums(M[i], E, n_low))
+        return out
+
+    run_all("tc")  # set-up: projector and tensor-core operands of every k-point
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 2
+    e0.record(stream)
+    for _ in range(reps):
+        sums = run_all("tc")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_all = e0.elapsed_time(e1) / reps
+    Mtc = [m.clone() for m in M]
+    # FP64 reference of every k-point (velocity and sums)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    sums64 = run_all("fp64")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = f0.elapsed_time(f1)
+    rel = max(float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) for a, b in zip(Mtc, M))
+    ds = max(float((a[0] - b[0]).abs().max() / b[0].abs().max()) for a, b in zip(sums, sums64))
+    npw = [H.dim(i) for i in range(len(kpts))]
+    flops = sum(3 * 8.0 * nb * nb * n for n in npw)  # psi^H (dH psi) algorithmic flops
+    H.close()
+    inv_mass = [(np.eye(3) + 2 * s[0][n].cpu().numpy()).diagonal().tolist() for s in sums[:1] for n in range(2)]
+    return {
+        "workload": "sc64 (64-atom SC diamond, 72^3, Ecut 20 Ha), 256 bands x 7 k (Gamma, Gamma +- 0.01 2pi/a x,y,z)",
+        "ms_all_kpoints": ms_all, "ms_per_kpoint": ms_all / len(kpts), "fp64_ms_all_kpoints": ms64,
+        "speedup_vs_fp64": ms64 / ms_all,
+        "velocity_gemm_flops_per_kpoint": flops / len(kpts),
+        "velocity_tflops_incl_gradient": flops / (ms_all * 1e-3) / 1e12,
+        "rel_err_velocity_tc_vs_fp64": rel, "kp_sums_max_rel_diff_tc_vs_fp64": ds,
+        "n_low": n_low, "example_inverse_mass_diag_gamma_bands_0_1": inv_mass,
+        "note": "each k-point: dH/dk_{x,y,z}|psi> (tensor-core projector GEMMs) + psi^H G_a on the tensor cores "
+                "(split FP16, FP32 accumulation, FP64 split-K sums) + FP64 k.p sums; timed with CUDA events",
     }
 
 

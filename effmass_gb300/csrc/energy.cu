@@ -7,9 +7,9 @@
 //   kinetic   sum_G kinetic(G) |psi(G)|^2                         (exact inputs)
 //   local     (1/N) sum_r V(r) |psi(r)|^2, from the x pass's FP64 sums
 //             S1 = sum_r V |psi_32(r)|^2 and S0 = sum_r |psi_32(r)|^2 of the
-//             complex64 transform, as S1 / S0 * sum_G' |psi(G)|^2 (Parseval:
-//             S0 = N sum_G' |psi|^2 in exact arithmetic, so the transform's
-//             gain error cancels); G' = the G-vectors scattered to the grid
+//             complex64 transform, as S1 / S0 * sum_G |psi(G)|^2 (Parseval:
+//             S0 = N sum_G |psi|^2 in exact arithmetic, so the transform's
+//             gain error cancels; every G-vector has its own grid point)
 //   nonlocal  sum_p lambda_p |<p|psi>|^2 from the projection's split-K
 //             partial sums.
 // All reductions run in a fixed order (one block per band, tree in shared
@@ -32,27 +32,29 @@ __device__ __forceinline__ double block_sum(double v, double* red)
     return r;  // valid in thread 0
 }
 
-// out[b] = {sum_G kinetic |psi|^2, sum_{scattered G} |psi|^2}
+// out[b] = {sum_G kinetic |psi|^2, sum_G |psi|^2} in G order (coalesced); used
+// when every G-vector has its own grid point
+// Grid (nb, KN_CHUNKS): chunk c of band b writes out[(b * KN_CHUNKS + c) * 2 + {0, 1}].
+constexpr int KN_CHUNKS = 8;
 __global__ void __launch_bounds__(256) kin_norm_kernel(int npw, const double2* __restrict__ psi,
-                                                       const double* __restrict__ kinetic,
-                                                       const int* __restrict__ ent_ig, double* __restrict__ out)
+                                                       const double* __restrict__ kinetic, double* __restrict__ out)
 {
     __shared__ double red[32];
     const double2* p = psi + (size_t)blockIdx.x * npw;
+    const int per = (npw + KN_CHUNKS - 1) / KN_CHUNKS;
+    const int g0 = blockIdx.y * per, g1 = min(npw, g0 + per);
     double k = 0.0, n = 0.0;
-    for (int e = threadIdx.x; e < npw; e += blockDim.x) {
-        const int ig = ent_ig[e];
-        const int g = ig & 0x7fffffff;
+    for (int g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
         const double2 v = p[g];
         const double m = v.x * v.x + v.y * v.y;
         k += kinetic[g] * m;
-        if (ig >= 0) n += m;
+        n += m;
     }
     k = block_sum(k, red);
     n = block_sum(n, red);
     if (threadIdx.x == 0) {
-        out[2 * blockIdx.x] = k;
-        out[2 * blockIdx.x + 1] = n;
+        out[2 * (blockIdx.x * KN_CHUNKS + blockIdx.y)] = k;
+        out[2 * (blockIdx.x * KN_CHUNKS + blockIdx.y) + 1] = n;
     }
 }
 
@@ -102,9 +104,14 @@ __global__ void combine_kernel(int nb, const double* __restrict__ kn, const doub
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nb) return;
+    double kin = 0.0, nrm = 0.0;
+    for (int c = 0; c < KN_CHUNKS; ++c) {
+        kin += kn[2 * (b * KN_CHUNKS + c)];
+        nrm += kn[2 * (b * KN_CHUNKS + c) + 1];
+    }
     const double s1 = loc[2 * b], s0 = loc[2 * b + 1];
-    const double el = s0 > 0.0 ? s1 / s0 * kn[2 * b + 1] : 0.0;
-    e[b] = kn[2 * b] + el + (enl ? enl[b] : 0.0);
+    const double el = s0 > 0.0 ? s1 / s0 * nrm : 0.0;
+    e[b] = kin + el + (enl ? enl[b] : 0.0);
 }
 
 // d[b] = Re sum_G conj(psi) h (the Rayleigh-quotient numerator)
@@ -126,13 +133,62 @@ __global__ void sub_kernel(int nb, const double* __restrict__ after, const doubl
     if (b < nb) e[b] = after[b] - before[b];
 }
 
+// k·p sums of band n (one block per band of the lowest n_low):
+//   S[n][a][b] = sum_{m != n, |E_n - E_m| > tol} Re(M_a[n][m] M_b[m][n]) / (E_n - E_m)
+// with M_a[m][n] = <psi_m|dH/dk_a|psi_n> at M[(a nb + m) nb + n]; FP64.
+__global__ void __launch_bounds__(256) kp_sums_kernel(int nb, const double2* __restrict__ M,
+                                                      const double* __restrict__ E, double tol,
+                                                      double* __restrict__ S, int* __restrict__ skipped)
+{
+    __shared__ double red[32];
+    const int n = blockIdx.x;
+    const size_t mm = (size_t)nb * nb;
+    double acc[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) acc[i] = 0.0;
+    double sk = 0.0;
+    for (int m = threadIdx.x; m < nb; m += blockDim.x) {
+        if (m == n) continue;
+        const double de = E[n] - E[m];
+        if (fabs(de) <= tol) {
+            sk += 1.0;
+            continue;
+        }
+        const double inv = 1.0 / de;
+        double2 a[3], b[3];
+#pragma unroll
+        for (int al = 0; al < 3; ++al) {
+            a[al] = M[al * mm + (size_t)n * nb + m];
+            b[al] = M[al * mm + (size_t)m * nb + n];
+        }
+#pragma unroll
+        for (int al = 0; al < 3; ++al)
+#pragma unroll
+            for (int be = 0; be < 3; ++be) acc[al * 3 + be] += (a[al].x * b[be].x - a[al].y * b[be].y) * inv;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const double v = block_sum(acc[i], red);
+        if (threadIdx.x == 0) S[(size_t)n * 9 + i] = v;
+    }
+    const double k = block_sum(sk, red);
+    if (threadIdx.x == 0 && skipped) skipped[n] = (int)k;
+}
+
 }  // namespace
 
-cudaError_t launch_kin_norm(int npw, int nb, const double2* psi, const double* kinetic, const int* ent_ig, double* out,
-                            cudaStream_t st)
+cudaError_t launch_kp_sums(int nb, int n_low, const double2* M, const double* E, double tol, double* S, int* skipped,
+                           cudaStream_t st)
+{
+    if (n_low == 0) return cudaSuccess;
+    kp_sums_kernel<<<n_low, 256, 0, st>>>(nb, M, E, tol, S, skipped);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kin_norm(int npw, int nb, const double2* psi, const double* kinetic, double* out, cudaStream_t st)
 {
     if (nb == 0) return cudaSuccess;
-    kin_norm_kernel<<<nb, 256, 0, st>>>(npw, psi, kinetic, ent_ig, out);
+    kin_norm_kernel<<<dim3(nb, KN_CHUNKS), 256, 0, st>>>(npw, psi, kinetic, out);
     return cudaGetLastError();
 }
 
@@ -176,3 +232,5 @@ cudaError_t launch_band_sub(int nb, const double* after, const double* before, d
 
 template cudaError_t launch_nl_energy<double2>(int, int, int, const double2*, const double*, double*, cudaStream_t);
 template cudaError_t launch_nl_energy<float2>(int, int, int, const float2*, const double*, double*, cudaStream_t);
+
+int kin_norm_words(int nb) { return 2 * KN_CHUNKS * nb; }

@@ -436,7 +436,7 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
         int nbc = std::min(ch, nb - b0);
         a.epart = epart;
         a.e_band0 = b0;
-        a.v64e = epart ? c->d_v64 : nullptr;
+        a.v64e = (epart && sizeof(V) == sizeof(float)) ? c->d_v64 : nullptr;
         CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
                                         tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
     }
@@ -498,7 +498,10 @@ static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
 // accumulation chains in TMEM are kept to kEnergyChain k-tiles per split (the
 // partials are summed in FP64): the tensor cores' FP32 accumulation drifts
 // over long chains, which the band energies would show at the 1e-8 Ha level.
-constexpr int kEnergyChain = 4;
+constexpr int kEnergyChain = 16;
+// the band-pair velocity GEMMs (K = 2 npw deep, results compared element-wise)
+// need shorter chains still: 4 k-tiles keep them within 1e-6 of FP64
+constexpr int kVelocityChain = 4;
 static int tc_splits(const KSlot& s, int nb, bool energy)
 {
     const size_t k1 = tc_round_k(2 * (size_t)s.npw);
@@ -522,6 +525,7 @@ static size_t tc_ws(const KSlot& s, int nb, bool energy = false)
     cv.take<uint16_t>((size_t)NB * k2);
     cv.take<float>((size_t)NB);
     cv.take<unsigned>((size_t)nb);
+    if (energy) cv.take<double>((size_t)s.P * nb);
     return cv.off;
 }
 
@@ -541,6 +545,7 @@ static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     const size_t ob2h = cv.take<uint16_t>((size_t)NB * k2), ob2l = cv.take<uint16_t>((size_t)NB * k2);
     const size_t ob2s = cv.take<float>((size_t)NB);
     unsigned* rowmax = reinterpret_cast<unsigned*>(ws + cv.take<unsigned>((size_t)nb));
+    double* eterm = e_nl ? reinterpret_cast<double*>(ws + cv.take<double>((size_t)s.P * nb)) : nullptr;
     TcOperand B1{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
     TcOperand B2{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
     float2* W = reinterpret_cast<float2*>(ws + ow);
@@ -548,10 +553,7 @@ static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &B1, rowmax, st));
     c->prof.close(h, st);
     CUDA_TRY(c, tc_projection(s.tc_proj, s.P, B1, nb, ns, fp16, reinterpret_cast<float*>(ws + opart), s.d_lam, s.P, W,
-                              c->d_err, st, &c->prof));
-    if (e_nl)
-        CUDA_TRY(c, tc_proj_energy(s.tc_proj, s.P, nb, ns, reinterpret_cast<const float*>(ws + opart), s.d_lam, e_nl,
-                                   st));
+                              c->d_err, st, &c->prof, eterm, e_nl));
     h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_w_operand(W, s.P, nb, fp16, &B2, rowmax, st));
     c->prof.close(h, st);
@@ -799,7 +801,7 @@ static EnergyWs energy_layout(const hpsi_ctx* c, int nb, int prec)
     EnergyWs w;
     w.nslots = local_energy_slots(a);
     Carver cv;
-    w.kn = cv.take<double>(2 * (size_t)nb);
+    w.kn = cv.take<double>((size_t)kin_norm_words(nb));
     w.loc = cv.take<double>(2 * (size_t)nb);
     w.enl = cv.take<double>((size_t)nb);
     w.epart = cv.take<double>((size_t)nb * w.nslots * 2);
@@ -829,9 +831,8 @@ static int energies_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, doubl
         CUDA_TRY(c, launch_band_sub(nb, dots + nb, dots, e, st));
         return HPSI_OK;
     }
-    const int* ent_ig = s.d_plane + 2 * s.nxs + 1;
     int h = c->prof.open(PH_OTHER, st);
-    CUDA_TRY(c, launch_kin_norm(s.npw, nb, psi, s.d_kin, ent_ig, kn, st));
+    CUDA_TRY(c, launch_kin_norm(s.npw, nb, psi, s.d_kin, kn, st));
     c->prof.close(h, st);
     if ((rc = apply_dev(c, s, nb, psi, hpsi, prec, ws + w.work, st, epart, enl))) return rc;
     h = c->prof.open(PH_OTHER, st);
@@ -858,14 +859,51 @@ static int grad_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* 
                                   : grad_device<float2, float2>(c, s, nb, psi, d, work, st);
 }
 
-// velocity workspace: G_a (3 nb npw complex128), psi^H G partials, then the gradient workspace
+// velocity workspace: G_a (3 nb npw complex128), then either the gradient's
+// workspace or (after the gradient) the psi^H G GEMM's: SIMT split partials, or
+// the tensor-core operands (psi rows, G_a band rows) and partials
+struct VelWs {
+    size_t g, rest;           // G_a; start of the shared region
+    size_t vp;                // SIMT partials (relative to rest)
+    size_t ah, al, as, bh, bl, bs, part, rowmax;  // tensor-core pieces (relative to rest)
+    size_t gemm_bytes;        // bytes of the GEMM region
+    int nsv;                  // SIMT split count
+    int ns_tc;                // tensor-core split count
+    size_t k1;
+};
+
+static VelWs vel_layout(const KSlot& s, int nb, int prec)
+{
+    VelWs w{};
+    Carver cv;
+    w.g = cv.take<double2>((size_t)3 * nb * s.npw);
+    w.rest = cv.off;
+    w.nsv = split_for(nb, nb, s.npw);
+    Carver g;
+    if (is_tc(prec)) {
+        const int NB = tc_band_rows(nb);
+        w.k1 = tc_round_k(2 * (size_t)s.npw);
+        // short FP32 accumulation chains in TMEM (FP64 sums of the splits)
+        w.ns_tc = std::max(tc_proj_splits(nb, nb, w.k1), ceil_div((long)(w.k1 / 64), kVelocityChain));
+        w.ah = g.take<uint16_t>((size_t)nb * w.k1);
+        w.al = g.take<uint16_t>((size_t)nb * w.k1);
+        w.as = g.take<float>((size_t)nb);
+        w.bh = g.take<uint16_t>((size_t)NB * w.k1);
+        w.bl = g.take<uint16_t>((size_t)NB * w.k1);
+        w.bs = g.take<float>((size_t)NB);
+        w.part = g.take<float>((size_t)w.ns_tc * nb * NB);
+        w.rowmax = g.take<unsigned>((size_t)nb);
+    } else {
+        w.vp = g.take<double2>((size_t)w.nsv * nb * nb);
+    }
+    w.gemm_bytes = g.off;
+    return w;
+}
+
 static size_t vel_ws_bytes(const KSlot& s, int nb, int prec)
 {
-    const int nsv = split_for(nb, nb, s.npw);
-    Carver cv;
-    cv.take<double2>((size_t)3 * nb * s.npw);
-    cv.take<double2>((size_t)nsv * nb * nb);
-    return cv.off + grad_ws_bytes(s, nb, prec);
+    const VelWs w = vel_layout(s, nb, prec);
+    return w.rest + std::max(w.gemm_bytes, grad_ws_bytes(s, nb, prec));
 }
 
 // m[a][i][j] = sum_G conj(psi_i) (dH_a psi_j), overwritten, device pointers
@@ -873,29 +911,46 @@ static int velocity_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, doubl
                         cudaStream_t st)
 {
     const size_t nel = (size_t)nb * s.npw;
-    const int nsv = split_for(nb, nb, s.npw);
-    Carver cv;
-    const size_t o_g = cv.take<double2>(3 * nel);
-    const size_t o_vp = cv.take<double2>((size_t)nsv * nb * nb);
-    double2* g = reinterpret_cast<double2*>(ws + o_g);
+    const VelWs w = vel_layout(s, nb, prec);
+    double2* g = reinterpret_cast<double2*>(ws + w.g);
+    unsigned char* rest = ws + w.rest;
     CUDA_TRY(c, cudaMemsetAsync(g, 0, 3 * nel * sizeof(double2), st));
     double2* d[3] = {g, g + nel, g + 2 * nel};
-    int rc = grad_dev(c, s, nb, psi, d, prec, ws + cv.off, st);
+    int rc = grad_dev(c, s, nb, psi, d, prec, rest, st);
     if (rc) return rc;
+    if (is_tc(prec)) {
+        // tensor cores: psi rows split once, each G_a as the band operand.  Both
+        // tensor-core precisions use the scaled FP16 split here: a BF16 hi + lo
+        // pair holds a value to ~2^-17, which leaves ~7e-6 in these K = 2 npw
+        // band-pair sums, while the FP16 pair (per-row power-of-two scale) holds ~2^-22
+        const bool fp16 = true;
+        TcOperand A{rest + w.ah, rest + w.al, reinterpret_cast<float*>(rest + w.as), w.k1};
+        TcOperand B{rest + w.bh, rest + w.bl, reinterpret_cast<float*>(rest + w.bs), w.k1};
+        unsigned* rowmax = reinterpret_cast<unsigned*>(rest + w.rowmax);
+        float* part = reinterpret_cast<float*>(rest + w.part);
+        int h = c->prof.open(PH_OTHER, st);
+        CUDA_TRY(c, tc_rows_operand(psi, nb, s.npw, fp16, &A, st));
+        for (int a = 0; a < 3; ++a) {
+            CUDA_TRY(c, tc_band_operand(d[a], nb, s.npw, fp16, &B, rowmax, st));
+            CUDA_TRY(c, tc_gemm_c128(A, nb, B, nb, w.ns_tc, fp16, part, m + (size_t)a * nb * nb, c->d_err, st));
+        }
+        c->prof.close(h, st);
+        return HPSI_OK;
+    }
     for (int a = 0; a < 3; ++a) {
         int h = c->prof.open(PH_OTHER, st);
         if (prec == HPSI_PREC_FP64) {
-            double2* vp = reinterpret_cast<double2*>(ws + o_vp);
+            double2* vp = reinterpret_cast<double2*>(rest + w.vp);
             CUDA_TRY(c, (launch_proj_gemm<double2, double2, double2>(nb, nb, s.npw, psi, (size_t)s.npw, d[a],
-                                                                     (size_t)s.npw, vp, nsv, st)));
-            CUDA_TRY(c, (launch_reduce_splits<double2, double2>(nb, nb, nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
+                                                                     (size_t)s.npw, vp, w.nsv, st)));
+            CUDA_TRY(c, (launch_reduce_splits<double2, double2>(nb, nb, w.nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
                                                                 (size_t)nb, st)));
         } else {
             // FP32 products of the FP64 inputs, FP64 split-K reduction
-            float2* vp = reinterpret_cast<float2*>(ws + o_vp);
+            float2* vp = reinterpret_cast<float2*>(rest + w.vp);
             CUDA_TRY(c, (launch_proj_gemm<double2, double2, float2>(nb, nb, s.npw, psi, (size_t)s.npw, d[a],
-                                                                    (size_t)s.npw, vp, nsv, st)));
-            CUDA_TRY(c, (launch_reduce_splits<float2, double2>(nb, nb, nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
+                                                                    (size_t)s.npw, vp, w.nsv, st)));
+            CUDA_TRY(c, (launch_reduce_splits<float2, double2>(nb, nb, w.nsv, vp, nullptr, 0, m + (size_t)a * nb * nb,
                                                                (size_t)nb, st)));
         }
         c->prof.close(h, st);
@@ -979,6 +1034,53 @@ extern "C" int hpsi_apply_energies(hpsi_ctx* c, int kid, int nb, const double* p
         CUDA_TRY(c, cudaStreamSynchronize(st));
         if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
     }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_kp_sums(int nb, int n_low, const double* m_, const double* e_in, double deg_tol, double* s_out,
+                            int* n_skipped, int flags, void* stream)
+{
+    if (nb < 0 || n_low < 0 || n_low > nb) return fail(nullptr, HPSI_ERR_BAD_ARG, "need 0 <= n_low <= nb");
+    if (n_low == 0) return HPSI_OK;
+    if (!m_ || !e_in || !s_out) return fail(nullptr, HPSI_ERR_BAD_ARG, "m/e/s NULL");
+    if (!(deg_tol >= 0.0)) return fail(nullptr, HPSI_ERR_BAD_ARG, "deg_tol must be >= 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t mb = (size_t)3 * nb * nb * sizeof(double2), eb = (size_t)nb * sizeof(double);
+    const size_t sb = (size_t)n_low * 9 * sizeof(double), kb = (size_t)n_low * sizeof(int);
+    const double2* M = (const double2*)m_;
+    const double* E = e_in;
+    double* S = s_out;
+    int* K = n_skipped;
+    unsigned char* buf = nullptr;
+    cudaError_t e;
+#define KP_TRY(expr)                                                                                          \
+    do {                                                                                                       \
+        if ((e = (expr)) != cudaSuccess) {                                                                     \
+            if (buf) cudaFree(buf);                                                                            \
+            return fail(nullptr, e == cudaErrorMemoryAllocation ? HPSI_ERR_OOM : HPSI_ERR_CUDA, "%s: %s", #expr, \
+                        cudaGetErrorString(e));                                                                \
+        }                                                                                                      \
+    } while (0)
+    if (!dev) {
+        KP_TRY(cudaMalloc(&buf, mb + eb + sb + kb));
+        M = reinterpret_cast<const double2*>(buf);
+        E = reinterpret_cast<const double*>(buf + mb);
+        S = reinterpret_cast<double*>(buf + mb + eb);
+        K = reinterpret_cast<int*>(buf + mb + eb + sb);
+        KP_TRY(cudaMemcpyAsync((void*)M, m_, mb, cudaMemcpyHostToDevice, st));
+        KP_TRY(cudaMemcpyAsync((void*)E, e_in, eb, cudaMemcpyHostToDevice, st));
+    }
+    KP_TRY(launch_kp_sums(nb, n_low, M, E, deg_tol, S, K, st));
+    if (!dev) {
+        KP_TRY(cudaMemcpyAsync(s_out, S, sb, cudaMemcpyDeviceToHost, st));
+        if (n_skipped) KP_TRY(cudaMemcpyAsync(n_skipped, K, kb, cudaMemcpyDeviceToHost, st));
+        KP_TRY(cudaStreamSynchronize(st));
+        cudaFree(buf);
+    } else if (flags & HPSI_SYNC) {
+        KP_TRY(cudaStreamSynchronize(st));
+    }
+#undef KP_TRY
     return HPSI_OK;
 }
 

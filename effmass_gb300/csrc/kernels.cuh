@@ -203,18 +203,22 @@ cudaError_t launch_bexp(int P, const BGemmItem* items, int n_items, int nb_max, 
                         const Acc* part, C* W, cudaStream_t st);
 
 // ---- FP64 band-energy reductions (energy.cu) -------------------------------
-// out[2b] = sum_G kinetic |psi_b|^2, out[2b+1] = sum over scattered G of |psi_b|^2
-cudaError_t launch_kin_norm(int npw, int nb, const double2* psi, const double* kinetic, const int* ent_ig, double* out,
-                            cudaStream_t st);
+// per band, chunked partial sums of kinetic |psi|^2 and |psi|^2 over G (kin_norm_words(nb) doubles)
+cudaError_t launch_kin_norm(int npw, int nb, const double2* psi, const double* kinetic, double* out, cudaStream_t st);
+int kin_norm_words(int nb);
 // out[2b], out[2b+1] = the x pass's V|psi(r)|^2 and |psi(r)|^2 sums of band b
 cudaError_t launch_local_sums(int nb, int nslots, const double* epart, double* out, cudaStream_t st);
 // out[b] = sum_p lam_p |sum_s part[s][p][b]|^2 (SIMT projection partials)
 template <typename Acc>
 cudaError_t launch_nl_energy(int P, int nb, int nsplit, const Acc* part, const double* lam, double* out,
                              cudaStream_t st);
-// e[b] = kinetic + S1/S0 * norm + nonlocal (enl may be null)
+// e[b] = kinetic + S1/S0 * norm + nonlocal (kn from launch_kin_norm; enl may be null)
 cudaError_t launch_energy_combine(int nb, const double* kn, const double* loc, const double* enl, double* e,
                                   cudaStream_t st);
 // d[b] = Re <psi_b|h_b>;  e[b] = after[b] - before[b]
 cudaError_t launch_band_dot(int npw, int nb, const double2* psi, const double2* h, double* d, cudaStream_t st);
 cudaError_t launch_band_sub(int nb, const double* after, const double* before, double* e, cudaStream_t st);
+// S[n][a][b] = sum_{m != n, |E_n - E_m| > tol} Re(M_a[n][m] M_b[m][n]) / (E_n - E_m), n < n_low;
+// skipped[n] = pairs within tol (skipped may be null)
+cudaError_t launch_kp_sums(int nb, int n_low, const double2* M, const double* E, double tol, double* S, int* skipped,
+                           cudaStream_t st);

@@ -177,6 +177,21 @@ __global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::
         int x = t / KT, kk = t % KT;
         vt[t] = kk < kt ? vloc[((size_t)x * n2 + j) * n3 + k0 + kk] : (V)0;
     }
+    // energy sums: per-line FP64 totals, per-thread partials, and the FP32
+    // correction dV = V64 - V of the tile (zero when V is already FP64)
+    using R = typename Real<C>::type;
+    const int TPL = 256 / NL > 1 ? 256 / NL : 1;  // threads per line in the energy pass
+    double* lsum = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(xpl + n1) + 7) & ~static_cast<uintptr_t>(7));
+    R* psum = reinterpret_cast<R*>(lsum + 2 * NL);
+    float* dvt = reinterpret_cast<float*>(psum + 3 * NL * TPL);
+    if constexpr (ENERGY) {
+        for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) {
+            int x = t / KT, kk = t % KT;
+            float d = 0.f;
+            if (a.v64e && kk < kt) d = (float)(a.v64e[((size_t)x * n2 + j) * n3 + k0 + kk] - (double)vt[t]);
+            dvt[t] = d;
+        }
+    }
     __syncthreads();
     for (int t = threadIdx.x; t < nxs; t += blockDim.x) xpl[plane_x[t]] = t;
     __syncthreads();
@@ -189,27 +204,41 @@ __global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::
         fft_lines_io<C, true, WIDE>(ld, XStoreV<C, V>{vo, vt, NL, KT, a.kt_f}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
         __syncthreads();
     } else {
-        // psi(r) unscaled; per line the FP64 sums of V|psi|^2 and |psi|^2, then psi <- V psi
+        // psi(r) unscaled; sums of V|psi|^2 and |psi|^2 per line, then psi <- V psi.
+        // Each of TPL threads per line accumulates a strided slice of x in the
+        // working precision (with the FP64 part of V as dV); the slices are
+        // combined in FP64 in a fixed order.
         fft_lines_io<C, true, WIDE>(ld, SmemLines<C>{vo, 1, NL}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
         __syncthreads();
-        double* sums = reinterpret_cast<double*>(
-            (reinterpret_cast<uintptr_t>(xpl + n1) + 7) & ~static_cast<uintptr_t>(7));
-        for (int L = threadIdx.x; L < NL; L += blockDim.x) {
-            const int kk = L - (L / KT) * KT;
-            double s1 = 0.0, s0 = 0.0;
-            for (int x = 0; x < n1; ++x) {
+        for (int t = threadIdx.x; t < NL * TPL; t += blockDim.x) {
+            const int L = t % NL, part = t / NL, kk = L % KT;
+            R s1 = 0, s1c = 0, s0 = 0;
+            for (int x = part; x < n1; x += TPL) {
                 const C v = vo[x * NL + L];
-                const V w = vt[x * KT + kk];
-                const double wv = a.v64e ? a.v64e[((size_t)x * n2 + j) * n3 + k0 + kk] : (double)w;
-                const double m = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+                const R w = (R)vt[x * KT + kk];
+                const R m = v.x * v.x + v.y * v.y;
                 s0 += m;
-                s1 += wv * m;
-                vo[x * NL + L] = cscale(v, (typename Real<C>::type)w);
+                s1 += w * m;
+                s1c += (R)dvt[x * KT + kk] * m;
+                vo[x * NL + L] = cscale(v, w);
             }
-            sums[2 * L] = s1;
-            sums[2 * L + 1] = s0;
+            psum[3 * t] = s1;
+            psum[3 * t + 1] = s1c;
+            psum[3 * t + 2] = s0;
         }
         __syncthreads();
+        for (int L = threadIdx.x; L < NL; L += blockDim.x) {
+            double s1 = 0.0, s0 = 0.0;
+            for (int part = 0; part < TPL; ++part) {
+                const int t = part * NL + L;
+                s1 += (double)psum[3 * t] + (double)psum[3 * t + 1];
+                s0 += (double)psum[3 * t + 2];
+            }
+            lsum[2 * L] = s1;
+            lsum[2 * L + 1] = s0;
+        }
+        __syncthreads();
+        double* sums = lsum;
         const int nslots = gridDim.x * gridDim.y, slot = blockIdx.y * gridDim.x + blockIdx.x;
         for (int bb = threadIdx.x; bb < nbb; bb += blockDim.x) {
             double s1 = 0.0, s0 = 0.0;
@@ -299,7 +328,12 @@ static size_t xpass_smem(const LocalArgs& a)
 {
     const size_t NL = (size_t)a.kt * a.bb;
     size_t b = sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(V) * (size_t)a.n1 * a.kt + sizeof(int) * a.n1;
-    if (a.epart) b = (b + 7) / 8 * 8 + 2 * sizeof(double) * NL;  // per-line energy sums
+    if (a.epart) {
+        // energy pass: line totals (double), per-thread partials, dV tile
+        const size_t tpl = 256 / NL > 1 ? 256 / NL : 1;
+        b = (b + 7) / 8 * 8 + 2 * sizeof(double) * NL + 3 * sizeof(typename Real<C>::type) * NL * tpl +
+            sizeof(float) * (size_t)a.n1 * a.kt;
+    }
     return b;
 }
 

@@ -344,28 +344,60 @@ __device__ __forceinline__ float block_max(float v, float* red)
     return r;
 }
 
-// Projection A: row p of Pr (complex, length npw) -> [hi|lo][p][kpad] interleaved re/im
+// split of an FP64 value: hi from its FP32 rounding, lo from the FP64 remainder
 template <typename T>
-__global__ void split_rows_kernel(const float2* __restrict__ pr, int npw, size_t ldk, T* hi, T* lo, float* inv_scale,
+__device__ __forceinline__ void split_store_d(double x, T* hi, T* lo);
+template <>
+__device__ __forceinline__ void split_store_d<__half>(double x, __half* hi, __half* lo)
+{
+    __half h = __float2half_rn((float)x);
+    *hi = h;
+    *lo = __float2half_rn((float)(x - (double)__half2float(h)));
+}
+template <>
+__device__ __forceinline__ void split_store_d<__nv_bfloat16>(double x, __nv_bfloat16* hi, __nv_bfloat16* lo)
+{
+    __nv_bfloat16 h = __float2bfloat16_rn((float)x);
+    *hi = h;
+    *lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
+}
+
+__device__ __forceinline__ void split_any(float x, float sc, __half* h, __half* l) { split_store<__half>(x * sc, h, l); }
+__device__ __forceinline__ void split_any(float x, float sc, __nv_bfloat16* h, __nv_bfloat16* l)
+{
+    split_store<__nv_bfloat16>(x * sc, h, l);
+}
+__device__ __forceinline__ void split_any(double x, float sc, __half* h, __half* l) { split_store_d<__half>(x * sc, h, l); }
+__device__ __forceinline__ void split_any(double x, float sc, __nv_bfloat16* h, __nv_bfloat16* l)
+{
+    split_store_d<__nv_bfloat16>(x * sc, h, l);
+}
+
+// Projection A: row p of a complex matrix (complex64 Pr or complex128 psi,
+// length npw) -> [hi|lo][p][kpad] interleaved re/im
+template <typename T, typename S>
+__global__ void split_rows_kernel(const S* __restrict__ pr, int npw, size_t ldk, T* hi, T* lo, float* inv_scale,
                                   bool fp16)
 {
+    using R = typename Real<S>::type;
     __shared__ float red[32];
     const int p = blockIdx.x;
-    const float2* row = pr + (size_t)p * npw;
+    const S* row = pr + (size_t)p * npw;
     float mx = 0.f;
-    for (int g = threadIdx.x; g < npw; g += blockDim.x) mx = fmaxf(mx, fmaxf(fabsf(row[g].x), fabsf(row[g].y)));
+    for (int g = threadIdx.x; g < npw; g += blockDim.x)
+        mx = fmaxf(mx, fmaxf(fabsf((float)row[g].x), fabsf((float)row[g].y)));
     mx = block_max(mx, red);
     const float sc = row_scale(mx, fp16);
     if (threadIdx.x == 0) inv_scale[p] = 1.f / sc;
     T* h = hi + (size_t)p * ldk;
     T* l = lo + (size_t)p * ldk;
     for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
-        float x = 0.f;
+        R x = 0;
         if (k < 2 * (size_t)npw) {
-            float2 v = row[k >> 1];
+            S v = row[k >> 1];
             x = (k & 1) ? v.y : v.x;
         }
-        split_store<T>(x * sc, h + k, l + k);
+        split_any(x, sc, h + k, l + k);
     }
 }
 
@@ -500,7 +532,7 @@ __global__ void zero_rows_kernel(int nb, int nbp, size_t ldk, T* hi, T* lo, floa
 // W[p][b] = lambda_p * sum_z (C[z][p][re b] + i C[z][p][im b])
 template <typename CW>
 __global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float* __restrict__ part,
-                                   const double* __restrict__ lam, int period, CW* W)
+                                   const double* __restrict__ lam, int period, CW* W, double* eterm = nullptr)
 {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)P * nb) return;
@@ -515,6 +547,25 @@ __global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float
     }
     const double f = lam ? lam[p % period] : 1.0;
     W[idx] = from_c128<CW>(make_double2(f * sr, f * si));
+    if (eterm) eterm[idx] = f * (sr * sr + si * si);  // lambda_p |<p|psi_b>|^2, FP64
+}
+
+// out[b] = sum_p eterm[p][b], in p order
+__global__ void __launch_bounds__(256) eterm_sum_kernel(int P, int nb, const double* __restrict__ eterm,
+                                                        double* __restrict__ out)
+{
+    __shared__ double red[32];
+    const int b = blockIdx.x;
+    double e = 0.0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) e += eterm[(size_t)p * nb + b];
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        out[b] = s;
+    }
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -562,10 +613,10 @@ cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, 
 {
     if (P == 0 || npw == 0) return cudaSuccess;
     if (fp16) {
-        split_rows_kernel<__half><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__half*)proj->hi, (__half*)proj->lo,
+        split_rows_kernel<__half, float2><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__half*)proj->hi, (__half*)proj->lo,
                                                      proj->inv_scale, true);
     } else {
-        split_rows_kernel<__nv_bfloat16><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__nv_bfloat16*)proj->hi,
+        split_rows_kernel<__nv_bfloat16, float2><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__nv_bfloat16*)proj->hi,
                                                             (__nv_bfloat16*)proj->lo, proj->inv_scale, false);
     }
     col_max_kernel<<<ceil_div(npw, 256), 256, 0, st>>>(pr, nullptr, P, npw, cmax_scratch);
@@ -586,10 +637,10 @@ cudaError_t tc_build_grad_operands(const float2* pr4, int P, int npw, bool fp16,
     if (P == 0 || npw == 0) return cudaSuccess;
     const int P4 = 4 * P;
     if (fp16)
-        split_rows_kernel<__half><<<P4, 256, 0, st>>>(pr4, npw, proj4->ldk, (__half*)proj4->hi, (__half*)proj4->lo,
+        split_rows_kernel<__half, float2><<<P4, 256, 0, st>>>(pr4, npw, proj4->ldk, (__half*)proj4->hi, (__half*)proj4->lo,
                                                       proj4->inv_scale, true);
     else
-        split_rows_kernel<__nv_bfloat16><<<P4, 256, 0, st>>>(pr4, npw, proj4->ldk, (__nv_bfloat16*)proj4->hi,
+        split_rows_kernel<__nv_bfloat16, float2><<<P4, 256, 0, st>>>(pr4, npw, proj4->ldk, (__nv_bfloat16*)proj4->hi,
                                                              (__nv_bfloat16*)proj4->lo, proj4->inv_scale, false);
     const size_t PN = (size_t)P * npw;
     dim3 g(ceil_div(npw, 32), ceil_div(P, 32));
@@ -704,7 +755,8 @@ static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperan
 }
 
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
-                          const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof)
+                          const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof,
+                          double* eterm, double* e_nl)
 {
     const int N = tc_band_rows(nb);
     TcEpilogue ep{};
@@ -719,46 +771,39 @@ cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb,
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
     h = prof->open(PH_REDUCE, st);
-    proj_reduce_kernel<float2><<<ceil_div((long)P * nb, 256), 256, 0, st>>>(P, nb, N, nz, part, lam, period, W);
+    proj_reduce_kernel<float2><<<ceil_div((long)P * nb, 256), 256, 0, st>>>(P, nb, N, nz, part, lam, period, W,
+                                                                            e_nl ? eterm : nullptr);
+    if (e_nl) eterm_sum_kernel<<<nb, 256, 0, st>>>(P, nb, eterm, e_nl);
     prof->close(h, st);
     return cudaGetLastError();
 }
 
-// out[b] = sum_p lam_p |sum_z (C[z][p][re b] + i C[z][p][im b])|^2 from the projection partials
-__global__ void __launch_bounds__(256) tc_energy_kernel(int P, int N, int nz, const float* __restrict__ part,
-                                                        const double* __restrict__ lam, double* __restrict__ out)
+cudaError_t tc_rows_operand(const double2* x, int rows, int npw, bool fp16, TcOperand* A, cudaStream_t st)
 {
-    __shared__ double red[32];
-    const int b = blockIdx.x, t = b / 128, j = b % 128;
-    const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
-    double e = 0.0;
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        double re = 0.0, im = 0.0;
-        for (int z = 0; z < nz; ++z) {
-            const float* row = part + ((size_t)z * P + p) * N;
-            re += row[cre];
-            im += row[cim];
-        }
-        e += lam[p] * (re * re + im * im);
-    }
-    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-        out[b] = s;
-    }
+    if (rows == 0) return cudaSuccess;
+    if (fp16)
+        split_rows_kernel<__half, double2><<<rows, 256, 0, st>>>(x, npw, A->ldk, (__half*)A->hi, (__half*)A->lo,
+                                                                 A->inv_scale, true);
+    else
+        split_rows_kernel<__nv_bfloat16, double2><<<rows, 256, 0, st>>>(x, npw, A->ldk, (__nv_bfloat16*)A->hi,
+                                                                        (__nv_bfloat16*)A->lo, A->inv_scale, false);
+    return cudaGetLastError();
 }
 
-cudaError_t tc_proj_energy(const TcOperand& A, int P, int nb, int nsplit, const float* part, const double* lam,
-                           double* out, cudaStream_t st)
+cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
+                         double2* out, int* err, cudaStream_t st)
 {
-    if (nb == 0) return cudaSuccess;
+    const int N = tc_band_rows(nb);
+    TcEpilogue ep{};
+    ep.part = part;
+    ep.sa_scale = A.inv_scale;
+    ep.sb_scale = B.inv_scale;
+    cudaError_t e = launch_tc(0, A, M, B, N, nsplit, fp16, ep, err, st);
+    if (e) return e;
     const int ktiles = (int)(A.ldk / BK);
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
-    tc_energy_kernel<<<nb, 256, 0, st>>>(P, tc_band_rows(nb), nz, part, lam, out);
+    proj_reduce_kernel<double2><<<ceil_div((long)M * nb, 256), 256, 0, st>>>(M, nb, N, nz, part, nullptr, 1, out);
     return cudaGetLastError();
 }
 

@@ -40,12 +40,16 @@ cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOp
                             cudaStream_t st);
 // Band operand of the expansion from W (complex64 [P][nb]).
 cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, unsigned* rowmax, cudaStream_t st);
-// W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null)
+// W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null); with e_nl also
+// e_nl[b] = sum_p lambda_p |<p|psi_b>|^2 in FP64 (eterm: P*nb doubles of scratch)
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
-                          const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof);
-// out[b] = sum_p lam_p |<p|psi_b>|^2 in FP64 from the partials of a tc_projection
-cudaError_t tc_proj_energy(const TcOperand& A, int P, int nb, int nsplit, const float* part, const double* lam,
-                           double* out, cudaStream_t st);
+                          const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof,
+                          double* eterm = nullptr, double* e_nl = nullptr);
+// Row operand [rows][2npw] of a complex128 matrix (psi), for conj(A) B^T GEMMs
+cudaError_t tc_rows_operand(const double2* x, int rows, int npw, bool fp16, TcOperand* A, cudaStream_t st);
+// out[m][n] = sum_G conj(A[m][G]) B[n][G] in complex128 (B a band operand of nb rows)
+cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
+                         double2* out, int* err, cudaStream_t st);
 // hpsi[b][G] += sum_p W[p][b] Pr[p][G]
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
                          cudaStream_t st, Prof* prof);

@@ -253,3 +253,24 @@ class GradientCallable:
 
     def __call__(self, psi, out: GradHPsi, n_bands: int = 1):
         self._h.grad_apply(self._kid, int(n_bands), psi, out, self._prec)
+
+
+def kp_sums(m, e, n_low: int, deg_tol: float = 1e-8):
+    """FP64 k·p sums s[n][a][b] = sum_{m != n, |e_n - e_m| > deg_tol} Re(M_a[n][m] M_b[m][n]) / (e_n - e_m)
+    for the lowest n_low bands, from a velocity matrix m [3, nb, nb] and energies e [nb] (numpy host
+    arrays or CUDA torch tensors).  Returns (s [n_low, 3, 3], skipped [n_low])."""
+    L = load()
+    nb = int(e.shape[0])
+    if _is_torch(m):
+        import torch
+        s = torch.zeros((n_low, 3, 3), dtype=torch.float64, device=m.device)
+        k = torch.zeros(n_low, dtype=torch.int32, device=m.device)
+        check(L.hpsi_kp_sums(nb, n_low, m.data_ptr(), e.data_ptr(), deg_tol, s.data_ptr(), k.data_ptr(),
+                             abi.HPSI_DEVICE_PTRS | abi.HPSI_SYNC, None))
+        return s, k
+    m = np.ascontiguousarray(m, dtype=np.complex128)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    s = np.zeros((n_low, 3, 3), dtype=np.float64)
+    k = np.zeros(n_low, dtype=np.int32)
+    check(L.hpsi_kp_sums(nb, n_low, m.ctypes.data, e.ctypes.data, deg_tol, s.ctypes.data, k.ctypes.data, 0, None))
+    return s, k

@@ -125,12 +125,27 @@ int hpsi_dim(const hpsi_ctx* ctx, int kid);
 int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
                int flags, void* stream);
 
+/* k·p sums of second-order perturbation theory, FP64, for the lowest n_low bands:
+ *   s[n][a][b] = sum_{m != n, |e_n - e_m| > deg_tol} Re(m_a[n][m] m_b[m][n]) / (e_n - e_m)
+ * from a velocity matrix m ([3][nb][nb] complex, hpsi_velocity_matrix's layout)
+ * and band energies e[nb] (Ha).  Without a nonlocal second derivative the
+ * inverse effective-mass tensor of band n is delta_ab + 2 s[n][a][b].  Pairs
+ * within deg_tol are left out and counted in n_skipped[n] (may be NULL).
+ * s: [n_low][3][3] doubles.  m, e, s, n_skipped: device memory with
+ * HPSI_DEVICE_PTRS, else host memory (the call then allocates a staging
+ * buffer and synchronises).  No counterpart in the reference. */
+int hpsi_kp_sums(int nb, int n_low, const double* m, const double* e, double deg_tol, double* s,
+                 int* n_skipped, int flags, void* stream);
+
 /* hpsi += H psi (as hpsi_apply) and e[b] = <psi_b|H|psi_b> (Ha) with FP64
  * reductions on the device: kinetic energy summed in FP64; local energy
  * (1/N) sum_r V|psi_b(r)|^2 from the G->r transform of the call, divided by
  * that transform's own Parseval norm sum_r |psi_b(r)|^2 / (N sum_G |psi_b|^2),
  * which cancels the gain error of the complex64 FFTs; nonlocal energy
- * sum_p lambda_p |<p|psi_b>|^2 from the projection's partial sums.  When two
+ * sum_p lambda_p |<p|psi_b>|^2 from the projection's split sums in FP64 (the
+ * tensor-core projection then keeps its FP32 accumulation chains in TMEM to
+ * 16 k-tiles of 64, so hpsi differs from hpsi_apply's within the path's
+ * tolerance; FP64 and FP32 hpsi are bit-identical to hpsi_apply's).  When two
  * G-vectors of the k-point share a grid point the Rayleigh quotient of the
  * computed hpsi is returned instead.  e: nb doubles (device memory with
  * HPSI_DEVICE_PTRS).  The reference forms these Rayleigh quotients on the host
@@ -144,7 +159,10 @@ int hpsi_grad_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi,
                     double* dx, double* dy, double* dz, int flags, void* stream);
 
 /* m[a][m][n] = <psi_m| dH/dk_a |psi_n>, a = x,y,z, complex, overwritten (not accumulated).
- * Output layout [3][nb][nb] complex<double>; psi as in hpsi_apply. */
+ * Output layout [3][nb][nb] complex<double>; psi as in hpsi_apply.  With the
+ * tensor-core precisions the band-pair GEMMs psi^H (dH_a psi) also run on the
+ * tensor cores, for both in the scaled split-FP16 form (FP32 accumulation in
+ * short chains, FP64 split-K sums). */
 int hpsi_velocity_matrix(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* m,
                          int flags, void* stream);
 
