@@ -287,7 +287,15 @@ def run_gb300(args, rank, world, local):
         ach = work / (tms * 1e-3) / 1e12
         roof = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "peak_source": src + " dense bf16 tensor peak"}
-    roof["traffic"] = None
+    # DRAM bytes (read + write) of one launch from the ncu capture summarised in
+    # profiles/ncu_full_fft_tc_sc64_nb32.md (same kernel, 32 bands per launch,
+    # which is also the x pass's per-launch band chunk here)
+    ncu_traffic = {"x_pass": 58.6e6}
+    roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec != "fp64") else None
+    if roof["traffic"] is not None and bound == "hbm":
+        roof["algorithmic_bytes_per_launch"] = alg[dom][1] / prof[dom][1]
+        roof["traffic_note"] = "ncu dram__bytes_read+write of one launch; below the algorithmic bytes because " \
+                               "the launch's writes are still in the 129 MB L2 when it ends"
     # the tensor-core projection GEMM, reported beside the dominant phase
     roof_gemm = None
     if prof["proj_gemm"][1]:
