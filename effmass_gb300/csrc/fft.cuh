@@ -292,6 +292,70 @@ HPSI_D void fft_stage_io_p(int p, const LD& ld, const ST& st, int n, const FastD
     }
 }
 
+// ---- compile-time two-stage transforms --------------------------------------
+// For the grid lengths of the common cells (72 = 8*9, 36 = 9*4, 24 = 8*3,
+// 64 = 8*8) the stage shapes are template constants: the per-element index
+// arithmetic (butterfly -> group and offset, twiddle index, output position)
+// folds into constant multiplies and shifts instead of runtime divisions.
+// The radix order is the one fft_factor picks: the same arithmetic as the
+// runtime-plan path.
+template <int R0, int R1>
+struct FftPlan2 {
+    static constexpr int r0 = R0, r1 = R1, n = R0 * R1;
+};
+
+template <typename C, int N, int P, int NS, typename LD, typename ST>
+HPSI_D void fft_stage_ct(const LD& ld, const ST& st, const FastDiv& nlf, const C* tw, int sign)
+{
+    constexpr int nbf = N / P;
+    constexpr int tstep = N / (NS * P);
+    const int nl = (int)nlf.d;
+    const int total = nl * nbf;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int i = (int)fdiv((uint32_t)t, nlf);  // lines walked fastest
+        const int L = t - i * nl;
+        const int hi = i / NS;
+        const int k = i - hi * NS;
+        C v[HPSI_FFT_MAXR];
+#pragma unroll
+        for (int q = 0; q < P; ++q) v[q] = ld(L, i + q * nbf);
+        if (NS > 1 && k > 0) {
+#pragma unroll
+            for (int q = 1; q < P; ++q) v[q] = cmul(v[q], tw_get(tw, q * k * tstep, sign));
+        }
+        dft_small<C, P>(v, tw, N, sign);
+        const int base = hi * NS * P + k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) st(L, base + q * NS, v[q]);
+    }
+}
+
+// Two-stage transform of nl lines: stage 0 reads through ld and writes bufA
+// (line stride ls, element stride es), stage 1 reads bufA and writes through
+// st (the same buffer contract as fft_lines_io with nst == 2: the last stage
+// reads bufA).
+template <typename C, typename PL, typename LD, typename ST>
+HPSI_D void fft_lines_ct(const LD& ld, const ST& st, C* bufA, const FastDiv& nlf, int ls, int es, const C* tw,
+                         int sign)
+{
+    const SmemLines<C> A{bufA, ls, es};
+    fft_stage_ct<C, PL::n, PL::r0, 1>(ld, A, nlf, tw, sign);
+    __syncthreads();
+    fft_stage_ct<C, PL::n, PL::r1, PL::r0>(A, st, nlf, tw, sign);
+}
+
+// Plan ids the host selects (0 = runtime plan)
+enum { FFT_CT_NONE = 0, FFT_CT_72 = 1, FFT_CT_36 = 2, FFT_CT_24 = 3, FFT_CT_64 = 4 };
+static inline int fft_ct_id(const FftLen& L)
+{
+    if (L.nst != 2) return FFT_CT_NONE;
+    if (L.rad[0] == 8 && L.rad[1] == 9) return FFT_CT_72;
+    if (L.rad[0] == 9 && L.rad[1] == 4) return FFT_CT_36;
+    if (L.rad[0] == 8 && L.rad[1] == 3) return FFT_CT_24;
+    if (L.rad[0] == 8 && L.rad[1] == 8) return FFT_CT_64;
+    return FFT_CT_NONE;
+}
+
 // Which buffer the last stage of fft_lines_io reads: 0 = ld, 1 = bufA, 2 = bufB.
 HPSI_HD int fft_last_read(const FftLen& L) { return L.nst <= 1 ? 0 : (((L.nst - 2) % 2 == 0) ? 1 : 2); }
 

@@ -17,6 +17,8 @@
 //                   the sphere points: hpsi += kinetic*psi + grid/N.
 // T is sized for a chunk of bands so that it stays resident in L2 between
 // the passes.  Kinetic energy is fused into pass C.
+#include <type_traits>
+
 #include "fft.cuh"
 #include "kernels.cuh"
 
@@ -26,6 +28,17 @@
 template <typename C> struct Cfg;
 template <> struct Cfg<float2> { static constexpr int plane_threads = 512, plane_min = 2, x_min = 4; };
 template <> struct Cfg<double2> { static constexpr int plane_threads = 256, plane_min = 1, x_min = 1; };
+
+// Transform of a kernel's lines: the runtime plan (NoPlan) or a compile-time
+// two-stage plan (FftPlan2) chosen by the host for common grid lengths.
+struct NoPlan {};
+template <typename C, bool WIDE, typename PL, typename LD, typename ST>
+HPSI_D void lines(const LD& ld, const ST& st, C* bufA, C* bufB, const FftLen& L, const FastDiv& nlf, int ls, int es,
+                  const C* tw, int sign)
+{
+    if constexpr (std::is_same<PL, NoPlan>::value) fft_lines_io<C, true, WIDE>(ld, st, bufA, bufB, L, nlf, ls, es, tw, sign);
+    else fft_lines_ct<C, PL>(ld, st, bufA, nlf, ls, es, tw, sign);
+}
 
 // Shared-memory planes use a padded row stride n3p = n3 + 1 (odd) so that
 // both the z-lines (rows) and the y-lines (columns) are read and written by
@@ -43,7 +56,7 @@ struct PlaneGlobal {
     HPSI_D void operator()(int L, int e, C v) const { p[e * n3 + L] = v; }
 };
 
-template <typename C, bool WIDE>
+template <typename C, bool WIDE, typename PL>
 __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
@@ -84,12 +97,12 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     // z (rows of b0): intermediates in b1 then b0; output to the buffer the last stage does not read
     const int rz = fft_last_read(a.Lz);
     C* zo = (rz == 1) ? b0 : b1;
-    fft_lines_io<C, true, WIDE>(SmemLines<C>{b0, n3p, 1}, SmemLines<C>{zo, n3p, 1}, b1, b0, a.Lz, a.nl_z, n3p, 1,
+    lines<C, WIDE, PL>(SmemLines<C>{b0, n3p, 1}, SmemLines<C>{zo, n3p, 1}, b1, b0, a.Lz, a.nl_z, n3p, 1,
                                 twz, +1);
     __syncthreads();
     // y (columns), last stage straight to T
     C* zother = (zo == b0) ? b1 : b0;
-    fft_lines_io<C, true, WIDE>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{T + ((size_t)b * nxs + p) * n23, n3},
+    lines<C, WIDE, PL>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{T + ((size_t)b * nxs + p) * n23, n3},
                                 zother, zo, a.Ly, a.nl_y, 1, n3p, twy, +1);
 }
 
@@ -98,7 +111,15 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
 // is loaded once per block.  The G->r transform reads the sphere planes of T
 // directly (zero for other x) and multiplies by V as it stores; the r->G
 // transform stores the sphere planes back into T.
-template <typename C>
+// line L -> (band in block, z-value): KTC > 0 is a compile-time KT
+template <int KTC>
+HPSI_D int line_band(int L, const FastDiv& ktf)
+{
+    if constexpr (KTC > 0) return L / KTC;
+    else return (int)fdiv((uint32_t)L, ktf);
+}
+
+template <typename C, int KTC>
 struct XLoad {
     const C* T;
     const int* xpl;      // smem: plane index of x or -1
@@ -108,14 +129,14 @@ struct XLoad {
     FastDiv ktf;
     HPSI_D C operator()(int L, int x) const
     {
-        const int bb = (int)fdiv((uint32_t)L, ktf), kk = L - bb * KT;
+        const int bb = line_band<KTC>(L, ktf), kk = L - bb * (KTC > 0 ? KTC : KT);
         const int pl = xpl[x];
         if (pl < 0 || bb >= nbb || kk >= kt) return cmake<C>(0, 0);
         return T[((size_t)(bb0 + bb) * nxs + pl) * plane + base + kk];
     }
 };
 
-template <typename C, typename V>
+template <typename C, typename V, int KTC>
 struct XStoreV {
     C* buf;
     const V* vt;         // smem V tile [x*KT + kk]
@@ -123,12 +144,12 @@ struct XStoreV {
     FastDiv ktf;
     HPSI_D void operator()(int L, int x, C v) const
     {
-        const int bb = (int)fdiv((uint32_t)L, ktf), kk = L - bb * KT;
+        const int bb = line_band<KTC>(L, ktf), kk = L - bb * (KTC > 0 ? KTC : KT);
         buf[x * NL + L] = cscale(v, (typename Real<C>::type)vt[x * KT + kk]);
     }
 };
 
-template <typename C>
+template <typename C, int KTC>
 struct XStore {
     C* T;
     const int* xpl;
@@ -137,14 +158,14 @@ struct XStore {
     FastDiv ktf;
     HPSI_D void operator()(int L, int x, C v) const
     {
-        const int bb = (int)fdiv((uint32_t)L, ktf), kk = L - bb * KT;
+        const int bb = line_band<KTC>(L, ktf), kk = L - bb * (KTC > 0 ? KTC : KT);
         const int pl = xpl[x];
         if (pl < 0 || bb >= nbb || kk >= kt) return;
         T[((size_t)(bb0 + bb) * nxs + pl) * plane + base + kk] = v;
     }
 };
 
-template <typename C, typename V, bool WIDE, bool ENERGY>
+template <typename C, typename V, bool WIDE, bool ENERGY, typename PL, int KTC>
 __global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::x_min) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
                                               const C* __restrict__ tw_x_g)
 {
@@ -196,19 +217,19 @@ __global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::
     for (int t = threadIdx.x; t < nxs; t += blockDim.x) xpl[plane_x[t]] = t;
     __syncthreads();
     const size_t base = (size_t)j * n3 + k0;
-    const XLoad<C> ld{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
+    const XLoad<C, KTC> ld{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
     // G->r, times V, into the buffer the last stage does not read
     const int r = fft_last_read(a.Lx);
     C* vo = (r == 1) ? b1 : b0;
     if constexpr (!ENERGY) {
-        fft_lines_io<C, true, WIDE>(ld, XStoreV<C, V>{vo, vt, NL, KT, a.kt_f}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
+        lines<C, WIDE, PL>(ld, XStoreV<C, V, KTC>{vo, vt, NL, KT, a.kt_f}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
         __syncthreads();
     } else {
         // psi(r) unscaled; sums of V|psi|^2 and |psi|^2 per line, then psi <- V psi.
         // Each of TPL threads per line accumulates a strided slice of x in the
         // working precision (with the FP64 part of V as dV); the slices are
         // combined in FP64 in a fixed order.
-        fft_lines_io<C, true, WIDE>(ld, SmemLines<C>{vo, 1, NL}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
+        lines<C, WIDE, PL>(ld, SmemLines<C>{vo, 1, NL}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
         __syncthreads();
         for (int t = threadIdx.x; t < NL * TPL; t += blockDim.x) {
             const int L = t % NL, part = t / NL, kk = L % KT;
@@ -254,11 +275,11 @@ __global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::
     }
     // r->G, back into the sphere planes of T
     C* vother = (vo == b0) ? b1 : b0;
-    const XStore<C> stT{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
-    fft_lines_io<C, true, WIDE>(SmemLines<C>{vo, 1, NL}, stT, vother, vo, a.Lx, a.nl_x, 1, NL, twx, -1);
+    const XStore<C, KTC> stT{T, xpl, plane, base, nxs, KT, kt, nbb, bb0, a.kt_f};
+    lines<C, WIDE, PL>(SmemLines<C>{vo, 1, NL}, stT, vother, vo, a.Lx, a.nl_x, 1, NL, twx, -1);
 }
 
-template <typename C, bool WIDE>
+template <typename C, bool WIDE, typename PL>
 __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
                                                   double2* __restrict__ hpsi, const double* __restrict__ kinetic,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
@@ -288,7 +309,7 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     // y (columns) straight from T; output into the buffer the last stage does not read
     const int ry = fft_last_read(a.Ly);
     C* yo = (ry == 1) ? b1 : b0;
-    fft_lines_io<C, true, WIDE>(PlaneGlobal<C>{const_cast<C*>(T) + ((size_t)b * nxs + p) * n23, n3},
+    lines<C, WIDE, PL>(PlaneGlobal<C>{const_cast<C*>(T) + ((size_t)b * nxs + p) * n23, n3},
                                 SmemLines<C>{yo, 1, n3p}, b0, b1, a.Ly, a.nl_y, 1, n3p, twy, -1);
     __syncthreads();
     // z (rows)
@@ -296,7 +317,7 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     const int rz = fft_last_read(a.Lz);
     // intermediates: bufA = yother, bufB = yo; last stage reads yo (rz == 2) or yother (rz == 1) or yo via ld (rz == 0)
     C* zo = (rz == 1) ? yo : yother;
-    fft_lines_io<C, true, WIDE>(SmemLines<C>{yo, n3p, 1}, SmemLines<C>{zo, n3p, 1}, yother, yo, a.Lz, a.nl_z, n3p, 1,
+    lines<C, WIDE, PL>(SmemLines<C>{yo, n3p, 1}, SmemLines<C>{zo, n3p, 1}, yother, yo, a.Lz, a.nl_z, n3p, 1,
                                 twz, -1);
     __syncthreads();
     const C* res = zo;
@@ -364,54 +385,88 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
     a->kt_f = make_fastdiv((uint32_t)a->kt);
 }
 
-template <typename C, typename V, bool WIDE>
+template <typename C, typename V, bool WIDE, typename PL, int KTC>
 static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic,
                                   C* T, const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st,
                                   Prof* prof)
 {
     const size_t sp = plane_smem<C>(a), sx = xpass_smem<C, V>(a);
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(g2r_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(r2g_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
-        return e;
-    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
-        return e;
+    auto g2r = g2r_planes<C, WIDE, PL>;
+    auto r2g = r2g_planes<C, WIDE, PL>;
+    auto xp = a.epart ? x_pass<C, V, WIDE, true, PL, KTC> : x_pass<C, V, WIDE, false, PL, KTC>;
+    if ((e = cudaFuncSetAttribute(g2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(r2g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(xp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
     dim3 gp(a.nxs, nb);
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     int h = prof->open(PH_G2R, st);
-    g2r_planes<C, WIDE><<<gp, pt, sp, st>>>(a, psi, T, twy, twz);
+    g2r<<<gp, pt, sp, st>>>(a, psi, T, twy, twz);
     prof->close(h, st);
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
-    if (a.epart) x_pass<C, V, WIDE, true><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
-    else x_pass<C, V, WIDE, false><<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    xp<<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
     prof->close(h, st);
     h = prof->open(PH_R2G, st);
-    r2g_planes<C, WIDE><<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
+    r2g<<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
     prof->close(h, st);
     return cudaGetLastError();
 }
 
-template <typename C, typename V, bool WIDE>
+template <typename C, typename V, bool WIDE, typename PL, int KTC>
 static cudaError_t launch_local_batch_t(const LocalArgs& a, int nbands, int max_nxs, int nxblk, C* T, const V* vloc,
                                         const C* twx, const C* twy, const C* twz, cudaStream_t st)
 {
     const size_t sp = plane_smem<C>(a), sx = xpass_smem<C, V>(a);
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(g2r_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(r2g_planes<C, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
-    if ((e = cudaFuncSetAttribute(x_pass<C, V, WIDE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
-        return e;
+    auto g2r = g2r_planes<C, WIDE, PL>;
+    auto r2g = r2g_planes<C, WIDE, PL>;
+    auto xp = x_pass<C, V, WIDE, false, PL, KTC>;
+    if ((e = cudaFuncSetAttribute(g2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(r2g, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(xp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
     if (max_nxs == 0 || nbands == 0 || nxblk == 0) return cudaSuccess;
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     dim3 gp(max_nxs, nbands);
-    g2r_planes<C, WIDE><<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
+    g2r<<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, nxblk);
-    x_pass<C, V, WIDE, false><<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
-    r2g_planes<C, WIDE><<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
+    xp<<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
+    r2g<<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
     return cudaGetLastError();
+}
+
+// Kernel set of a launch: the wide-radix set, a compile-time two-stage plan
+// (complex64, the same plan on all three axes; with KT = 8 also a
+// compile-time z-tile in the x pass), or the runtime-plan set.
+template <int K> using IntC = std::integral_constant<int, K>;
+template <typename C, typename F>
+static cudaError_t with_kernels(const LocalArgs& a, F&& f)
+{
+    if (fft_needs_wide(a.Lx) || fft_needs_wide(a.Ly) || fft_needs_wide(a.Lz))
+        return f(std::true_type{}, NoPlan{}, IntC<0>{});
+    if constexpr (std::is_same<C, float2>::value) {
+        const int id = fft_ct_id(a.Lx);
+        if (id != FFT_CT_NONE && fft_ct_id(a.Ly) == id && fft_ct_id(a.Lz) == id) {
+            const bool k8 = a.kt == 8;
+            switch (id) {
+                case FFT_CT_72:
+                    return k8 ? f(std::false_type{}, FftPlan2<8, 9>{}, IntC<8>{})
+                              : f(std::false_type{}, FftPlan2<8, 9>{}, IntC<0>{});
+                case FFT_CT_36:
+                    return k8 ? f(std::false_type{}, FftPlan2<9, 4>{}, IntC<8>{})
+                              : f(std::false_type{}, FftPlan2<9, 4>{}, IntC<0>{});
+                case FFT_CT_24:
+                    return k8 ? f(std::false_type{}, FftPlan2<8, 3>{}, IntC<8>{})
+                              : f(std::false_type{}, FftPlan2<8, 3>{}, IntC<0>{});
+                case FFT_CT_64:
+                    return k8 ? f(std::false_type{}, FftPlan2<8, 8>{}, IntC<8>{})
+                              : f(std::false_type{}, FftPlan2<8, 8>{}, IntC<0>{});
+                default: break;
+            }
+        }
+    }
+    return f(std::false_type{}, NoPlan{}, IntC<0>{});
 }
 
 template <typename C, typename V>
@@ -420,9 +475,10 @@ cudaError_t launch_local_batch(const LocalArgs& a, int nbands, int max_nxs, int 
 {
     if (!a.items || a.epart) return cudaErrorInvalidValue;
     if (a.plane_threads > Cfg<C>::plane_threads || a.plane_threads % 32) return cudaErrorInvalidValue;
-    const bool wide = fft_needs_wide(a.Lx) || fft_needs_wide(a.Ly) || fft_needs_wide(a.Lz);
-    if (wide) return launch_local_batch_t<C, V, true>(a, nbands, max_nxs, nxblk, T, vloc, twx, twy, twz, st);
-    return launch_local_batch_t<C, V, false>(a, nbands, max_nxs, nxblk, T, vloc, twx, twy, twz, st);
+    return with_kernels<C>(a, [&](auto wide, auto pl, auto ktc) {
+        return launch_local_batch_t<C, V, decltype(wide)::value, decltype(pl), decltype(ktc)::value>(
+            a, nbands, max_nxs, nxblk, T, vloc, twx, twy, twz, st);
+    });
 }
 
 size_t local_xpass_smem(const LocalArgs& a, bool fp64)
@@ -434,9 +490,10 @@ template <typename C, typename V>
 cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
                          const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof)
 {
-    const bool wide = fft_needs_wide(a.Lx) || fft_needs_wide(a.Ly) || fft_needs_wide(a.Lz);
-    if (wide) return launch_local_t<C, V, true>(a, nb, psi, hpsi, kinetic, T, vloc, twx, twy, twz, st, prof);
-    return launch_local_t<C, V, false>(a, nb, psi, hpsi, kinetic, T, vloc, twx, twy, twz, st, prof);
+    return with_kernels<C>(a, [&](auto wide, auto pl, auto ktc) {
+        return launch_local_t<C, V, decltype(wide)::value, decltype(pl), decltype(ktc)::value>(
+            a, nb, psi, hpsi, kinetic, T, vloc, twx, twy, twz, st, prof);
+    });
 }
 
 template cudaError_t launch_local<double2, double>(const LocalArgs&, int, const double2*, double2*, const double*,
