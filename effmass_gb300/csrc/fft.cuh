@@ -304,15 +304,24 @@ struct FftPlan2 {
     static constexpr int r0 = R0, r1 = R1, n = R0 * R1;
 };
 
-template <typename C, int N, int P, int NS, typename LD, typename ST>
+// Line accessor with compile-time strides: element e of line L at b[L*LS + e*ES]
+template <typename C, int LS, int ES>
+struct SmemLinesC {
+    C* b;
+    HPSI_D C operator()(int L, int e) const { return b[L * LS + e * ES]; }
+    HPSI_D void operator()(int L, int e, C v) const { b[L * LS + e * ES] = v; }
+};
+
+// NLC > 0: the number of lines is the compile-time NLC, else nlf.d
+template <typename C, int N, int P, int NS, int NLC, typename LD, typename ST>
 HPSI_D void fft_stage_ct(const LD& ld, const ST& st, const FastDiv& nlf, const C* tw, int sign)
 {
     constexpr int nbf = N / P;
     constexpr int tstep = N / (NS * P);
-    const int nl = (int)nlf.d;
+    const int nl = NLC > 0 ? NLC : (int)nlf.d;
     const int total = nl * nbf;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int i = (int)fdiv((uint32_t)t, nlf);  // lines walked fastest
+        const int i = NLC > 0 ? t / NLC : (int)fdiv((uint32_t)t, nlf);  // lines walked fastest
         const int L = t - i * nl;
         const int hi = i / NS;
         const int k = i - hi * NS;
@@ -339,9 +348,20 @@ HPSI_D void fft_lines_ct(const LD& ld, const ST& st, C* bufA, const FastDiv& nlf
                          int sign)
 {
     const SmemLines<C> A{bufA, ls, es};
-    fft_stage_ct<C, PL::n, PL::r0, 1>(ld, A, nlf, tw, sign);
+    fft_stage_ct<C, PL::n, PL::r0, 1, 0>(ld, A, nlf, tw, sign);
     __syncthreads();
-    fft_stage_ct<C, PL::n, PL::r1, PL::r0>(A, st, nlf, tw, sign);
+    fft_stage_ct<C, PL::n, PL::r1, PL::r0, 0>(A, st, nlf, tw, sign);
+}
+
+// The same with a compile-time line count NLC and intermediate accessor A
+// (constant strides): no runtime index arithmetic left but the loop.
+template <typename C, typename PL, int NLC, typename AB, typename LD, typename ST>
+HPSI_D void fft_lines_cc(const LD& ld, const ST& st, const AB& A, const C* tw, int sign)
+{
+    const FastDiv unused{};
+    fft_stage_ct<C, PL::n, PL::r0, 1, NLC>(ld, A, unused, tw, sign);
+    __syncthreads();
+    fft_stage_ct<C, PL::n, PL::r1, PL::r0, NLC>(A, st, unused, tw, sign);
 }
 
 // Plan ids the host selects (0 = runtime plan)

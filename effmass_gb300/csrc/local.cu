@@ -56,12 +56,29 @@ struct PlaneGlobal {
     HPSI_D void operator()(int L, int e, C v) const { p[e * n3 + L] = v; }
 };
 
+// global plane of T as y-lines with a compile-time row length N3
+template <typename C, int N3>
+struct PlaneGlobalC {
+    C* p;
+    HPSI_D C operator()(int L, int e) const { return p[e * N3 + L]; }
+    HPSI_D void operator()(int L, int e, C v) const { p[e * N3 + L] = v; }
+};
+
+// grid length of an axis: the compile-time plan's when there is one (then all
+// three axes share it), else the runtime value
+template <typename PL>
+HPSI_D int plan_n(int runtime)
+{
+    if constexpr (std::is_same<PL, NoPlan>::value) return runtime;
+    else return PL::n;
+}
+
 template <typename C, bool WIDE, typename PL>
 __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n2 = a.n2, n3 = a.n3, n3p = n3 + 1, n23 = n2 * n3, n23p = n2 * n3p;
+    const int n2 = plan_n<PL>(a.n2), n3 = plan_n<PL>(a.n3), n3p = n3 + 1, n23 = n2 * n3, n23p = n2 * n3p;
     C* b0 = reinterpret_cast<C*>(smem_raw);
     C* b1 = b0 + n23p;
     C* twy = b1 + n23p;
@@ -97,13 +114,22 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     // z (rows of b0): intermediates in b1 then b0; output to the buffer the last stage does not read
     const int rz = fft_last_read(a.Lz);
     C* zo = (rz == 1) ? b0 : b1;
-    lines<C, WIDE, PL>(SmemLines<C>{b0, n3p, 1}, SmemLines<C>{zo, n3p, 1}, b1, b0, a.Lz, a.nl_z, n3p, 1,
-                                twz, +1);
-    __syncthreads();
-    // y (columns), last stage straight to T
     C* zother = (zo == b0) ? b1 : b0;
-    lines<C, WIDE, PL>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{T + ((size_t)b * nxs + p) * n23, n3},
-                                zother, zo, a.Ly, a.nl_y, 1, n3p, twy, +1);
+    C* Tp = T + ((size_t)b * nxs + p) * n23;
+    if constexpr (std::is_same<PL, NoPlan>::value) {
+        lines<C, WIDE, PL>(SmemLines<C>{b0, n3p, 1}, SmemLines<C>{zo, n3p, 1}, b1, b0, a.Lz, a.nl_z, n3p, 1, twz,
+                           +1);
+        __syncthreads();
+        // y (columns), last stage straight to T
+        lines<C, WIDE, PL>(SmemLines<C>{zo, 1, n3p}, PlaneGlobal<C>{Tp, n3}, zother, zo, a.Ly, a.nl_y, 1, n3p, twy,
+                           +1);
+    } else {
+        constexpr int N = PL::n, NP = PL::n + 1;  // n2 = n3 = N lines per axis
+        fft_lines_cc<C, PL, N>(SmemLinesC<C, NP, 1>{b0}, SmemLinesC<C, NP, 1>{zo}, SmemLinesC<C, NP, 1>{b1}, twz, +1);
+        __syncthreads();
+        fft_lines_cc<C, PL, N>(SmemLinesC<C, 1, NP>{zo}, PlaneGlobalC<C, N>{Tp}, SmemLinesC<C, 1, NP>{zother}, twy,
+                               +1);
+    }
 }
 
 // x pass: a block owns the x-lines of (j, k0..k0+KT) for BB consecutive bands
@@ -285,7 +311,7 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n2 = a.n2, n3 = a.n3, n3p = n3 + 1, n23 = n2 * n3, n23p = n2 * n3p;
+    const int n2 = plan_n<PL>(a.n2), n3 = plan_n<PL>(a.n3), n3p = n3 + 1, n23 = n2 * n3, n23p = n2 * n3p;
     C* b0 = reinterpret_cast<C*>(smem_raw);
     C* b1 = b0 + n23p;
     C* twy = b1 + n23p;
@@ -309,16 +335,23 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     // y (columns) straight from T; output into the buffer the last stage does not read
     const int ry = fft_last_read(a.Ly);
     C* yo = (ry == 1) ? b1 : b0;
-    lines<C, WIDE, PL>(PlaneGlobal<C>{const_cast<C*>(T) + ((size_t)b * nxs + p) * n23, n3},
-                                SmemLines<C>{yo, 1, n3p}, b0, b1, a.Ly, a.nl_y, 1, n3p, twy, -1);
-    __syncthreads();
-    // z (rows)
     C* yother = (yo == b0) ? b1 : b0;
     const int rz = fft_last_read(a.Lz);
-    // intermediates: bufA = yother, bufB = yo; last stage reads yo (rz == 2) or yother (rz == 1) or yo via ld (rz == 0)
+    // z intermediates: bufA = yother, bufB = yo; last stage reads yo (rz == 2) or yother (rz == 1) or yo via ld (rz == 0)
     C* zo = (rz == 1) ? yo : yother;
-    lines<C, WIDE, PL>(SmemLines<C>{yo, n3p, 1}, SmemLines<C>{zo, n3p, 1}, yother, yo, a.Lz, a.nl_z, n3p, 1,
-                                twz, -1);
+    C* Tp = const_cast<C*>(T) + ((size_t)b * nxs + p) * n23;
+    if constexpr (std::is_same<PL, NoPlan>::value) {
+        lines<C, WIDE, PL>(PlaneGlobal<C>{Tp, n3}, SmemLines<C>{yo, 1, n3p}, b0, b1, a.Ly, a.nl_y, 1, n3p, twy, -1);
+        __syncthreads();
+        lines<C, WIDE, PL>(SmemLines<C>{yo, n3p, 1}, SmemLines<C>{zo, n3p, 1}, yother, yo, a.Lz, a.nl_z, n3p, 1, twz,
+                           -1);
+    } else {
+        constexpr int N = PL::n, NP = PL::n + 1;
+        fft_lines_cc<C, PL, N>(PlaneGlobalC<C, N>{Tp}, SmemLinesC<C, 1, NP>{yo}, SmemLinesC<C, 1, NP>{b0}, twy, -1);
+        __syncthreads();
+        fft_lines_cc<C, PL, N>(SmemLinesC<C, NP, 1>{yo}, SmemLinesC<C, NP, 1>{zo}, SmemLinesC<C, NP, 1>{yother}, twz,
+                               -1);
+    }
     __syncthreads();
     const C* res = zo;
     const double2* ps = psi + (size_t)b * npw;
