@@ -495,19 +495,19 @@ static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
 }
 
 // Split count of the tensor-core projection.  With band energies the FP32
-// accumulation chains in TMEM are kept to kEnergyChain k-tiles per split (the
+// accumulation chains in TMEM are kept to kEnergyChainK of K per split (the
 // partials are summed in FP64): the tensor cores' FP32 accumulation drifts
 // over long chains, which the band energies would show at the 1e-8 Ha level.
-constexpr int kEnergyChain = 16;
+constexpr int kEnergyChainK = 1024;
 // the band-pair velocity GEMMs (K = 2 npw deep, results compared element-wise)
-// need shorter chains still: 4 k-tiles keep them within 1e-6 of FP64
-constexpr int kVelocityChain = 4;
+// need shorter chains still: 256 of K keeps them within 1e-6 of FP64
+constexpr int kVelocityChainK = 256;
 static int tc_splits(const KSlot& s, int nb, bool energy)
 {
     const size_t k1 = tc_round_k(2 * (size_t)s.npw);
     const int ns = tc_proj_splits(s.P, nb, k1);
     if (!energy) return ns;
-    return std::max(ns, ceil_div((long)(k1 / 64), kEnergyChain));
+    return std::max(ns, tc_chain_splits(k1, kEnergyChainK));
 }
 
 static size_t tc_ws(const KSlot& s, int nb, bool energy = false)
@@ -884,7 +884,7 @@ static VelWs vel_layout(const KSlot& s, int nb, int prec)
         const int NB = tc_band_rows(nb);
         w.k1 = tc_round_k(2 * (size_t)s.npw);
         // short FP32 accumulation chains in TMEM (FP64 sums of the splits)
-        w.ns_tc = std::max(tc_proj_splits(nb, nb, w.k1), ceil_div((long)(w.k1 / 64), kVelocityChain));
+        w.ns_tc = std::max(tc_proj_splits(nb, nb, w.k1), tc_chain_splits(w.k1, kVelocityChainK));
         w.ah = g.take<uint16_t>((size_t)nb * w.k1);
         w.al = g.take<uint16_t>((size_t)nb * w.k1);
         w.as = g.take<float>((size_t)nb);

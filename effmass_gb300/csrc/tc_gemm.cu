@@ -18,7 +18,7 @@
 // significand bits each, so hi+lo represents x to ~2^-22; BF16 pieces to ~2^-18.
 //
 // Kernel: one 128 x 256 output tile per CTA (cta_group::1, UMMA M=128, N=256,
-// K=16), 64-deep K stages loaded by TMA (SWIZZLE_128B) into two pipeline
+// K=16), 32-deep K stages loaded by TMA (SWIZZLE_64B) into four pipeline
 // stages of A_hi, A_lo, B_hi, B_lo; warp 0 issues TMA, warp 1 owns TMEM and
 // issues the MMAs from one thread, warps 2-5 drain TMEM.  Every mbarrier wait
 // is bounded; on timeout the CTA sets an error flag, drains and frees TMEM.
@@ -31,9 +31,10 @@
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
-constexpr int A_TILE = BM * BK * 2;   // bytes of one A piece per stage (16 KB)
-constexpr int B_TILE = BN * BK * 2;   // 32 KB
+constexpr int BM = 128, BN = 256, BK = 32, STAGES = 4;
+constexpr int A_TILE = BM * BK * 2;   // bytes of one A piece per stage (8 KB)
+constexpr int B_TILE = BN * BK * 2;   // 16 KB
+constexpr int MAX_CHAIN_K = 3072;     // K depth of one split (FP32 accumulation chain length)
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr uint32_t TMEM_COLS = 512;  // two 256-column FP32 accumulators, alternating by k-tile
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
@@ -83,17 +84,17 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// SMEM matrix descriptor for a K-major tile written by TMA with SWIZZLE_128B:
-// 8-row x 128-byte swizzle atoms stacked along M/N every 1024 bytes (SBO);
+// SMEM matrix descriptor for a K-major tile written by TMA with SWIZZLE_64B:
+// 8-row x 64-byte swizzle atoms stacked along M/N every 512 bytes (SBO);
 // LBO is not used by swizzled K-major layouts (encoded as 1).
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr)
 {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
     d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)(512 >> 4) << 32;
     d |= (uint64_t)1 << 46;  // descriptor version of sm_100-class tensor cores
-    d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+    d |= (uint64_t)4 << 61;  // SWIZZLE_64B
     return d;
 }
 
@@ -211,8 +212,8 @@ __global__ void __launch_bounds__(192, 1)
             if (!mbar_wait(&sh->full[s], ph)) { atomicExch(err, 2); sh->abort_flag = 1; ok = false; break; }
             tc_fence_after();
             const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
-            const uint64_t ah = sdesc_sw128(st), al = sdesc_sw128(st + A_TILE);
-            const uint64_t bh = sdesc_sw128(st + 2 * A_TILE), bl = sdesc_sw128(st + 2 * A_TILE + B_TILE);
+            const uint64_t ah = sdesc_sw64(st), al = sdesc_sw64(st + A_TILE);
+            const uint64_t bh = sdesc_sw64(st + 2 * A_TILE), bl = sdesc_sw64(st + 2 * A_TILE + B_TILE);
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
                 const uint64_t adv = (uint64_t)((kk * 32) >> 4);  // 16 elements = 32 bytes along K
@@ -597,7 +598,7 @@ bool make_map(CUtensorMap* m, const void* base, size_t rows, size_t ldk, int box
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(m, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
 
@@ -705,21 +706,21 @@ cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B
     return cudaGetLastError();
 }
 
-// Split-K of the projection: at most 48 k-tiles per CTA (short FP32
-// accumulation chains: with the two alternating accumulators at most 24
-// k-tiles, 288 MMAs, add into one accumulator), rounded up so that the CTAs
-// fill whole waves of the 148 SMs the kernel plans for.
+// Split-K of the projection: at most MAX_CHAIN_K of K per CTA (short FP32
+// accumulation chains: with the two alternating accumulators at most half of
+// that, 288 MMAs, add into one accumulator), rounded up so that the CTAs fill
+// whole waves of the 148 SMs the kernel plans for.
 int tc_proj_splits(int P, int nb, size_t ldk)
 {
     const int tiles = ceil_div(P, BM) * (tc_band_rows(nb) / BN);
     const int ktiles = (int)(ldk / BK);
-    int s = ceil_div(ktiles, 48);
+    int s = ceil_div(ktiles, MAX_CHAIN_K / BK);
     if (tiles * s < 148) s = ceil_div(148, tiles);
-    // cost model: waves x k-tiles per split, plus the partial-sum reduction
+    // cost model: waves x K per split (in 64-deep units), plus the partial-sum reduction
     int best = s;
     double best_cost = 1e300;
     for (int c = s; c <= 2 * s && c <= ktiles; ++c) {
-        const double cost = (double)ceil_div(tiles * c, 148) * ceil_div(ktiles, c) + c / 8.0;
+        const double cost = (double)ceil_div(tiles * c, 148) * ceil_div(ktiles, c) * (BK / 64.0) + c / 8.0;
         if (cost < best_cost) { best = c; best_cost = cost; }
     }
     if (best > ktiles) best = ktiles;
@@ -821,4 +822,10 @@ cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb
     cudaError_t e = launch_tc(1, A, npw, B, N, 1, fp16, ep, err, st);
     prof->close(h, st);
     return e;
+}
+
+int tc_chain_splits(size_t ldk, int chain_k)
+{
+    const int kt = (int)(ldk / BK), per = chain_k / BK > 0 ? chain_k / BK : 1;
+    return ceil_div(kt, per);
 }

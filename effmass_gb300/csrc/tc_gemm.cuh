@@ -21,7 +21,8 @@ struct TcEpilogue {
     const float* sb_scale;     // per B row
 };
 
-size_t tc_round_k(size_t k);   // K padded to the 64-deep stage
+size_t tc_round_k(size_t k);   // K padded to the K depth of a pipeline stage
+int tc_chain_splits(size_t ldk, int chain_k);  // splits that keep every split's K depth <= chain_k
 int tc_band_rows(int nb);      // B rows for nb bands (re/im blocks of 128)
 size_t tc_gemm_smem_bytes();
 int tc_proj_splits(int P, int nb, size_t ldk);

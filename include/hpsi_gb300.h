@@ -144,7 +144,7 @@ int hpsi_kp_sums(int nb, int n_low, const double* m, const double* e, double deg
  * which cancels the gain error of the complex64 FFTs; nonlocal energy
  * sum_p lambda_p |<p|psi_b>|^2 from the projection's split sums in FP64 (the
  * tensor-core projection then keeps its FP32 accumulation chains in TMEM to
- * 16 k-tiles of 64, so hpsi differs from hpsi_apply's within the path's
+ * 1024 of K, so hpsi differs from hpsi_apply's within the path's
  * tolerance; FP64 and FP32 hpsi are bit-identical to hpsi_apply's).  When two
  * G-vectors of the k-point share a grid point the Rayleigh quotient of the
  * computed hpsi is returned instead.  e: nb doubles (device memory with
