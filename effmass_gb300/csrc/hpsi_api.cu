@@ -443,6 +443,34 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     return HPSI_OK;
 }
 
+// rho += sum_b occ_b |psi_b(r)|^2 on device pointers (T chunks in ws)
+template <typename C>
+static int density_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, const double* occ, double* rho,
+                         unsigned char* ws, const C* tw, cudaStream_t st)
+{
+    if (nb == 0 || s.npw == 0) return HPSI_OK;
+    const int* pl = s.d_plane;
+    LocalArgs a{};
+    a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
+    a.npw = s.npw;
+    a.nxs = s.nxs;
+    local_xpass_shape(&a, sizeof(C));
+    a.inv_n = 1.0 / ((double)c->n1 * c->n2 * c->n3);
+    a.plane_x = pl;
+    a.plane_off = pl + s.nxs;
+    a.ent_ig = pl + 2 * s.nxs + 1;
+    a.ent_jk = pl + 2 * s.nxs + 1 + s.npw;
+    a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
+    const int ch = chunk_bands(s, c, nb, sizeof(C));
+    C* T = reinterpret_cast<C*>(ws);
+    for (int b0 = 0; b0 < nb; b0 += ch) {
+        const int nbc = std::min(ch, nb - b0);
+        CUDA_TRY(c, launch_density<C>(a, nbc, psi + (size_t)b0 * s.npw, occ + b0, rho, T, tw, tw + c->n1,
+                                      tw + c->n1 + c->n2, st));
+    }
+    return HPSI_OK;
+}
+
 static size_t local_ws(const hpsi_ctx* c, const KSlot& s, int nb, size_t csize)
 {
     int ch = chunk_bands(s, c, nb, csize);
@@ -1034,6 +1062,44 @@ extern "C" int hpsi_apply_energies(hpsi_ctx* c, int kid, int nb, const double* p
         CUDA_TRY(c, cudaStreamSynchronize(st));
         if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
     }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_density(hpsi_ctx* c, int kid, int nb, const double* psi_, const double* occ_, double* rho_,
+                            int flags, void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    if (nb > 0 && (!psi_ || !occ_ || !rho_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/occ/rho NULL");
+    if (nb == 0 || s->npw == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool fp64 = prec == HPSI_PREC_FP64;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t nel = (size_t)nb * s->npw, N = (size_t)c->n1 * c->n2 * c->n3;
+    Carver cv;
+    const size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    const size_t o_occ = dev ? 0 : cv.take<double>((size_t)nb);
+    const size_t o_rho = dev ? 0 : cv.take<double>(N);
+    const size_t o_work = cv.off;
+    if ((rc = ws_reserve(c, o_work + local_ws(c, *s, nb, fp64 ? sizeof(double2) : sizeof(float2))))) return rc;
+    const double2* psi = (const double2*)psi_;
+    const double* occ = occ_;
+    double* rho = rho_;
+    if (!dev) {
+        psi = reinterpret_cast<const double2*>(c->ws + o_psi);
+        occ = reinterpret_cast<const double*>(c->ws + o_occ);
+        rho = reinterpret_cast<double*>(c->ws + o_rho);
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync((void*)occ, occ_, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(rho, rho_, N * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    rc = fp64 ? density_apply<double2>(c, *s, nb, psi, occ, rho, c->ws + o_work, c->d_tw64, st)
+              : density_apply<float2>(c, *s, nb, psi, occ, rho, c->ws + o_work, c->d_tw32, st);
+    if (rc) return rc;
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(rho_, rho, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
     return HPSI_OK;
 }
 

@@ -104,6 +104,10 @@ void local_xpass_shape(LocalArgs* a, size_t csize);
 template <typename C, typename V>
 cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
                          const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof);
+// rho[i][j][k] += sum_b occ_b |psi_b(r)|^2 over nb bands (FP64 sums; FFT in C)
+template <typename C>
+cudaError_t launch_density(const LocalArgs& a, int nb, const double2* psi, const double* occ, double* rho, C* T,
+                           const C* twx, const C* twy, const C* twz, cudaStream_t st);
 // x-pass line buffer bytes of a given (kt, bb) shape
 size_t local_xpass_smem(const LocalArgs& a, bool fp64);
 // Batched local term over the items of a.items: nbands = all bands of the

@@ -305,6 +305,57 @@ __global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::
     lines<C, WIDE, PL>(SmemLines<C>{vo, 1, NL}, stT, vother, vo, a.Lx, a.nl_x, 1, NL, twx, -1);
 }
 
+// Density x pass: a block owns (j, k0..k0+KT) and loops over all bands of the
+// chunk in groups of BB: G->r along x, then
+//   rho[x][j][k0+kk] += sum_b occ_b |psi_b(x, j, k0+kk)|^2
+// with the sum over bands taken in band order in FP64 (one owner thread per
+// (x, kk)), so the result does not depend on the launch shape.
+template <typename C, bool WIDE>
+__global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::x_min)
+    x_density(LocalArgs a, int nb, const C* __restrict__ T, const double* __restrict__ occ, double* __restrict__ rho,
+              const C* __restrict__ tw_x_g)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3, KT = a.kt, BB = a.bb, NL = KT * BB;
+    C* b0 = reinterpret_cast<C*>(smem_raw);
+    C* b1 = b0 + n1 * NL;
+    C* twx = b1 + n1 * NL;
+    int* xpl = reinterpret_cast<int*>(twx + n1);
+    double* acc = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(xpl + n1) + 7) & ~static_cast<uintptr_t>(7));
+    const int j = blockIdx.y;
+    const int k0 = blockIdx.x * KT;
+    const int kt = min(KT, n3 - k0);
+    const size_t plane = (size_t)n2 * n3;
+    for (int t = threadIdx.x; t < n1; t += blockDim.x) { twx[t] = tw_x_g[t]; xpl[t] = -1; }
+    for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) acc[t] = 0.0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < a.nxs; t += blockDim.x) xpl[a.plane_x[t]] = t;
+    __syncthreads();
+    const size_t base = (size_t)j * n3 + k0;
+    const int r = fft_last_read(a.Lx);
+    C* vo = (r == 1) ? b1 : b0;
+    for (int bb0 = 0; bb0 < nb; bb0 += BB) {
+        const int nbb = min(BB, nb - bb0);
+        const XLoad<C, 0> ld{T, xpl, plane, base, a.nxs, KT, kt, nbb, bb0, a.kt_f};
+        lines<C, WIDE, NoPlan>(ld, SmemLines<C>{vo, 1, NL}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
+        __syncthreads();
+        for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) {
+            const int x = t / KT, kk = t - (t / KT) * KT;
+            double s = acc[t];
+            for (int bb = 0; bb < nbb; ++bb) {
+                const C v = vo[x * NL + bb * KT + kk];
+                s += occ[bb0 + bb] * ((double)v.x * (double)v.x + (double)v.y * (double)v.y);
+            }
+            acc[t] = s;
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) {
+        const int x = t / KT, kk = t - (t / KT) * KT;
+        if (kk < kt) rho[((size_t)x * n2 + j) * n3 + k0 + kk] += acc[t];
+    }
+}
+
 template <typename C, bool WIDE, typename PL>
 __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) r2g_planes(LocalArgs a, const C* __restrict__ T, const double2* __restrict__ psi,
                                                   double2* __restrict__ hpsi, const double* __restrict__ kinetic,
@@ -514,6 +565,41 @@ cudaError_t launch_local_batch(const LocalArgs& a, int nbands, int max_nxs, int 
     });
 }
 
+template <typename C>
+static size_t density_smem(const LocalArgs& a)
+{
+    const size_t NL = (size_t)a.kt * a.bb;
+    size_t b = sizeof(C) * (2 * (size_t)a.n1 * NL + a.n1) + sizeof(int) * a.n1;
+    return (b + 7) / 8 * 8 + sizeof(double) * (size_t)a.n1 * a.kt;
+}
+
+template <typename C, bool WIDE, typename PL>
+static cudaError_t launch_density_t(const LocalArgs& a, int nb, const double2* psi, const double* occ, double* rho,
+                                    C* T, const C* twx, const C* twy, const C* twz, cudaStream_t st)
+{
+    const size_t sp = plane_smem<C>(a), sx = density_smem<C>(a);
+    cudaError_t e;
+    auto g2r = g2r_planes<C, WIDE, PL>;
+    auto xd = x_density<C, WIDE>;
+    if ((e = cudaFuncSetAttribute(g2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
+    if ((e = cudaFuncSetAttribute(xd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
+    if (a.nxs == 0 || nb == 0) return cudaSuccess;
+    const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
+    g2r<<<dim3(a.nxs, nb), pt, sp, st>>>(a, psi, T, twy, twz);
+    xd<<<dim3(ceil_div(a.n3, a.kt), a.n2), 256, sx, st>>>(a, nb, T, occ, rho, twx);
+    return cudaGetLastError();
+}
+
+template <typename C>
+cudaError_t launch_density(const LocalArgs& a, int nb, const double2* psi, const double* occ, double* rho, C* T,
+                           const C* twx, const C* twy, const C* twz, cudaStream_t st)
+{
+    if (a.items || a.epart) return cudaErrorInvalidValue;
+    return with_kernels<C>(a, [&](auto wide, auto pl, auto) {
+        return launch_density_t<C, decltype(wide)::value, decltype(pl)>(a, nb, psi, occ, rho, T, twx, twy, twz, st);
+    });
+}
+
 size_t local_xpass_smem(const LocalArgs& a, bool fp64)
 {
     return fp64 ? xpass_smem<double2, double>(a) : xpass_smem<float2, float>(a);
@@ -539,3 +625,7 @@ template cudaError_t launch_local_batch<double2, double>(const LocalArgs&, int, 
                                                          const double2*, const double2*, const double2*, cudaStream_t);
 template cudaError_t launch_local_batch<float2, float>(const LocalArgs&, int, int, int, float2*, const float*,
                                                        const float2*, const float2*, const float2*, cudaStream_t);
+template cudaError_t launch_density<double2>(const LocalArgs&, int, const double2*, const double*, double*, double2*,
+                                             const double2*, const double2*, const double2*, cudaStream_t);
+template cudaError_t launch_density<float2>(const LocalArgs&, int, const double2*, const double*, double*, float2*,
+                                            const float2*, const float2*, const float2*, cudaStream_t);

@@ -169,6 +169,28 @@ class Hamiltonian:
                                             _stream_for(dev_p)), self._ctx)
         return e
 
+    def density(self, kid: int, nb: int, psi, occ, rho=None, precision: Optional[str] = None):
+        """rho += sum_b occ_b |psi_b(r)|^2 (the reference's buildDensity for one k-point), [n1, n2, n3]."""
+        npw = self.dim(kid)
+        p, dev = _ptr(psi, npw, nb, "psi")
+        s = self.system
+        if rho is None:
+            if dev:
+                import torch
+                rho = torch.zeros((s.n1, s.n2, s.n3), dtype=torch.float64, device=psi.device)
+            else:
+                rho = np.zeros((s.n1, s.n2, s.n3), dtype=np.float64)
+        if dev:
+            op, rp = occ.data_ptr(), rho.data_ptr()
+        else:
+            occ = np.ascontiguousarray(occ, dtype=np.float64)
+            if rho.dtype != np.float64 or not rho.flags["C_CONTIGUOUS"] or rho.size != s.n1 * s.n2 * s.n3:
+                raise HpsiError(abi.HPSI_ERR_BAD_ARG, "rho must be a C-contiguous float64 grid")
+            op, rp = occ.ctypes.data, rho.ctypes.data
+        check(self._lib.hpsi_density(self._ctx, kid, nb, p, op, rp, self.flags(precision, dev), _stream_for(dev)),
+              self._ctx)
+        return rho
+
     def grad_apply(self, kid: int, nb: int, psi, out: GradHPsi, precision: Optional[str] = None):
         npw = self.dim(kid)
         p, dev = _ptr(psi, npw, nb, "psi")

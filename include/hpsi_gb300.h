@@ -125,6 +125,18 @@ int hpsi_dim(const hpsi_ctx* ctx, int kid);
 int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
                int flags, void* stream);
 
+/* Charge density of one k-point: rho[i][j][k] += sum_b occ[b] |psi_b(r)|^2,
+ * psi_b(r) the unnormalised G->r transform of the band scattered onto the grid
+ * (the last of several aliasing G wins), as the reference's buildDensity
+ * (src/support/density.cppm:41-94) accumulates it per k-point and band; call
+ * once per k-point to sum a Monkhorst-Pack grid.  rho: n1*n2*n3 doubles in
+ * [i][j][k] order (the RHO file order), accumulated; occ: nb doubles.  The
+ * transform runs in complex128 for HPSI_PREC_FP64 and complex64 otherwise;
+ * the band sums are FP64 in band order.  Host or device pointers as in
+ * hpsi_apply. */
+int hpsi_density(hpsi_ctx* ctx, int kid, int nb, const double* psi, const double* occ, double* rho,
+                 int flags, void* stream);
+
 /* k·p sums of second-order perturbation theory, FP64, for the lowest n_low bands:
  *   s[n][a][b] = sum_{m != n, |e_n - e_m| > deg_tol} Re(m_a[n][m] m_b[m][n]) / (e_n - e_m)
  * from a velocity matrix m ([3][nb][nb] complex, hpsi_velocity_matrix's layout)

@@ -647,6 +647,42 @@ int oracle_velocity(const hpsi_system* sys, const hpsi_kpoint* kp, int nb, const
     return rc;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Charge density (src/support/density.cppm:41-94): for every band with a      */
+/* non-zero occupation, scatter psi onto a zeroed grid at (g mod n) (the last  */
+/* write wins), G2R transform, rho[r] += occ * |psi(r)|^2.  rho accumulates.   */
+/* ------------------------------------------------------------------------ */
+int oracle_density(const hpsi_system* sys, const hpsi_kpoint* kp, int nb, const double* psi, const double* occ,
+                   double* rho)
+{
+    const int n1 = sys->n1, n2 = sys->n2, n3 = sys->n3, ng = kp->npw;
+    const size_t n123 = (size_t)n1 * n2 * n3;
+    double* grid = (double*)malloc(sizeof(double) * 2 * n123);
+    if (!grid) return HPSI_ERR_OOM;
+    for (int b = 0; b < nb; ++b) {
+        const double o = occ[b];
+        if (o == 0.0) continue;  /* density.cppm:66 */
+        const double* ps = psi + (size_t)2 * b * ng;
+        memset(grid, 0, sizeof(double) * 2 * n123);
+        for (int ig = 0; ig < ng; ++ig) {
+            int i = ((kp->g_idx[3 * ig] % n1) + n1) % n1;
+            int j = ((kp->g_idx[3 * ig + 1] % n2) + n2) % n2;
+            int k = ((kp->g_idx[3 * ig + 2] % n3) + n3) % n3;
+            size_t idx = (size_t)i * n2 * n3 + (size_t)j * n3 + k;
+            grid[2 * idx] = ps[2 * ig];
+            grid[2 * idx + 1] = ps[2 * ig + 1];
+        }
+        oracle_fft3d(grid, n1, n2, n3, +1);
+        for (size_t r = 0; r < n123; ++r) {
+            /* std::norm(z) = re^2 + im^2 */
+            const double m = grid[2 * r] * grid[2 * r] + grid[2 * r + 1] * grid[2 * r + 1];
+            rho[r] += o * m;
+        }
+    }
+    free(grid);
+    return HPSI_OK;
+}
+
 /* 1-D transform with the pocketfft convention (test hook for the FFT KATs). */
 int oracle_fft1d(double* c, int n, int sign, double fct)
 {

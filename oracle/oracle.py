@@ -45,6 +45,7 @@ def lib():
         L.oracle_hpsi.argtypes = [sysp, kpp, C.c_int, dp, dp, C.c_int]
         L.oracle_grad.argtypes = [sysp, kpp, C.c_int, dp, dp, dp, dp]
         L.oracle_velocity.argtypes = [sysp, kpp, C.c_int, dp, dp]
+        L.oracle_density.argtypes = [sysp, kpp, C.c_int, dp, dp, dp]
         L.oracle_ylm.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
         L.oracle_ylm.restype = None
         L.oracle_beta_interp.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
@@ -86,6 +87,16 @@ def velocity(sysm, kp, psi: np.ndarray):
     out = np.zeros((3, nb, nb), dtype=np.complex128)
     S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
     _check(lib().oracle_velocity(S.ref(), K.ref(), nb, abi.cptr(psi), abi.cptr(out)))
+    return out
+
+
+def density(sysm, kp, psi: np.ndarray, occ, rho: np.ndarray = None) -> np.ndarray:
+    """rho[i][j][k] += sum_b occ_b |psi_b(r)|^2 (the reference's buildDensity for one k-point)."""
+    psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1, kp.npw)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    out = np.zeros(sysm.n1 * sysm.n2 * sysm.n3) if rho is None else rho
+    S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
+    _check(lib().oracle_density(S.ref(), K.ref(), psi.shape[0], abi.cptr(psi), abi.cptr(occ), abi.cptr(out)))
     return out
 
 

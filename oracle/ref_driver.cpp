@@ -18,6 +18,7 @@
 //
 // Modes:
 //   ref_driver golden <spec.bin> <out.bin> <workdir>
+//   ref_driver density <spec.bin> <occ.txt> <out.bin> <workdir>
 //   ref_driver time   <spec.bin> <workdir> <ikpt> <band0> <nbands>
 //       (prints one JSON line with the seconds spent in H|psi> alone)
 
@@ -373,6 +374,50 @@ int timeit(const std::string& spec_path, const std::string& dir, int ik, int ban
     return 0;
 }
 
+// Charge density through the reference's own buildDensity
+// (src/support/density.cppm:41-94): the spec's k-points and bands, occupations
+// read from occ_path (nkpt*nband whitespace-separated values, k-point major)
+// and written as an OUT.OCC file for the reference's OCC reader
+// (src/io/OCC.cppm:84-230).  Output: "RHOREF01", n1, n2, n3, rho[n1*n2*n3].
+int density(const std::string& spec_path, const std::string& occ_path, const std::string& out_path,
+            const std::string& dir) {
+    Spec s = readSpec(spec_path);
+    setup(s, dir);
+    std::vector<double> occ;
+    {
+        std::FILE* f = std::fopen(occ_path.c_str(), "r");
+        if (!f) throw std::runtime_error("cannot read " + occ_path);
+        double v;
+        while (std::fscanf(f, "%lf", &v) == 1) occ.push_back(v);
+        std::fclose(f);
+    }
+    const int nk = static_cast<int>(s.kpts.size());
+    if (static_cast<int>(occ.size()) != nk * s.nband) throw std::runtime_error("occupations: wrong count");
+    {
+        std::FILE* f = std::fopen((dir + "/OUT.OCC").c_str(), "w");
+        if (!f) throw std::runtime_error("cannot write OUT.OCC");
+        for (int ik = 0; ik < nk; ++ik) {
+            std::fprintf(f, "KPOINTS %d: 0.0 0.0 0.0\n", ik + 1);
+            for (int b = 0; b < s.nband; ++b) std::fprintf(f, "%d 0.0 %.17g\n", b + 1, occ[ik * s.nband + b]);
+        }
+        std::fclose(f);
+    }
+    GKK gkk(dir + "/OUT.GKK");
+    WG wg(dir + "/OUT.WG");
+    OCC oc(dir + "/OUT.OCC");
+    auto rho = buildDensity(gkk, wg, oc);
+    std::FILE* f = std::fopen(out_path.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot write " + out_path);
+    Out O{f};
+    O.arr("RHOREF01", 8);
+    O.put(s.n1);
+    O.put(s.n2);
+    O.put(s.n3);
+    O.arr(rho.data(), rho.size());
+    std::fclose(f);
+    return 0;
+}
+
 }  // namespace refdrv
 
 // UPF from the in-memory registry (replaces the pugixml reader of
@@ -410,9 +455,11 @@ int main(int argc, char** argv) {
     try {
         std::string mode = argc > 1 ? argv[1] : "";
         if (mode == "golden" && argc == 5) return refdrv::golden(argv[2], argv[3], argv[4]);
+        if (mode == "density" && argc == 6) return refdrv::density(argv[2], argv[3], argv[4], argv[5]);
         if (mode == "time" && argc == 7)
             return refdrv::timeit(argv[2], argv[3], std::atoi(argv[4]), std::atoi(argv[5]), std::atoi(argv[6]));
-        std::fprintf(stderr, "usage: ref_driver golden <spec> <out> <dir> | time <spec> <dir> <ik> <b0> <nb>\n");
+        std::fprintf(stderr, "usage: ref_driver golden <spec> <out> <dir> | density <spec> <occ> <out> <dir> | "
+                             "time <spec> <dir> <ik> <b0> <nb>\n");
         return 2;
     } catch (const std::exception& e) {
         std::fprintf(stderr, "ref_driver: %s\n", e.what());

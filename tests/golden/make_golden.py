@@ -7,7 +7,8 @@ oracle/ref_driver.cpp) on a synthetic system from effmass_gb300.system.  The
 fixture stores everything the reference used — lattice, volume, raw beta and
 dbeta tables with lambda after its per-l diagonalisation, the G-sphere views
 (g_idx, K, kinetic, q, theta, phi, inferred k), V_loc, atoms, psi — and its
-outputs hpsi and grad.
+outputs hpsi and grad, and the reference's charge density (buildDensity) of the
+same bands with seeded occupations.
 
 Run in a checkout where the reference sources are available:
     python tests/golden/make_golden.py
@@ -49,6 +50,9 @@ def make_case(name, sysname, kf, nb, grid):
         sysm.v_loc = S.local_potential(sysm.lattice, sysm.atom_tau, *grid)
     kp = S.g_sphere(sysm.lattice, kf, sysm.ecut)
     psi = S.make_bands(kp, nb, seed=17)
+    # occupations in [0, 2] with one empty band (the reference skips those)
+    occ = np.random.default_rng(23).uniform(0.0, 2.0, nb)
+    occ[nb // 2] = 0.0
     with tempfile.TemporaryDirectory() as td:
         spec = os.path.join(td, "spec.bin")
         gold = os.path.join(td, "gold.bin")
@@ -56,6 +60,16 @@ def make_case(name, sysname, kf, nb, grid):
         subprocess.run([O.REF_DRIVER, "golden", spec, gold, os.path.join(td, "wd")], check=True,
                        stderr=subprocess.DEVNULL)
         g = S.read_golden(gold)
+        # the reference's buildDensity on the same k-point and bands
+        occ_txt, rho_bin = os.path.join(td, "occ.txt"), os.path.join(td, "rho.bin")
+        np.savetxt(occ_txt, occ, fmt="%.17g")
+        subprocess.run([O.REF_DRIVER, "density", spec, occ_txt, rho_bin, os.path.join(td, "wd2")], check=True,
+                       stderr=subprocess.DEVNULL)
+        raw = open(rho_bin, "rb").read()
+        assert raw[:8] == b"RHOREF01"
+        dims = np.frombuffer(raw[8:20], dtype=np.int32)
+        rho = np.frombuffer(raw[20:], dtype=np.float64).copy()
+        assert tuple(dims) == (sysm.n1, sysm.n2, sysm.n3) and rho.size == int(np.prod(dims))
     sp = g["species"][0]
     gk = g["kpts"][0]
     out = dict(
@@ -66,7 +80,7 @@ def make_case(name, sysname, kf, nb, grid):
         sp_beta_q=sp["beta_q"], sp_dbeta_q=sp["dbeta_q"],
         k_frac=gk["k_frac"], g_idx=gk["g_idx"], kvec=gk["kvec"], kinetic=gk["kinetic"],
         q=gk["q"], theta=gk["theta"], phi=gk["phi"],
-        psi=psi, hpsi=gk["hpsi"], grad=gk["grad"])
+        psi=psi, hpsi=gk["hpsi"], grad=gk["grad"], occ=occ, rho=rho)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     return kp.npw
 

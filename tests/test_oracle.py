@@ -9,6 +9,7 @@
   BetaqTables::interpolate (src/pseudo/ncpp_advance.cppm:644-674).
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -31,6 +32,17 @@ def test_oracle_matches_reference_grad(oracle_lib, case):
     sysm, kp, psi, _, gref = load_case(case)
     g = oracle_lib.grad(sysm, kp, psi)
     assert rel_err(g, gref) <= 1e-14, case
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_reference_density(oracle_lib, case):
+    """rho from the reference's buildDensity (src/support/density.cppm:41-94),
+    occupations with one empty band, aliasing included (the 6^3 case)."""
+    import numpy as np
+    sysm, kp, psi, _, _ = load_case(case)
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{case}.npz"))
+    rho = oracle_lib.density(sysm, kp, psi, z["occ"])
+    assert rel_err(rho, z["rho"]) <= 1e-14, rel_err(rho, z["rho"])
 
 
 @pytest.mark.parametrize("case", ["tiny", "tinyd", "fcc2"])
