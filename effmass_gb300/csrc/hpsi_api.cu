@@ -1065,6 +1065,149 @@ extern "C" int hpsi_apply_energies(hpsi_ctx* c, int kid, int nb, const double* p
     return HPSI_OK;
 }
 
+// ---------------------------------------------------------------- Sternheimer
+// v <- P_c v = v - psi (psi^H v) for nb vectors against the nv occupied bands
+// psi (FP64 SIMT GEMMs: the nv x nb overlap, split over G, then the update).
+struct ProjWs {
+    double2* part;   // [ns][nv][nb]
+    double2* W;      // [nv][nb]
+    double* minus;   // nv x (-1)
+    int ns;
+};
+
+static int project_out(hpsi_ctx* c, KSlot& s, int nv, const double2* psi, int nb, double2* v, const ProjWs& w,
+                       cudaStream_t st)
+{
+    CUDA_TRY(c, (launch_proj_gemm<double2, double2, double2>(nv, nb, s.npw, psi, (size_t)s.npw, v, (size_t)s.npw, w.part,
+                                                             w.ns, st)));
+    CUDA_TRY(c, (launch_reduce_splits<double2, double2>(nv, nb, w.ns, w.part, w.minus, nv, w.W, (size_t)nb, st)));
+    CUDA_TRY(c, launch_expand_gemm<double2>(nv, nb, s.npw, w.W, (size_t)nb, psi, (size_t)s.npw, v, (size_t)s.npw, st));
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_sternheimer(hpsi_ctx* c, int kid, int nv, const double* psi_, const double* eps_, int direction,
+                                double tol, int max_iter, double* x_, int* iterations, double* residual, int flags,
+                                void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nv, &s, flags);
+    if (rc) return rc;
+    if (direction < 0 || direction > 2) return fail(c, HPSI_ERR_BAD_ARG, "direction must be 0, 1 or 2");
+    if (!(tol > 0.0) || max_iter < 1) return fail(c, HPSI_ERR_BAD_ARG, "need tol > 0 and max_iter >= 1");
+    if (nv > 0 && (!psi_ || !eps_ || !x_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/eps/x NULL");
+    if (nv == 0 || s->npw == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const int npw = s->npw;
+    const size_t nel = (size_t)nv * npw;
+    const int ns = split_for(nv, nv, npw);
+    // workspace: inputs (host case), x, r, z, p, q, projection and scalars, then H / gradient workspace
+    Carver cv;
+    const size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    const size_t o_eps = dev ? 0 : cv.take<double>((size_t)nv);
+    const size_t o_x = dev ? 0 : cv.take<double2>(nel);
+    const size_t o_r = cv.take<double2>(nel), o_z = cv.take<double2>(nel), o_p = cv.take<double2>(nel);
+    const size_t o_q = cv.take<double2>(nel);
+    const size_t o_part = cv.take<double2>((size_t)ns * nv * nv), o_W = cv.take<double2>((size_t)nv * nv);
+    const size_t o_min = cv.take<double>((size_t)nv);
+    const size_t o_sc = cv.take<double>((size_t)8 * nv);
+    const size_t o_act = cv.take<int>((size_t)nv);
+    const size_t o_work = cv.off;
+    const size_t work = std::max(apply_ws_bytes(c, *s, nv, prec), grad_ws_bytes(*s, nv, prec));
+    if ((rc = ws_reserve(c, o_work + work))) return rc;
+    unsigned char* ws = c->ws;
+    const double2* psi = dev ? (const double2*)psi_ : reinterpret_cast<const double2*>(ws + o_psi);
+    const double* eps = dev ? eps_ : reinterpret_cast<const double*>(ws + o_eps);
+    double2* x = dev ? (double2*)x_ : reinterpret_cast<double2*>(ws + o_x);
+    double2 *r = reinterpret_cast<double2*>(ws + o_r), *z = reinterpret_cast<double2*>(ws + o_z);
+    double2 *p = reinterpret_cast<double2*>(ws + o_p), *q = reinterpret_cast<double2*>(ws + o_q);
+    double* sc = reinterpret_cast<double*>(ws + o_sc);
+    double *rz = sc, *rz_new = sc + nv, *pq = sc + 2 * nv, *alpha = sc + 3 * nv, *beta = sc + 4 * nv;
+    double *rr = sc + 5 * nv, *bb = sc + 6 * nv;
+    int* active = reinterpret_cast<int*>(ws + o_act);
+    ProjWs pw{reinterpret_cast<double2*>(ws + o_part), reinterpret_cast<double2*>(ws + o_W),
+              reinterpret_cast<double*>(ws + o_min), ns};
+    unsigned char* wk = ws + o_work;
+    if (!dev) {
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync((void*)eps, eps_, nv * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    {
+        std::vector<double> m1(nv, -1.0);
+        std::vector<int> one(nv, 1);
+        CUDA_TRY(c, cudaMemcpyAsync(pw.minus, m1.data(), nv * sizeof(double), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(active, one.data(), nv * sizeof(int), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaStreamSynchronize(st));  // the host vectors go out of scope
+    }
+    // b = -P_c dH/dk_a psi  (in r), x = 0
+    CUDA_TRY(c, cudaMemsetAsync(q, 0, nel * sizeof(double2), st));
+    double2* d3[3] = {nullptr, nullptr, nullptr};
+    d3[direction] = q;
+    if ((rc = grad_dev(c, *s, nv, psi, d3, prec, wk, st))) return rc;
+    if ((rc = project_out(c, *s, nv, psi, nv, q, pw, st))) return rc;
+    CUDA_TRY(c, cudaMemsetAsync(r, 0, nel * sizeof(double2), st));
+    CUDA_TRY(c, launch_baxpy(npw, nv, nullptr, -1.0, q, r, st));
+    CUDA_TRY(c, cudaMemsetAsync(x, 0, nel * sizeof(double2), st));
+    CUDA_TRY(c, launch_bdot(npw, nv, r, r, bb, st));
+    // z = P_c M^-1 r, p = z, rz = <r, z>
+    const double tau = 1.0;  // Ha: keeps the diagonal preconditioner positive
+    CUDA_TRY(c, launch_bprec(npw, nv, s->d_kin, eps, tau, r, z, st));
+    if ((rc = project_out(c, *s, nv, psi, nv, z, pw, st))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(p, z, nel * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(c, launch_bdot(npw, nv, r, z, rz, st));
+    std::vector<double> hb(nv), hr(nv);
+    std::vector<int> hact(nv, 1);
+    CUDA_TRY(c, cudaMemcpyAsync(hb.data(), bb, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    int it = 0, n_active = 0;
+    for (int b = 0; b < nv; ++b) {
+        hact[b] = hb[b] > 0.0;
+        n_active += hact[b];
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(active, hact.data(), nv * sizeof(int), cudaMemcpyHostToDevice, st));
+    for (; it < max_iter && n_active > 0; ++it) {
+        // q = A p = P_c (H p - e p)
+        CUDA_TRY(c, cudaMemsetAsync(q, 0, nel * sizeof(double2), st));
+        if ((rc = apply_dev(c, *s, nv, p, q, prec, wk, st))) return rc;
+        CUDA_TRY(c, launch_bscale_add(npw, nv, eps, -1.0, p, q, st));
+        if ((rc = project_out(c, *s, nv, psi, nv, q, pw, st))) return rc;
+        // alpha = rz / <p, q>;  x += alpha p;  r -= alpha q
+        CUDA_TRY(c, launch_bdot(npw, nv, p, q, pq, st));
+        CUDA_TRY(c, launch_bratio(nv, rz, pq, active, alpha, st));
+        CUDA_TRY(c, launch_baxpy(npw, nv, alpha, 1.0, p, x, st));
+        CUDA_TRY(c, launch_baxpy(npw, nv, alpha, -1.0, q, r, st));
+        // convergence: |r| <= tol |b| per band
+        CUDA_TRY(c, launch_bdot(npw, nv, r, r, rr, st));
+        CUDA_TRY(c, cudaMemcpyAsync(hr.data(), rr, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        n_active = 0;
+        for (int b = 0; b < nv; ++b) {
+            if (hact[b] && hr[b] <= tol * tol * hb[b]) hact[b] = 0;
+            n_active += hact[b];
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(active, hact.data(), nv * sizeof(int), cudaMemcpyHostToDevice, st));
+        if (n_active == 0) { ++it; break; }
+        // z = P_c M^-1 r;  beta = <r, z>_new / <r, z>;  p = z + beta p
+        CUDA_TRY(c, launch_bprec(npw, nv, s->d_kin, eps, tau, r, z, st));
+        if ((rc = project_out(c, *s, nv, psi, nv, z, pw, st))) return rc;
+        CUDA_TRY(c, launch_bdot(npw, nv, r, z, rz_new, st));
+        CUDA_TRY(c, launch_bratio(nv, rz_new, rz, active, beta, st));
+        CUDA_TRY(c, launch_baxpby(npw, nv, nullptr, 1.0, z, beta, p, st));
+        CUDA_TRY(c, cudaMemcpyAsync(rz, rz_new, nv * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+    if (iterations) *iterations = it;
+    if (residual)
+        for (int b = 0; b < nv; ++b) residual[b] = hb[b] > 0.0 ? std::sqrt(hr[b] / hb[b]) : 0.0;
+    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(x_, x, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (is_tc(prec) && (rc = check_device_flag(c))) return rc;
+    if (n_active > 0)
+        return fail(c, HPSI_ERR_TIMEOUT, "Sternheimer CG: %d of %d bands above tol after %d iterations", n_active, nv,
+                    it);
+    return HPSI_OK;
+}
+
 extern "C" int hpsi_density(hpsi_ctx* c, int kid, int nb, const double* psi_, const double* occ_, double* rho_,
                             int flags, void* stream)
 {

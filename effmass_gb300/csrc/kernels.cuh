@@ -226,3 +226,22 @@ cudaError_t launch_band_sub(int nb, const double* after, const double* before, d
 // skipped[n] = pairs within tol (skipped may be null)
 cudaError_t launch_kp_sums(int nb, int n_low, const double2* M, const double* E, double tol, double* S, int* skipped,
                            cudaStream_t st);
+
+// ---- band-batched FP64 vector kernels of the Sternheimer CG (sternheimer.cu) ----
+// vectors are [nb][n] complex128; scalars one per band
+cudaError_t launch_bdot(int n, int nb, const double2* x, const double2* y, double* d, cudaStream_t st);
+// y_b += asign * alpha_b x_b (alpha null: 1)
+cudaError_t launch_baxpy(int n, int nb, const double* alpha, double asign, const double2* x, double2* y,
+                         cudaStream_t st);
+// y_b = asign * alpha_b x_b + beta_b y_b
+cudaError_t launch_baxpby(int n, int nb, const double* alpha, double asign, const double2* x, const double* beta,
+                          double2* y, cudaStream_t st);
+// y_b += scale * e_b x_b
+cudaError_t launch_bscale_add(int n, int nb, const double* e, double scale, const double2* x, double2* y,
+                              cudaStream_t st);
+// z_b(G) = r_b(G) / (max(kin(G) - e_b, 0) + tau)
+cudaError_t launch_bprec(int n, int nb, const double* kin, const double* e, double tau, const double2* r, double2* z,
+                         cudaStream_t st);
+// out_b = active_b && den_b > 0 ? num_b / den_b : 0
+cudaError_t launch_bratio(int nb, const double* num, const double* den, const int* active, double* out,
+                          cudaStream_t st);

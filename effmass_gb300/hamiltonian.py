@@ -169,6 +169,24 @@ class Hamiltonian:
                                             _stream_for(dev_p)), self._ctx)
         return e
 
+    def sternheimer(self, kid: int, psi, eps, direction: int, tol: float = 1e-10, max_iter: int = 500,
+                    precision: Optional[str] = None):
+        """Solve P_c (H - eps_n) P_c x_n = -P_c dH/dk_a psi_n for the occupied eigenstates psi
+        (numpy [nv, npw]); returns (x [nv, npw], iterations, relative residuals [nv])."""
+        npw = self.dim(kid)
+        psi = np.ascontiguousarray(psi, dtype=np.complex128)
+        nv = psi.shape[0]
+        eps = np.ascontiguousarray(eps, dtype=np.float64)
+        x = np.zeros_like(psi)
+        its = C.c_int()
+        res = np.zeros(nv)
+        st = self._lib.hpsi_sternheimer(self._ctx, kid, nv, psi.ctypes.data, eps.ctypes.data, direction, tol,
+                                        max_iter, x.ctypes.data, C.byref(its),
+                                        res.ctypes.data_as(C.POINTER(C.c_double)), self.flags(precision, False),
+                                        None)
+        check(st, self._ctx)
+        return x, its.value, res
+
     def density(self, kid: int, nb: int, psi, occ, rho=None, precision: Optional[str] = None):
         """rho += sum_b occ_b |psi_b(r)|^2 (the reference's buildDensity for one k-point), [n1, n2, n3]."""
         npw = self.dim(kid)

@@ -125,6 +125,23 @@ int hpsi_dim(const hpsi_ctx* ctx, int kid);
 int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
                int flags, void* stream);
 
+/* Sternheimer equations for the k-derivative of the occupied bands (the
+ * reference's roadmap item: conjugate-gradient solution of the linear
+ * equations, docs/roadmap.md): for each of the nv occupied bands psi_n with
+ * eigenvalue eps_n (orthonormal eigenstates of this k-point's H, lowest first)
+ *   P_c (H - eps_n) P_c x_n = -P_c dH/dk_a psi_n,   P_c = 1 - sum_m |psi_m><psi_m|,
+ * x_n = P_c dpsi_n/dk_a.  One preconditioned CG per band, all bands batched
+ * (each iteration applies H to nv vectors through the hpsi_apply path of the
+ * flags' precision; dots, updates and the projections are FP64), stopping
+ * when |r_n| <= tol |b_n| for every band.  x: nv x npw output (overwritten);
+ * iterations (may be NULL): CG iterations taken; residual (may be NULL, host):
+ * nv final relative residuals.  HPSI_ERR_TIMEOUT when max_iter is reached
+ * first (x then holds the last iterate).  psi, eps, x: host or device per
+ * HPSI_DEVICE_PTRS.  The reference has no implementation of this step. */
+int hpsi_sternheimer(hpsi_ctx* ctx, int kid, int nv, const double* psi, const double* eps, int direction,
+                     double tol, int max_iter, double* x, int* iterations, double* residual, int flags,
+                     void* stream);
+
 /* Charge density of one k-point: rho[i][j][k] += sum_b occ[b] |psi_b(r)|^2,
  * psi_b(r) the unnormalised G->r transform of the band scattered onto the grid
  * (the last of several aliasing G wins), as the reference's buildDensity
