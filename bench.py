@@ -44,6 +44,8 @@ def parse():
                     help="requests of the served Poisson stream (0 skips serving)")
     ap.add_argument("--serving-rate", type=float, default=200.0)
     ap.add_argument("--serving-lanes", type=int, default=4)
+    ap.add_argument("--no-sternheimer", action="store_true",
+                    help="skip the Sternheimer dpsi/dk solve (2-atom fcc cell, 4 occupied bands, x/y/z)")
     ap.add_argument("--no-kp", action="store_true",
                     help="skip the k.p workload (64-atom cell, 256 bands, 7 k-points, velocity + FP64 sums)")
     ap.add_argument("--no-batched", action="store_true",
@@ -209,6 +211,20 @@ def run_gb300(args, rank, world, local):
                 "max_abs_diff_vs_fp64_Ha": de_api, "value": nb / (ms_e * 1e-3), "unit": "band-apps/s",
                 "ms_per_step": ms_e}
     del h_e
+    # charge density of the same bands (G->r only, FP64 band sums), complex64 transforms
+    occ_d = torch.full((nb,), 2.0, dtype=torch.float64, device="cuda")
+    rho_d = torch.zeros((sysm.n1, sysm.n2, sysm.n3), dtype=torch.float64, device="cuda")
+    H.density(0, nb, psi_d, occ_d, rho=rho_d, precision="fp32")
+    torch.cuda.synchronize()
+    g0.record(stream)
+    for _ in range(args.steps):
+        H.density(0, nb, psi_d, occ_d, rho=rho_d, precision="fp32")
+    g1.record(stream)
+    torch.cuda.synchronize()
+    ms_d = g0.elapsed_time(g1) / args.steps
+    density = {"api": "hpsi_density (complex64 G->r, FP64 band sums)", "bands": nb,
+               "value": nb / (ms_d * 1e-3), "unit": "band-densities/s", "ms_per_step": ms_d}
+    del rho_d
 
     fp64 = None
     if not args.no_fp64 and args.prec != "fp64":
@@ -315,6 +331,9 @@ def run_gb300(args, rank, world, local):
     kp_out = None
     if rank == 0 and not args.no_kp:
         kp_out = run_kp(args)
+    stern = None
+    if rank == 0 and not args.no_sternheimer:
+        stern = run_sternheimer(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -337,11 +356,11 @@ def run_gb300(args, rank, world, local):
                    "l2": "inputs larger than L2 (projector matrix %d MB, psi %d MB)" % (P * npw * csz >> 20,
                                                                                        psi.nbytes >> 20)},
         "rel_err_vs_fp64": err, "band_energy_max_abs_diff_Ha": de_api,
-        "rayleigh_quotient_of_hpsi_max_abs_diff_Ha": de, "band_energies": energies,
+        "rayleigh_quotient_of_hpsi_max_abs_diff_Ha": de, "band_energies": energies, "density": density,
         "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "grad_value": grad_value, "grad_unit": "band-apps/s of dH/dk_{x,y,z}|psi> (all three directions)",
         "e2e": e2e, "roofline": roof, "roofline_gemm": roof_gemm, "phases": phases, "gpu_launches": gpu_launches,
-        "cpu_baseline": cpu, "clocks": clk, "serving": serving, "batched": batched, "kp": kp_out,
+        "cpu_baseline": cpu, "clocks": clk, "serving": serving, "batched": batched, "kp": kp_out, "sternheimer": stern,
     }
     if rank == 0:
         print(json.dumps(out))
@@ -638,6 +657,47 @@ def run_kp(args):
         "note": "each k-point: dH/dk_{x,y,z}|psi> (tensor-core projector GEMMs) + psi^H G_a on the tensor cores "
                 "(split FP16, FP32 accumulation, FP64 split-K sums) + FP64 k.p sums; timed with CUDA events",
     }
+
+
+def run_sternheimer(args):
+    """dpsi/dk of the 4 occupied bands of the 2-atom fcc cell (Ecut 15 Ha, 24^3,
+    k = (0.1, 0.2, 0.3)) by the batched CG, x/y/z, in FP64 and with the
+    tensor-core H, against the exact sum over states of a dense FP64
+    diagonalisation (the k-point's full H matrix, npw columns)."""
+    import numpy as np
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import GradHPsi, Hamiltonian
+    nv = 4
+    sysm = S.make_system("fcc2")
+    kp = S.g_sphere(sysm.lattice, (0.1, 0.2, 0.3), sysm.ecut)
+    npw = kp.npw
+    out = {"workload": f"fcc2, k=(0.1,0.2,0.3), npw {npw}, {nv} occupied bands, directions x,y,z"}
+    with Hamiltonian(sysm) as H:
+        H.set_kpoint(0, kp)
+        eye = np.eye(npw, dtype=np.complex128)
+        hm = np.zeros_like(eye)
+        H.apply(0, npw, eye, hm, "fp64")
+        hm = hm.T
+        E, V = np.linalg.eigh(0.5 * (hm + hm.conj().T))
+        psi = np.ascontiguousarray(V[:, :nv].T)
+        d = np.zeros((3, nv, npw), dtype=np.complex128)
+        H.grad_apply(0, nv, psi, GradHPsi(d[0], d[1], d[2]))
+        Vc = V[:, nv:]
+        for prec, tol in (("fp64", 1e-10), ("tc", 1e-6)):
+            errs, its, ms = [], [], []
+            for a in range(3):
+                coef = Vc.conj().T @ d[a].T
+                x_ref = -(Vc @ (coef / (E[nv:, None] - E[None, :nv]))).T
+                H.sternheimer(0, psi, E[:nv], a, tol=tol, precision=prec)  # warm
+                t0 = time.perf_counter()
+                x, it, _ = H.sternheimer(0, psi, E[:nv], a, tol=tol, precision=prec)
+                ms.append((time.perf_counter() - t0) * 1e3)
+                its.append(it)
+                errs.append(float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)))
+            out[prec] = {"tol": tol, "iterations": its, "ms_per_solve": ms, "rel_err_vs_sum_over_states": max(errs),
+                         "band_apps_per_s": float(sum(its) * nv / (sum(ms) * 1e-3))}
+    out["note"] = "host-timed solves (one H application of the 4 bands, projections and FP64 dots per iteration)"
+    return out
 
 
 def run_reference(args, rank, world, local):

@@ -20,50 +20,53 @@ template <> HPSI_D float2 load_as<float2, double2>(const double2& v) { return to
 template <> HPSI_D float2 load_as<float2, float2>(const float2& v) { return v; }
 template <> HPSI_D double2 load_as<double2, float2>(const float2& v) { return to_c128(v); }
 
-#define GB_M 64
-#define GB_N 64
-#define GB_K 16
+constexpr int GB_K = 16;  // K slice staged per iteration
 
-template <typename TA, typename TB, typename Acc>
+// Projection tile: (16 TM) x (16 TN) outputs per 256-thread block, each thread
+// TM x TN at stride 16 (conflict-free shared-memory reads).  The launcher picks
+// the tile from M and N so that small problems (a few bands, few projectors)
+// do not spend the block on padding — FP64 runs at a small fraction of the
+// FP32 rate on this part, so wasted FP64 work shows directly.
+template <typename TA, typename TB, typename Acc, int TM, int TN>
 __global__ void __launch_bounds__(256) proj_gemm_kernel(int M, int N, int K, const TA* __restrict__ A, size_t lda,
                                                         const TB* __restrict__ B, size_t ldb, Acc* __restrict__ part,
                                                         int kchunk)
 {
     using R = typename Real<Acc>::type;
-    __shared__ Acc As[GB_K][GB_M + 1];
-    __shared__ Acc Bs[GB_K][GB_N + 1];
-    const int m0 = blockIdx.x * GB_M, n0 = blockIdx.y * GB_N, s = blockIdx.z;
+    constexpr int BM = 16 * TM, BN = 16 * TN;
+    __shared__ Acc As[GB_K][BM + 1];
+    __shared__ Acc Bs[GB_K][BN + 1];
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, s = blockIdx.z;
     const int kbeg = s * kchunk;
     const int kend = min(K, kbeg + kchunk);
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    R accr[4][4], acci[4][4];
+    R accr[TM][TN], acci[TM][TN];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) accr[i][j] = acci[i][j] = 0;
+        for (int j = 0; j < TN; ++j) accr[i][j] = acci[i][j] = 0;
 
     for (int k0 = kbeg; k0 < kend; k0 += GB_K) {
-        for (int e = threadIdx.x; e < GB_M * GB_K; e += 256) {
-            const int r = e / GB_K, kk = e % GB_K;
-            const int gm = m0 + r, gk = k0 + kk;
-            Acc a = cmake<Acc>(0, 0), b = cmake<Acc>(0, 0);
-            if (gm < M && gk < kend) a = load_as<Acc>(A[(size_t)gm * lda + gk]);
-            if (n0 + r < N && gk < kend) b = load_as<Acc>(B[(size_t)(n0 + r) * ldb + gk]);
-            As[kk][r] = a;
-            Bs[kk][r] = b;
+        for (int e = threadIdx.x; e < BM * GB_K; e += 256) {
+            const int r = e / GB_K, kk = e % GB_K, gk = k0 + kk;
+            As[kk][r] = (m0 + r < M && gk < kend) ? load_as<Acc>(A[(size_t)(m0 + r) * lda + gk]) : cmake<Acc>(0, 0);
+        }
+        for (int e = threadIdx.x; e < BN * GB_K; e += 256) {
+            const int r = e / GB_K, kk = e % GB_K, gk = k0 + kk;
+            Bs[kk][r] = (n0 + r < N && gk < kend) ? load_as<Acc>(B[(size_t)(n0 + r) * ldb + gk]) : cmake<Acc>(0, 0);
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < GB_K; ++kk) {
-            Acc a[4], b[4];
+            Acc a[TM], b[TN];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + 16 * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < TN; ++j) {
                     // conj(a) * b
                     accr[i][j] += a[i].x * b[j].x + a[i].y * b[j].y;
                     acci[i][j] += a[i].x * b[j].y - a[i].y * b[j].x;
@@ -72,15 +75,24 @@ __global__ void __launch_bounds__(256) proj_gemm_kernel(int M, int N, int K, con
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < TM; ++i) {
         const int m = m0 + ty + 16 * i;
         if (m >= M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < TN; ++j) {
             const int n = n0 + tx + 16 * j;
             if (n < N) part[((size_t)s * M + m) * N + n] = cmake<Acc>(accr[i][j], acci[i][j]);
         }
     }
+}
+
+static inline int tile_mult(int extent) { return extent <= 16 ? 1 : (extent <= 32 ? 2 : 4); }
+
+template <typename TA, typename TB, typename Acc, int TM, int TN>
+static void proj_launch(dim3 g, int M, int N, int K, const TA* A, size_t lda, const TB* B, size_t ldb, Acc* part,
+                        int kchunk, cudaStream_t st)
+{
+    proj_gemm_kernel<TA, TB, Acc, TM, TN><<<g, 256, 0, st>>>(M, N, K, A, lda, B, ldb, part, kchunk);
 }
 
 template <typename TA, typename TB, typename Acc>
@@ -90,9 +102,29 @@ cudaError_t launch_proj_gemm(int M, int N, int K, const TA* A, size_t lda, const
     if (M == 0 || N == 0) return cudaSuccess;
     int kchunk = ceil_div(K, nsplit);
     kchunk = ceil_div(kchunk, GB_K) * GB_K;
-    dim3 g(ceil_div(M, GB_M), ceil_div(N, GB_N), nsplit);
-    proj_gemm_kernel<TA, TB, Acc><<<g, 256, 0, st>>>(M, N, K, A, lda, B, ldb, part, kchunk);
+    const int tm = tile_mult(M), tn = tile_mult(N);
+    dim3 g(ceil_div(M, 16 * tm), ceil_div(N, 16 * tn), nsplit);
+    // nsplit partial slabs are written even when K is split finer than needed (empty chunks write zeros)
+    if (tm == 1 && tn == 1) proj_launch<TA, TB, Acc, 1, 1>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tm == 1 && tn == 2) proj_launch<TA, TB, Acc, 1, 2>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tm == 2 && tn == 1) proj_launch<TA, TB, Acc, 2, 1>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tm == 2 && tn == 2) proj_launch<TA, TB, Acc, 2, 2>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tm == 1) proj_launch<TA, TB, Acc, 1, 4>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tn == 1) proj_launch<TA, TB, Acc, 4, 1>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tm == 2) proj_launch<TA, TB, Acc, 2, 4>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else if (tn == 2) proj_launch<TA, TB, Acc, 4, 2>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
+    else proj_launch<TA, TB, Acc, 4, 4>(g, M, N, K, A, lda, B, ldb, part, kchunk, st);
     return cudaGetLastError();
+}
+
+// Split count for a projection of an M x N result over K: enough blocks for
+// every SM (two per SM), at least 64 of K per split.
+int proj_gemm_splits(int M, int N, int K)
+{
+    const int blocks = ceil_div(M, 16 * tile_mult(M)) * ceil_div(N, 16 * tile_mult(N));
+    const int want = ceil_div(2 * 152, blocks);
+    const int maxs = K / 64 > 1 ? K / 64 : 1;
+    return want < 1 ? 1 : (want < maxs ? want : maxs);
 }
 
 template <typename Acc, typename CW>
@@ -123,44 +155,44 @@ cudaError_t launch_reduce_splits(int M, int N, int nsplit, const Acc* part, cons
     return cudaGetLastError();
 }
 
-template <typename C>
+template <typename C, int TM, int TN>
 __global__ void __launch_bounds__(256) expand_gemm_kernel(int M, int N, int K, const C* __restrict__ W, size_t ldw,
                                                           const C* __restrict__ A, size_t lda,
                                                           double2* __restrict__ out, size_t ldo)
 {
-    // out[n][k] += sum_m W[m][n] * A[m][k]; block tile: 64 n x 64 k, slices of 16 m
+    // out[n][k] += sum_m W[m][n] * A[m][k]; block tile: (16 TM) n x (16 TN) k, slices of 16 m
     using R = typename Real<C>::type;
-    __shared__ C Ws[GB_K][GB_N + 1];
-    __shared__ C As[GB_K][GB_M + 1];
-    const int k0 = blockIdx.x * GB_M, n0 = blockIdx.y * GB_N;
+    constexpr int BN = 16 * TM, BK = 16 * TN;
+    __shared__ C Ws[GB_K][BN + 1];
+    __shared__ C As[GB_K][BK + 1];
+    const int k0 = blockIdx.x * BK, n0 = blockIdx.y * BN;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    R accr[4][4], acci[4][4];
+    R accr[TM][TN], acci[TM][TN];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) accr[i][j] = acci[i][j] = 0;
+        for (int j = 0; j < TN; ++j) accr[i][j] = acci[i][j] = 0;
     for (int m0 = 0; m0 < M; m0 += GB_K) {
-        for (int e = threadIdx.x; e < GB_K * GB_M; e += 256) {
-            const int mm = e / GB_M, c = e % GB_M;
-            const int gm = m0 + mm;
-            C w = cmake<C>(0, 0), a = cmake<C>(0, 0);
-            if (gm < M && n0 + c < N) w = W[(size_t)gm * ldw + n0 + c];
-            if (gm < M && k0 + c < K) a = A[(size_t)gm * lda + k0 + c];
-            Ws[mm][c] = w;
-            As[mm][c] = a;
+        for (int e = threadIdx.x; e < GB_K * BN; e += 256) {
+            const int mm = e / BN, c = e % BN, gm = m0 + mm;
+            Ws[mm][c] = (gm < M && n0 + c < N) ? W[(size_t)gm * ldw + n0 + c] : cmake<C>(0, 0);
+        }
+        for (int e = threadIdx.x; e < GB_K * BK; e += 256) {
+            const int mm = e / BK, c = e % BK, gm = m0 + mm;
+            As[mm][c] = (gm < M && k0 + c < K) ? A[(size_t)gm * lda + k0 + c] : cmake<C>(0, 0);
         }
         __syncthreads();
 #pragma unroll
         for (int mm = 0; mm < GB_K; ++mm) {
-            C w[4], a[4];
+            C w[TM], a[TN];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) w[i] = Ws[mm][ty + 16 * i];
+            for (int i = 0; i < TM; ++i) w[i] = Ws[mm][ty + 16 * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) a[j] = As[mm][tx + 16 * j];
+            for (int j = 0; j < TN; ++j) a[j] = As[mm][tx + 16 * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < TM; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < TN; ++j) {
                     accr[i][j] += w[i].x * a[j].x - w[i].y * a[j].y;
                     acci[i][j] += w[i].x * a[j].y + w[i].y * a[j].x;
                 }
@@ -168,11 +200,11 @@ __global__ void __launch_bounds__(256) expand_gemm_kernel(int M, int N, int K, c
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < TM; ++i) {
         const int n = n0 + ty + 16 * i;
         if (n >= N) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < TN; ++j) {
             const int k = k0 + tx + 16 * j;
             if (k < K) {
                 double2 o = out[(size_t)n * ldo + k];
@@ -189,8 +221,17 @@ cudaError_t launch_expand_gemm(int M, int N, int K, const C* W, size_t ldw, cons
                                size_t ldo, cudaStream_t st)
 {
     if (N == 0 || K == 0 || M == 0) return cudaSuccess;
-    dim3 g(ceil_div(K, GB_M), ceil_div(N, GB_N));
-    expand_gemm_kernel<C><<<g, 256, 0, st>>>(M, N, K, W, ldw, A, lda, out, ldo);
+    // few bands: a narrow band tile and four G-columns per thread
+    if (N <= 16) {
+        dim3 g(ceil_div(K, 64), ceil_div(N, 16));
+        expand_gemm_kernel<C, 1, 4><<<g, 256, 0, st>>>(M, N, K, W, ldw, A, lda, out, ldo);
+    } else if (N <= 32) {
+        dim3 g(ceil_div(K, 64), ceil_div(N, 32));
+        expand_gemm_kernel<C, 2, 4><<<g, 256, 0, st>>>(M, N, K, W, ldw, A, lda, out, ldo);
+    } else {
+        dim3 g(ceil_div(K, 64), ceil_div(N, 64));
+        expand_gemm_kernel<C, 4, 4><<<g, 256, 0, st>>>(M, N, K, W, ldw, A, lda, out, ldo);
+    }
     return cudaGetLastError();
 }
 

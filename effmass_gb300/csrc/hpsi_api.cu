@@ -361,13 +361,7 @@ static int ensure_proj(hpsi_ctx* c, KSlot& s, bool grad, cudaStream_t st)
     return HPSI_OK;
 }
 
-static int split_for(int M, int N, int K)
-{
-    int blocks = ceil_div(M, 64) * ceil_div(N, 64);
-    int ns = ceil_div(2 * 152 * 2, blocks);
-    int maxs = std::max(1, K / 512);
-    return std::max(1, std::min(ns, maxs));
-}
+static int split_for(int M, int N, int K) { return proj_gemm_splits(M, N, K); }
 
 // hpsi_out[nb][npw] += nonlocal(psi) using projector matrix pr (complex C)
 template <typename C, typename Acc>

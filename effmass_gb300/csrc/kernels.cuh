@@ -170,6 +170,8 @@ cudaError_t launch_assemble(int P, int npw, const ProjRow* rows, const double* b
 
 // ---- SIMT complex GEMMs (gemm.cu) -----------------------------------------
 // Projection, split over K: part[s][m][n] = sum_{k in split s} conj(A[m][k]) * B[n][k]
+// split count of a projection GEMM: every SM busy, at least 64 of K per split
+int proj_gemm_splits(int M, int N, int K);
 template <typename TA, typename TB, typename Acc>
 cudaError_t launch_proj_gemm(int M, int N, int K, const TA* A, size_t lda, const TB* B, size_t ldb, Acc* part,
                              int nsplit, cudaStream_t st);
