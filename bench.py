@@ -306,7 +306,7 @@ def run_gb300(args, rank, world, local):
     # DRAM bytes (read + write) of one launch from the ncu capture summarised in
     # profiles/ncu_full_fft_tc_sc64_nb32.md (same kernel, 32 bands per launch,
     # which is also the x pass's per-launch band chunk here)
-    ncu_traffic = {"x_pass": 58.6e6}
+    ncu_traffic = {"x_pass": 58.1e6}
     roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec != "fp64") else None
     if roof["traffic"] is not None and bound == "hbm":
         roof["algorithmic_bytes_per_launch"] = alg[dom][1] / prof[dom][1]
