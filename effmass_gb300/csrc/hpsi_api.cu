@@ -1202,6 +1202,68 @@ extern "C" int hpsi_sternheimer(hpsi_ctx* c, int kid, int nv, const double* psi_
     return HPSI_OK;
 }
 
+extern "C" int hpsi_beta_table_length(double dq, double q_max)
+{
+    if (!(dq > 0.0) || !(q_max >= 0.0)) return fail(nullptr, HPSI_ERR_BAD_ARG, "need dq > 0 and q_max >= 0");
+    return beta_table_nq(dq, q_max);
+}
+
+extern "C" int hpsi_beta_tables(int nr, const double* r_, const double* rab_, int uniform_mesh, int n_proj,
+                                const int* l_, const double* beta_, double dq, double q_max, double* beta_q,
+                                double* dbeta_q, int flags, void* stream)
+{
+    if (nr < 0 || n_proj < 0) return fail(nullptr, HPSI_ERR_BAD_ARG, "nr and n_proj must be >= 0");
+    if (!(dq > 0.0) || !(q_max >= 0.0)) return fail(nullptr, HPSI_ERR_BAD_ARG, "need dq > 0 and q_max >= 0");
+    if (n_proj == 0) return HPSI_OK;
+    if (!r_ || !rab_ || !l_ || !beta_ || !beta_q || nr == 0)
+        return fail(nullptr, HPSI_ERR_BAD_ARG, "r/rab/l/beta/beta_q NULL or nr == 0");
+    const int nq = beta_table_nq(dq, q_max);
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t tb = (size_t)n_proj * nq * sizeof(double);
+    Carver cv;
+    const size_t o_r = dev ? 0 : cv.take<double>((size_t)nr), o_rab = dev ? 0 : cv.take<double>((size_t)nr);
+    const size_t o_l = dev ? 0 : cv.take<int>((size_t)n_proj);
+    const size_t o_b = dev ? 0 : cv.take<double>((size_t)n_proj * nr);
+    const size_t o_bq = dev ? 0 : cv.take<double>((size_t)n_proj * nq);
+    const size_t o_dq = (dev || !dbeta_q) ? 0 : cv.take<double>((size_t)n_proj * nq);
+    const size_t o_nm = cv.take<int>((size_t)n_proj);
+    unsigned char* buf = nullptr;
+    cudaError_t e;
+#define TB_TRY(expr)                                                                                           \
+    do {                                                                                                        \
+        if ((e = (expr)) != cudaSuccess) {                                                                      \
+            if (buf) cudaFree(buf);                                                                             \
+            return fail(nullptr, e == cudaErrorMemoryAllocation ? HPSI_ERR_OOM : HPSI_ERR_CUDA, "%s: %s", #expr, \
+                        cudaGetErrorString(e));                                                                 \
+        }                                                                                                       \
+    } while (0)
+    TB_TRY(cudaMalloc(&buf, cv.off));
+    const double* r = dev ? r_ : reinterpret_cast<const double*>(buf + o_r);
+    const double* rab = dev ? rab_ : reinterpret_cast<const double*>(buf + o_rab);
+    const int* l = dev ? l_ : reinterpret_cast<const int*>(buf + o_l);
+    const double* beta = dev ? beta_ : reinterpret_cast<const double*>(buf + o_b);
+    double* bq = dev ? beta_q : reinterpret_cast<double*>(buf + o_bq);
+    double* dbq = dev ? dbeta_q : (dbeta_q ? reinterpret_cast<double*>(buf + o_dq) : nullptr);
+    int* nmax = reinterpret_cast<int*>(buf + o_nm);
+    if (!dev) {
+        TB_TRY(cudaMemcpyAsync((void*)r, r_, nr * sizeof(double), cudaMemcpyHostToDevice, st));
+        TB_TRY(cudaMemcpyAsync((void*)rab, rab_, nr * sizeof(double), cudaMemcpyHostToDevice, st));
+        TB_TRY(cudaMemcpyAsync((void*)l, l_, n_proj * sizeof(int), cudaMemcpyHostToDevice, st));
+        TB_TRY(cudaMemcpyAsync((void*)beta, beta_, (size_t)n_proj * nr * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    TB_TRY(launch_trim(nr, n_proj, beta, nmax, st));
+    TB_TRY(launch_beta_tables(nr, r, rab, uniform_mesh, n_proj, l, nmax, beta, dq, nq, bq, dbq, st));
+    if (!dev) {
+        TB_TRY(cudaMemcpyAsync(beta_q, bq, tb, cudaMemcpyDeviceToHost, st));
+        if (dbeta_q) TB_TRY(cudaMemcpyAsync(dbeta_q, dbq, tb, cudaMemcpyDeviceToHost, st));
+    }
+    TB_TRY(cudaStreamSynchronize(st));
+    cudaFree(buf);
+#undef TB_TRY
+    return HPSI_OK;
+}
+
 extern "C" int hpsi_density(hpsi_ctx* c, int kid, int nb, const double* psi_, const double* occ_, double* rho_,
                             int flags, void* stream)
 {

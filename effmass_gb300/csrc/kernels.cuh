@@ -247,3 +247,11 @@ cudaError_t launch_bprec(int n, int nb, const double* kin, const double* e, doub
 // out_b = active_b && den_b > 0 ? num_b / den_b : 0
 cudaError_t launch_bratio(int nb, const double* num, const double* den, const int* active, double* out,
                           cudaStream_t st);
+
+// ---- radial beta(q) / dbeta(q)/dq tables (tables.cu) -------------------------
+int beta_table_nq(double dq, double q_max);
+// nmax[p] = points of projector p after trimming its trailing zeros
+cudaError_t launch_trim(int nr, int np, const double* beta, int* nmax, cudaStream_t st);
+cudaError_t launch_beta_tables(int nr, const double* r, const double* rab, int uniform, int np, const int* l,
+                               const int* nmax, const double* beta, double dq, int nq, double* bq, double* dbq,
+                               cudaStream_t st);

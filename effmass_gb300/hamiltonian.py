@@ -314,3 +314,21 @@ def kp_sums(m, e, n_low: int, deg_tol: float = 1e-8):
     k = np.zeros(n_low, dtype=np.int32)
     check(L.hpsi_kp_sums(nb, n_low, m.ctypes.data, e.ctypes.data, deg_tol, s.ctypes.data, k.ctypes.data, 0, None))
     return s, k
+
+
+def beta_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float = 20.0, derivative: bool = True):
+    """beta(q) (and dbeta/dq) tables [n_proj][nq] of radial projectors, built on the device."""
+    L = load()
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    rab = np.ascontiguousarray(rab, dtype=np.float64)
+    l = np.ascontiguousarray(l, dtype=np.int32)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    nq = L.hpsi_beta_table_length(dq, q_max)
+    if nq < 0:
+        check(nq)
+    bq = np.zeros((beta.shape[0], nq))
+    dbq = np.zeros_like(bq) if derivative else None
+    check(L.hpsi_beta_tables(r.size, r.ctypes.data, rab.ctypes.data, int(uniform), beta.shape[0], l.ctypes.data,
+                             beta.ctypes.data, dq, q_max, bq.ctypes.data,
+                             dbq.ctypes.data if dbq is not None else None, 0, None))
+    return bq, dbq

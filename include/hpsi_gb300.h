@@ -125,6 +125,23 @@ int hpsi_dim(const hpsi_ctx* ctx, int kid);
 int hpsi_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
                int flags, void* stream);
 
+/* Radial beta(q) and dbeta/dq tables on the device: what the reference's
+ * BetaqTables / DBetaqTables compute in Hamiltonian::finalize
+ * (src/pseudo/ncpp_advance.cppm:524-641, 718-835) from the radial mesh and the
+ * projectors after its sortByL / diagonalizeNonlocal, as the input tables of
+ * hpsi_species (raw, without 1/sqrt(omega)):
+ *   beta_q[p][i]  = 4 pi Simpson[beta_p(r) r j_l(q_i r)],
+ *   dbeta_q[p][i] = 4 pi Simpson[beta_p(r) r^2 j_l'(q_i r)],   q_i = i dq,
+ * i < hpsi_beta_table_length(dq, q_max) = ceil(q_max/dq) + 4.  r, rab: nr
+ * mesh points and dr/di (uniform_mesh != 0: rab[0] is the constant step);
+ * beta: [n_proj][nr], trailing zeros trimmed per projector; l: [n_proj].
+ * dbeta_q may be NULL.  Host or device pointers per HPSI_DEVICE_PTRS; the call
+ * allocates its scratch and synchronises stream. */
+int hpsi_beta_table_length(double dq, double q_max);
+int hpsi_beta_tables(int nr, const double* r, const double* rab, int uniform_mesh, int n_proj, const int* l,
+                     const double* beta, double dq, double q_max, double* beta_q, double* dbeta_q, int flags,
+                     void* stream);
+
 /* Sternheimer equations for the k-derivative of the occupied bands (the
  * reference's roadmap item: conjugate-gradient solution of the linear
  * equations, docs/roadmap.md): for each of the nv occupied bands psi_n with

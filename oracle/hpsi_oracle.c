@@ -683,6 +683,104 @@ int oracle_density(const hpsi_system* sys, const hpsi_kpoint* kp, int nb, const 
     return HPSI_OK;
 }
 
+/* ------------------------------------------------------------------------ */
+/* beta(q) and dbeta/dq tables (src/pseudo/ncpp_advance.cppm:524-641, 718-835) */
+/* ------------------------------------------------------------------------ */
+/* j_l(x) as SphericalBesselJ produces it (src/math/sph_bessel.cppm:15-50,     */
+/* 184-210, 295-325): 0 -> delta_l0; x < 0.5 the power series; else j_0, j_1   */
+/* in closed form and the upward recurrence.                                  */
+static double ref_jl(int l, double x)
+{
+    if (x < 1e-15) return l == 0 ? 1.0 : 0.0;
+    if (x < 0.5) {
+        const double x2h = x * x / 2.0;
+        double term = 1.0, sum = 1.0;
+        for (int k = 1; k <= 50; ++k) {
+            term *= -x2h / ((double)k * (2.0 * l + 2.0 * k + 1.0));
+            sum += term;
+            if (fabs(term) < 1e-16 * fabs(sum)) break;
+        }
+        double df = 1.0;
+        for (int i = 3; i <= 2 * l + 1; i += 2) df *= i;
+        return sum * pow(x, l) / df;
+    }
+    const double j0 = sin(x) / x;
+    if (l == 0) return j0;
+    const double j1 = j0 / x - cos(x) / x;
+    double jp = j0, jc = j1;
+    for (int n = 1; n < l; ++n) {
+        const double jn = (2.0 * n + 1.0) / x * jc - jp;
+        jp = jc;
+        jc = jn;
+    }
+    return jc;
+}
+
+/* simpson (src/math/numerical.cppm:33-90): 3/8 rule on the first four points */
+/* and 1/3 on the rest for an even count                                    */
+static double ref_simpson(const double* f, const double* rab, int n, int uniform)
+{
+    if (n == 0) return 0.0;
+    if (n == 1) return f[0] * rab[0];
+    if (uniform) {
+        const double dr = rab[0];
+        if (n % 2 == 1) {
+            double sum = f[0] + f[n - 1];
+            for (int i = 1; i < n - 1; ++i) sum += (i % 2 == 0 ? 2.0 : 4.0) * f[i];
+            return dr * sum / 3.0;
+        }
+        if (n == 2) return dr * 0.5 * (f[0] + f[1]);
+        const double s38 = f[0] + 3.0 * f[1] + 3.0 * f[2] + f[3];
+        double s13 = f[3] + f[n - 1];
+        for (int i = 4; i < n - 1; ++i) s13 += (i % 2 == 0 ? 4.0 : 2.0) * f[i];
+        return dr * (3.0 / 8.0 * s38 + s13 / 3.0);
+    }
+    if (n % 2 == 1) {
+        double sum = f[0] * rab[0] + f[n - 1] * rab[n - 1];
+        for (int i = 1; i < n - 1; ++i) sum += (i % 2 == 0 ? 2.0 : 4.0) * f[i] * rab[i];
+        return sum / 3.0;
+    }
+    if (n == 2) return 0.5 * (f[0] * rab[0] + f[1] * rab[1]);
+    const double s38 = f[0] * rab[0] + 3.0 * f[1] * rab[1] + 3.0 * f[2] * rab[2] + f[3] * rab[3];
+    double s13 = f[3] * rab[3] + f[n - 1] * rab[n - 1];
+    for (int i = 4; i < n - 1; ++i) s13 += (i % 2 == 0 ? 4.0 : 2.0) * f[i] * rab[i];
+    return 3.0 / 8.0 * s38 + s13 / 3.0;
+}
+
+/* Tables on q_i = i dq, i < ceil(q_max/dq) + 4: beta_q = 4 pi S[beta r j_l(q r)], */
+/* dbeta_q = 4 pi S[beta r^2 j_l'(q r)] with j_l' = (l/x) j_l - j_{l+1}          */
+/* (j_1'(0) = 1/3, else 0 at x = 0); each projector's trailing zeros trimmed.     */
+int oracle_beta_tables(int nr, const double* r, const double* rab, int uniform, int np, const int* l,
+                       const double* beta, double dq, double q_max, double* bq, double* dbq)
+{
+    const int nq = (int)ceil(q_max / dq) + 1 + 3;
+    double* f = (double*)malloc(sizeof(double) * (nr > 0 ? nr : 1));
+    if (!f) return HPSI_ERR_OOM;
+    const double FOUR_PI = 4.0 * 3.14159265358979323846;
+    for (int p = 0; p < np; ++p) {
+        const double* b = beta + (size_t)p * nr;
+        int n = nr;
+        while (n > 0 && b[n - 1] == 0.0) --n;
+        for (int iq = 0; iq < nq; ++iq) {
+            const double q = iq * dq;
+            for (int i = 0; i < n; ++i) f[i] = b[i] * r[i] * ref_jl(l[p], q * r[i]);
+            bq[(size_t)p * nq + iq] = n ? FOUR_PI * ref_simpson(f, rab, n, uniform) : 0.0;
+            if (dbq) {
+                for (int i = 0; i < n; ++i) {
+                    const double x = q * r[i];
+                    double d;
+                    if (x < 1e-15) d = l[p] == 1 ? 1.0 / 3.0 : 0.0;
+                    else d = (double)l[p] / x * ref_jl(l[p], x) - ref_jl(l[p] + 1, x);
+                    f[i] = b[i] * r[i] * r[i] * d;
+                }
+                dbq[(size_t)p * nq + iq] = n ? FOUR_PI * ref_simpson(f, rab, n, uniform) : 0.0;
+            }
+        }
+    }
+    free(f);
+    return HPSI_OK;
+}
+
 /* 1-D transform with the pocketfft convention (test hook for the FFT KATs). */
 int oracle_fft1d(double* c, int n, int sign, double fct)
 {

@@ -46,6 +46,7 @@ def lib():
         L.oracle_grad.argtypes = [sysp, kpp, C.c_int, dp, dp, dp, dp]
         L.oracle_velocity.argtypes = [sysp, kpp, C.c_int, dp, dp]
         L.oracle_density.argtypes = [sysp, kpp, C.c_int, dp, dp, dp]
+        L.oracle_beta_tables.argtypes = [C.c_int, dp, dp, C.c_int, C.c_int, ip, dp, C.c_double, C.c_double, dp, dp]
         L.oracle_ylm.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
         L.oracle_ylm.restype = None
         L.oracle_beta_interp.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, dp]
@@ -98,6 +99,21 @@ def density(sysm, kp, psi: np.ndarray, occ, rho: np.ndarray = None) -> np.ndarra
     S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
     _check(lib().oracle_density(S.ref(), K.ref(), psi.shape[0], abi.cptr(psi), abi.cptr(occ), abi.cptr(out)))
     return out
+
+
+def beta_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float = 20.0):
+    """(beta_q, dbeta_q) [n_proj][nq] as the reference's BetaqTables / DBetaqTables build them."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    rab = np.ascontiguousarray(rab, dtype=np.float64)
+    l = np.ascontiguousarray(l, dtype=np.int32)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    nq = int(np.ceil(q_max / dq)) + 4
+    bq = np.zeros((beta.shape[0], nq))
+    dbq = np.zeros_like(bq)
+    _check(lib().oracle_beta_tables(r.size, abi.cptr(r), abi.cptr(rab), int(uniform), beta.shape[0],
+                                    l.ctypes.data_as(C.POINTER(C.c_int)), abi.cptr(beta), dq, q_max,
+                                    abi.cptr(bq), abi.cptr(dbq)))
+    return bq, dbq
 
 
 def ylm(lmax: int, theta, phi):

@@ -19,6 +19,7 @@
 // Modes:
 //   ref_driver golden <spec.bin> <out.bin> <workdir>
 //   ref_driver density <spec.bin> <occ.txt> <out.bin> <workdir>
+//   ref_driver tables <spec.bin> <out.bin> <workdir>
 //   ref_driver time   <spec.bin> <workdir> <ikpt> <band0> <nbands>
 //       (prints one JSON line with the seconds spent in H|psi> alone)
 
@@ -374,6 +375,51 @@ int timeit(const std::string& spec_path, const std::string& dir, int ik, int ban
     return 0;
 }
 
+// Radial inputs of the beta(q) / dbeta(q)/dq tables as the reference builds
+// them in Hamiltonian::finalize (src/H_psi/hamiltonian.cpp:297-316: sortByL,
+// diagonalizeNonlocal, then BetaqTables / DBetaqTables from mesh r, rab and
+// the rotated beta(r)).  Output per species: "TABREF01", z, mesh type
+// (0 uniform, 1 general), nr, r[nr], rab[nr], n_proj, then per projector l,
+// len and beta[len]; then the tables: nt, nq, beta_q[nt][nq], dbeta_q[nt][nq].
+int tables(const std::string& spec_path, const std::string& out_path, const std::string& dir) {
+    Spec s = readSpec(spec_path);
+    setup(s, dir);
+    Hamiltonian H(dir);
+    load(H, s, true);
+    std::FILE* f = std::fopen(out_path.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot write " + out_path);
+    Out O{f};
+    O.arr("TABREF01", 8);
+    O.put(static_cast<int>(s.species.size()));
+    for (auto& sp : s.species) {
+        const auto& ncp = H.ncpp(sp.z);
+        O.put(sp.z);
+        O.put(ncp.mesh.type == MeshType::Uniform ? 0 : 1);
+        const int nr = static_cast<int>(ncp.mesh.r.size());
+        O.put(nr);
+        O.arr(ncp.mesh.r.data(), nr);
+        O.arr(ncp.mesh.rab.data(), nr);
+        const int np = static_cast<int>(ncp.nonlocal.beta.size());
+        O.put(np);
+        for (int i = 0; i < np; ++i) {
+            O.put(ncp.nonlocal.angular_momentum[i]);
+            const int len = static_cast<int>(ncp.nonlocal.beta[i].size());
+            O.put(len);
+            O.arr(ncp.nonlocal.beta[i].data(), len);
+        }
+        const auto& bt = H.betaqTables(sp.z);
+        const auto& dbt = H.dbetaqTables(sp.z);
+        const int nt = static_cast<int>(bt.tables_.size());
+        const int nq = nt ? static_cast<int>(bt.tables_[0].values.size()) : 0;
+        O.put(nt);
+        O.put(nq);
+        for (int t = 0; t < nt; ++t) O.arr(bt.tables_[t].values.data(), nq);
+        for (int t = 0; t < nt; ++t) O.arr(dbt.tables_[t].values.data(), nq);
+    }
+    std::fclose(f);
+    return 0;
+}
+
 // Charge density through the reference's own buildDensity
 // (src/support/density.cppm:41-94): the spec's k-points and bands, occupations
 // read from occ_path (nkpt*nband whitespace-separated values, k-point major)
@@ -455,6 +501,7 @@ int main(int argc, char** argv) {
     try {
         std::string mode = argc > 1 ? argv[1] : "";
         if (mode == "golden" && argc == 5) return refdrv::golden(argv[2], argv[3], argv[4]);
+        if (mode == "tables" && argc == 5) return refdrv::tables(argv[2], argv[3], argv[4]);
         if (mode == "density" && argc == 6) return refdrv::density(argv[2], argv[3], argv[4], argv[5]);
         if (mode == "time" && argc == 7)
             return refdrv::timeit(argv[2], argv[3], std::atoi(argv[4]), std::atoi(argv[5]), std::atoi(argv[6]));

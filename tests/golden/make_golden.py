@@ -43,6 +43,40 @@ CASES = {
 }
 
 
+def read_tables(path):
+    """The first species of a TABREF01 file: mesh, rotated beta(r) and the tables."""
+    raw = open(path, "rb").read()
+    assert raw[:8] == b"TABREF01"
+    o = 8
+
+    def ints(n):
+        nonlocal o
+        v = np.frombuffer(raw, dtype=np.int32, count=n, offset=o)
+        o += 4 * n
+        return v
+
+    def dbl(n):
+        nonlocal o
+        v = np.frombuffer(raw, dtype=np.float64, count=n, offset=o).copy()
+        o += 8 * n
+        return v
+
+    ints(1)  # species count
+    _z, mtype, nr = ints(3)
+    r, rab = dbl(nr), dbl(nr)
+    (np_,) = ints(1)
+    ls, betas = [], np.zeros((np_, nr))
+    for i in range(np_):
+        l, ln = ints(2)
+        ls.append(l)
+        betas[i, :ln] = dbl(ln)
+    nt, nq = ints(2)
+    bq = dbl(nt * nq).reshape(nt, nq)
+    dbq = dbl(nt * nq).reshape(nt, nq)
+    return dict(uniform=int(mtype == 0), r=r, rab=rab, l=np.array(ls, dtype=np.int32), beta=betas,
+                beta_q=bq, dbeta_q=dbq)
+
+
 def make_case(name, sysname, kf, nb, grid):
     sysm = S.make_system(sysname)
     if grid is not None:
@@ -65,6 +99,11 @@ def make_case(name, sysname, kf, nb, grid):
         np.savetxt(occ_txt, occ, fmt="%.17g")
         subprocess.run([O.REF_DRIVER, "density", spec, occ_txt, rho_bin, os.path.join(td, "wd2")], check=True,
                        stderr=subprocess.DEVNULL)
+        # the radial inputs the reference integrated into its beta / dbeta tables
+        tab_bin = os.path.join(td, "tab.bin")
+        subprocess.run([O.REF_DRIVER, "tables", spec, tab_bin, os.path.join(td, "wd3")], check=True,
+                       stderr=subprocess.DEVNULL)
+        rad = read_tables(tab_bin)
         raw = open(rho_bin, "rb").read()
         assert raw[:8] == b"RHOREF01"
         dims = np.frombuffer(raw[8:20], dtype=np.int32)
@@ -80,7 +119,11 @@ def make_case(name, sysname, kf, nb, grid):
         sp_beta_q=sp["beta_q"], sp_dbeta_q=sp["dbeta_q"],
         k_frac=gk["k_frac"], g_idx=gk["g_idx"], kvec=gk["kvec"], kinetic=gk["kinetic"],
         q=gk["q"], theta=gk["theta"], phi=gk["phi"],
-        psi=psi, hpsi=gk["hpsi"], grad=gk["grad"], occ=occ, rho=rho)
+        psi=psi, hpsi=gk["hpsi"], grad=gk["grad"], occ=occ, rho=rho,
+        rad_uniform=np.array(rad["uniform"]), rad_r=rad["r"], rad_rab=rad["rab"], rad_l=rad["l"],
+        rad_beta=rad["beta"])
+    # the tables of the tables mode are the same the golden mode exported
+    assert np.array_equal(rad["beta_q"], sp["beta_q"]) and np.array_equal(rad["dbeta_q"], sp["dbeta_q"])
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     return kp.npw
 

@@ -45,6 +45,18 @@ def test_oracle_matches_reference_density(oracle_lib, case):
     assert rel_err(rho, z["rho"]) <= 1e-14, rel_err(rho, z["rho"])
 
 
+@pytest.mark.parametrize("case", ["tiny", "tinyd"])
+def test_oracle_beta_tables_match_reference(oracle_lib, case):
+    """beta(q) and dbeta/dq tables built from the radial projectors the reference
+    integrated (after its sortByL / diagonalizeNonlocal), against its own tables."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{case}.npz"))
+    bq, dbq = oracle_lib.beta_tables(z["rad_r"], z["rad_rab"], bool(z["rad_uniform"]), z["rad_l"], z["rad_beta"],
+                                     float(z["sp_dq"]), float(z["sp_q_max"]))
+    assert bq.shape == z["sp_beta_q"].shape
+    # the same operations in the same order: bit for bit
+    assert np.array_equal(bq, z["sp_beta_q"]) and np.array_equal(dbq, z["sp_dbeta_q"])
+
+
 @pytest.mark.parametrize("case", ["tiny", "tinyd", "fcc2"])
 def test_oracle_spherical_coordinates_match_reference(oracle_lib, case):
     import os
