@@ -1264,6 +1264,72 @@ extern "C" int hpsi_beta_tables(int nr, const double* r_, const double* rab_, in
     return HPSI_OK;
 }
 
+extern "C" int hpsi_gsphere(const double* lattice, const double* k_frac, double ecut, int max_npw, int* g_idx,
+                            double* kvec, double* kinetic, int* npw_out, int flags, void* stream)
+{
+    if (!lattice || !k_frac || !npw_out) return fail(nullptr, HPSI_ERR_BAD_ARG, "lattice/k_frac/npw_out NULL");
+    if (!(ecut > 0.0)) return fail(nullptr, HPSI_ERR_BAD_ARG, "ecut must be > 0");
+    // B = 2 pi A^-T (rows = reciprocal vectors), by the adjugate
+    const double* A = lattice;
+    const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                       A[2] * (A[3] * A[7] - A[4] * A[6]);
+    if (!(std::fabs(det) > 0.0)) return fail(nullptr, HPSI_ERR_BAD_ARG, "singular lattice");
+    const double tp = 2.0 * 3.14159265358979323846 / det;
+    double B[9];
+    B[0] = tp * (A[4] * A[8] - A[5] * A[7]); B[1] = tp * (A[5] * A[6] - A[3] * A[8]); B[2] = tp * (A[3] * A[7] - A[4] * A[6]);
+    B[3] = tp * (A[2] * A[7] - A[1] * A[8]); B[4] = tp * (A[0] * A[8] - A[2] * A[6]); B[5] = tp * (A[1] * A[6] - A[0] * A[7]);
+    B[6] = tp * (A[1] * A[5] - A[2] * A[4]); B[7] = tp * (A[2] * A[3] - A[0] * A[5]); B[8] = tp * (A[0] * A[4] - A[1] * A[3]);
+    // box half-width: sqrt(2 ecut) over the shortest reciprocal vector, twice, plus margin
+    double bmin = 1e300;
+    for (int d = 0; d < 3; ++d)
+        bmin = std::min(bmin, std::sqrt(B[3 * d] * B[3 * d] + B[3 * d + 1] * B[3 * d + 1] + B[3 * d + 2] * B[3 * d + 2]));
+    const int gmax = (int)std::ceil(std::sqrt(2.0 * ecut) / bmin * 2.0) + 2;
+    if (gmax > 512) return fail(nullptr, HPSI_ERR_BAD_ARG, "ecut too large for the G box (gmax %d)", gmax);
+    const int L = 2 * gmax + 1;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    int* cnt = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&cnt, 2 * L * sizeof(int))))
+        return fail(nullptr, HPSI_ERR_OOM, "cudaMalloc: %s", cudaGetErrorString(e));
+    std::vector<int> h(L), off(L);
+    auto done = [&](int code) { cudaFree(cnt); return code; };
+    if ((e = launch_gs_count(B, k_frac, ecut, gmax, cnt, st)) ||
+        (e = cudaMemcpyAsync(h.data(), cnt, L * sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st)))
+        return done(fail(nullptr, HPSI_ERR_CUDA, "G-sphere count: %s", cudaGetErrorString(e)));
+    long npw = 0;
+    for (int i = 0; i < L; ++i) { off[i] = (int)npw; npw += h[i]; }
+    *npw_out = (int)npw;
+    if (!g_idx || !kvec || !kinetic) return done(HPSI_OK);  // size query
+    if (npw > max_npw) return done(fail(nullptr, HPSI_ERR_RANGE, "G-sphere holds %ld vectors, room for %d", npw, max_npw));
+    int *dg = g_idx;
+    double *dk = kvec, *dkin = kinetic;
+    unsigned char* buf = nullptr;
+    if (!dev) {
+        if ((e = cudaMalloc(&buf, (size_t)npw * (3 * sizeof(int) + 4 * sizeof(double)) + 64)))
+            return done(fail(nullptr, HPSI_ERR_OOM, "cudaMalloc: %s", cudaGetErrorString(e)));
+        dk = reinterpret_cast<double*>(buf);
+        dkin = dk + 3 * npw;
+        dg = reinterpret_cast<int*>(dkin + npw);
+    }
+    if ((e = cudaMemcpyAsync(cnt + L, off.data(), L * sizeof(int), cudaMemcpyHostToDevice, st)) ||
+        (e = launch_gs_write(B, k_frac, ecut, gmax, cnt + L, dg, dk, dkin, st)))
+        goto cuda_fail;
+    if (!dev) {
+        if ((e = cudaMemcpyAsync(g_idx, dg, npw * 3 * sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaMemcpyAsync(kvec, dk, npw * 3 * sizeof(double), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaMemcpyAsync(kinetic, dkin, npw * sizeof(double), cudaMemcpyDeviceToHost, st)))
+            goto cuda_fail;
+    }
+    if ((e = cudaStreamSynchronize(st))) goto cuda_fail;
+    if (buf) cudaFree(buf);
+    return done(HPSI_OK);
+cuda_fail:
+    if (buf) cudaFree(buf);
+    return done(fail(nullptr, HPSI_ERR_CUDA, "G-sphere write: %s", cudaGetErrorString(e)));
+}
+
 extern "C" int hpsi_density(hpsi_ctx* c, int kid, int nb, const double* psi_, const double* occ_, double* rho_,
                             int flags, void* stream)
 {

@@ -255,3 +255,8 @@ cudaError_t launch_trim(int nr, int np, const double* beta, int* nmax, cudaStrea
 cudaError_t launch_beta_tables(int nr, const double* r, const double* rab, int uniform, int np, const int* l,
                                const int* nmax, const double* beta, double dq, int nq, double* bq, double* dbq,
                                cudaStream_t st);
+// G-sphere of a k-point: counts per g1-plane, then the points in (g1, g2, g3) order
+// (B: reciprocal vectors as rows, host array; kf: k in reciprocal coordinates, host)
+cudaError_t launch_gs_count(const double* B, const double* kf, double ecut, int gmax, int* counts, cudaStream_t st);
+cudaError_t launch_gs_write(const double* B, const double* kf, double ecut, int gmax, const int* offsets, int* g,
+                            double* kvec, double* kinetic, cudaStream_t st);

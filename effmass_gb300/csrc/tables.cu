@@ -141,3 +141,110 @@ cudaError_t launch_beta_tables(int nr, const double* r, const double* rab, int u
     beta_table_kernel<<<dim3(nq, np), 128, 0, st>>>(nr, r, rab, uniform, l, nmax, beta, dq, nq, bq, dbq);
     return cudaGetLastError();
 }
+
+// ---- G-sphere of a k-point on the device (hpsi_gsphere) ----------------------
+// All integer G in the box |g_d| <= gmax with |k+G|^2/2 < ecut, K = (k+g) B
+// (B rows = reciprocal vectors), in lexicographic (g1, g2, g3) order: a count
+// pass per g1-plane, then one block per plane writes its points in order
+// with a block-wide prefix over (g2, g3).
+namespace {
+
+struct GsArgs {
+    double B[9];
+    double kf[3];
+    double ecut;
+    int gmax;
+};
+
+__device__ __forceinline__ void gs_point(const GsArgs& a, int g1, int g2, int g3, double* K, double* kin)
+{
+    const double f0 = g1 + a.kf[0], f1 = g2 + a.kf[1], f2 = g3 + a.kf[2];
+    K[0] = f0 * a.B[0] + f1 * a.B[3] + f2 * a.B[6];
+    K[1] = f0 * a.B[1] + f1 * a.B[4] + f2 * a.B[7];
+    K[2] = f0 * a.B[2] + f1 * a.B[5] + f2 * a.B[8];
+    *kin = 0.5 * (K[0] * K[0] + K[1] * K[1] + K[2] * K[2]);
+}
+
+__global__ void __launch_bounds__(256) gs_count_kernel(GsArgs a, int* __restrict__ counts)
+{
+    __shared__ int red[8];
+    const int L = 2 * a.gmax + 1, g1 = (int)blockIdx.x - a.gmax;
+    int c = 0;
+    for (int p = threadIdx.x; p < L * L; p += blockDim.x) {
+        double K[3], kin;
+        gs_point(a, g1, p / L - a.gmax, p % L - a.gmax, K, &kin);
+        c += kin < a.ecut;
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int w = 0; w < 8; ++w) s += red[w];
+        counts[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(256) gs_write_kernel(GsArgs a, const int* __restrict__ offsets, int* __restrict__ g,
+                                                       double* __restrict__ kvec, double* __restrict__ kinetic)
+{
+    __shared__ int wsum[8];
+    __shared__ int base;
+    const int L = 2 * a.gmax + 1, g1 = (int)blockIdx.x - a.gmax;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) base = offsets[blockIdx.x];
+    __syncthreads();
+    for (int p0 = 0; p0 < L * L; p0 += blockDim.x) {
+        const int p = p0 + threadIdx.x;
+        double K[3], kin = 0.0;
+        bool in = false;
+        if (p < L * L) {
+            gs_point(a, g1, p / L - a.gmax, p % L - a.gmax, K, &kin);
+            in = kin < a.ecut;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, in);
+        if (lane == 0) wsum[warp] = __popc(m);
+        __syncthreads();
+        int before = base;
+        for (int w = 0; w < warp; ++w) before += wsum[w];
+        if (in) {
+            const int pos = before + __popc(m & ((1u << lane) - 1u));
+            g[3 * pos] = g1;
+            g[3 * pos + 1] = p / L - a.gmax;
+            g[3 * pos + 2] = p % L - a.gmax;
+            kvec[3 * pos] = K[0];
+            kvec[3 * pos + 1] = K[1];
+            kvec[3 * pos + 2] = K[2];
+            kinetic[pos] = kin;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int w = 0; w < 8; ++w) base += wsum[w];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_gs_count(const double* B, const double* kf, double ecut, int gmax, int* counts, cudaStream_t st)
+{
+    GsArgs a;
+    for (int i = 0; i < 9; ++i) a.B[i] = B[i];
+    for (int i = 0; i < 3; ++i) a.kf[i] = kf[i];
+    a.ecut = ecut;
+    a.gmax = gmax;
+    gs_count_kernel<<<2 * gmax + 1, 256, 0, st>>>(a, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gs_write(const double* B, const double* kf, double ecut, int gmax, const int* offsets, int* g,
+                            double* kvec, double* kinetic, cudaStream_t st)
+{
+    GsArgs a;
+    for (int i = 0; i < 9; ++i) a.B[i] = B[i];
+    for (int i = 0; i < 3; ++i) a.kf[i] = kf[i];
+    a.ecut = ecut;
+    a.gmax = gmax;
+    gs_write_kernel<<<2 * gmax + 1, 256, 0, st>>>(a, offsets, g, kvec, kinetic);
+    return cudaGetLastError();
+}

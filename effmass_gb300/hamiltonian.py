@@ -332,3 +332,20 @@ def beta_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float =
                              beta.ctypes.data, dq, q_max, bq.ctypes.data,
                              dbq.ctypes.data if dbq is not None else None, 0, None))
     return bq, dbq
+
+
+def gsphere(lattice, k_frac, ecut: float):
+    """The k-point's G-sphere generated on the device, (g1, g2, g3) order: a system.KPoint."""
+    from .system import KPoint
+    L = load()
+    A = np.ascontiguousarray(lattice, dtype=np.float64).reshape(9)
+    kf = np.ascontiguousarray(k_frac, dtype=np.float64).reshape(3)
+    dp = C.POINTER(C.c_double)
+    n = C.c_int()
+    check(L.hpsi_gsphere(A.ctypes.data_as(dp), kf.ctypes.data_as(dp), ecut, 0, None, None, None, C.byref(n), 0, None))
+    g = np.zeros((n.value, 3), dtype=np.int32)
+    K = np.zeros((n.value, 3))
+    kin = np.zeros(n.value)
+    check(L.hpsi_gsphere(A.ctypes.data_as(dp), kf.ctypes.data_as(dp), ecut, n.value, g.ctypes.data, K.ctypes.data,
+                         kin.ctypes.data, C.byref(n), 0, None))
+    return KPoint(npw=n.value, k_frac=kf.copy(), g_idx=g, kvec=K, kinetic=kin)

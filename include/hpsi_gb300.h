@@ -142,6 +142,17 @@ int hpsi_beta_tables(int nr, const double* r, const double* rab, int uniform_mes
                      const double* beta, double dq, double q_max, double* beta_q, double* dbeta_q, int flags,
                      void* stream);
 
+/* G-sphere of a k-point generated on the device: every integer G with
+ * |k+G|^2/2 < ecut (Ha), K = (k_frac + g) B with B = 2 pi A^-T (A rows =
+ * lattice vectors, bohr), in lexicographic (g1, g2, g3) order, as the
+ * hpsi_kpoint arrays g_idx [npw][3], kvec [npw][3], kinetic [npw].  The
+ * reference reads these from OUT.GKK (src/io/GKK.cppm:511-593); here they
+ * need no host enumeration.  With g_idx/kvec/kinetic NULL the call only
+ * stores the count in *npw_out; a count above max_npw is HPSI_ERR_RANGE.
+ * Output arrays host or device per HPSI_DEVICE_PTRS; synchronises stream. */
+int hpsi_gsphere(const double* lattice, const double* k_frac, double ecut, int max_npw, int* g_idx,
+                 double* kvec, double* kinetic, int* npw_out, int flags, void* stream);
+
 /* Sternheimer equations for the k-derivative of the occupied bands (the
  * reference's roadmap item: conjugate-gradient solution of the linear
  * equations, docs/roadmap.md): for each of the nv occupied bands psi_n with
