@@ -15,7 +15,8 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhpsi_gb3
 
 # every entry point declared in include/hpsi_gb300.h
 EXPORTS = ["hpsi_abi_version", "hpsi_ctx_create", "hpsi_ctx_destroy", "hpsi_set_kpoint", "hpsi_dim",
-           "hpsi_apply", "hpsi_apply_energies", "hpsi_density", "hpsi_sternheimer", "hpsi_kp_sums", "hpsi_beta_table_length", "hpsi_beta_tables", "hpsi_gsphere", "hpsi_grad_apply", "hpsi_velocity_matrix", "hpsi_profile", "hpsi_profile_read",
+           "hpsi_apply", "hpsi_apply_energies", "hpsi_density", "hpsi_sternheimer", "hpsi_kp_sums", "hpsi_beta_table_length", "hpsi_beta_tables", "hpsi_gsphere", "hpsi_hessian_tables",
+           "hpsi_set_hessian_tables", "hpsi_hess_apply", "hpsi_grad_apply", "hpsi_velocity_matrix", "hpsi_profile", "hpsi_profile_read",
            "hpsi_apply_noalloc", "hpsi_server_create", "hpsi_server_submit", "hpsi_server_wait",
            "hpsi_server_stats", "hpsi_server_destroy", "hpsi_server_last_error", "hpsi_batch_create",
            "hpsi_batch_buffers", "hpsi_batch_offset", "hpsi_batch_run", "hpsi_batch_apply", "hpsi_batch_info",
@@ -57,6 +58,10 @@ def load():
                                    C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     L.hpsi_gsphere.argtypes = [dp, dp, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
                                C.c_int, C.c_void_p]
+    L.hpsi_hessian_tables.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                      C.c_double, C.c_double, C.c_void_p, C.c_int, C.c_void_p]
+    L.hpsi_set_hessian_tables.argtypes = [ctxp, C.c_int, C.c_int, C.c_double, dp]
+    L.hpsi_hess_apply.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p] + [C.c_void_p] * 6 + [C.c_int, C.c_void_p]
     L.hpsi_kp_sums.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
                                C.c_int, C.c_void_p]
     L.hpsi_grad_apply.argtypes = [ctxp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -43,6 +43,8 @@ struct KSlot {
     unsigned char* tcg_mem = nullptr;
     TcOperand tcg_proj, tcg_exp[3];
     long gen = 0;                  // binding generation: changes when the slot is rebound
+    double2* hess64 = nullptr;     // projector second derivatives [6][P][npw] (Hessian), per precision
+    float2* hess32 = nullptr;
 };
 
 template <typename T>
@@ -64,7 +66,7 @@ inline void slot_free(KSlot& s)
 {
     dfree(s.d_kin); dfree(s.d_kvec); dfree(s.d_g); dfree(s.d_q); dfree(s.d_trig); dfree(s.d_ylm);
     dfree(s.d_beta); dfree(s.d_dbeta0); dfree(s.d_sf); dfree(s.d_plane); dfree(s.d_rows); dfree(s.d_lam);
-    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem); dfree(s.tcg_mem);
+    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem); dfree(s.tcg_mem); dfree(s.hess64); dfree(s.hess32);
     s = KSlot();
 }
 
@@ -91,6 +93,10 @@ struct hpsi_ctx {
     Prof prof;
     int* d_err = nullptr;         // device-side error flag of the bounded waits (tcgen05 GEMMs)
     long gen_counter = 0;         // source of KSlot::gen
+    double* d_hess = nullptr;     // Hessian radial tables [nrad][3][hess_nq] (F0, F1, F3), raw
+    int hess_nq = 0;
+    double hess_dq = 0.0;
+    std::vector<char> hess_set;   // per radial function: tables given
     std::string err;
 };
 

@@ -37,7 +37,7 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     cudaSetDevice(c->dev);
     for (auto& kv : c->slots) slot_free(kv.second);
     dfree(c->d_tables); dfree(c->d_rad_nq); dfree(c->d_rad_dq); dfree(c->d_tau); dfree(c->d_v64); dfree(c->d_v32);
-    dfree(c->d_tw64); dfree(c->d_tw32); dfree(c->d_err);
+    dfree(c->d_tw64); dfree(c->d_tw32); dfree(c->d_err); dfree(c->d_hess);
     if (c->ws) cudaFree(c->ws);
     for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof.pool) cudaEventDestroy(e);
@@ -1328,6 +1328,194 @@ extern "C" int hpsi_gsphere(const double* lattice, const double* k_frac, double 
 cuda_fail:
     if (buf) cudaFree(buf);
     return done(fail(nullptr, HPSI_ERR_CUDA, "G-sphere write: %s", cudaGetErrorString(e)));
+}
+
+// ------------------------------------------------------------------- Hessian
+extern "C" int hpsi_hessian_tables(int nr, const double* r_, const double* rab_, int uniform_mesh, int n_proj,
+                                   const int* l_, const double* beta_, double dq, double q_max, double* f_out,
+                                   int flags, void* stream)
+{
+    if (nr <= 0 || n_proj < 0) return fail(nullptr, HPSI_ERR_BAD_ARG, "need nr > 0 and n_proj >= 0");
+    if (!(dq > 0.0) || !(q_max >= 0.0)) return fail(nullptr, HPSI_ERR_BAD_ARG, "need dq > 0 and q_max >= 0");
+    if (n_proj == 0) return HPSI_OK;
+    if (!r_ || !rab_ || !l_ || !beta_ || !f_out) return fail(nullptr, HPSI_ERR_BAD_ARG, "NULL argument");
+    for (int p = 0; p < n_proj && !(flags & HPSI_DEVICE_PTRS); ++p)
+        if (l_[p] < 0 || l_[p] > HPSI_LMAX) return fail(nullptr, HPSI_ERR_BAD_ARG, "l outside [0, %d]", HPSI_LMAX);
+    const int nq = beta_table_nq(dq, q_max);
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    Carver cv;
+    const size_t o_r = dev ? 0 : cv.take<double>((size_t)nr), o_rab = dev ? 0 : cv.take<double>((size_t)nr);
+    const size_t o_l = dev ? 0 : cv.take<int>((size_t)n_proj);
+    const size_t o_b = dev ? 0 : cv.take<double>((size_t)n_proj * nr);
+    const size_t o_f = dev ? 0 : cv.take<double>((size_t)3 * n_proj * nq);
+    const size_t o_nm = cv.take<int>((size_t)n_proj);
+    unsigned char* buf = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&buf, cv.off))) return fail(nullptr, HPSI_ERR_OOM, "cudaMalloc: %s", cudaGetErrorString(e));
+    const double* r = dev ? r_ : reinterpret_cast<const double*>(buf + o_r);
+    const double* rab = dev ? rab_ : reinterpret_cast<const double*>(buf + o_rab);
+    const int* l = dev ? l_ : reinterpret_cast<const int*>(buf + o_l);
+    const double* beta = dev ? beta_ : reinterpret_cast<const double*>(buf + o_b);
+    double* f = dev ? f_out : reinterpret_cast<double*>(buf + o_f);
+    int* nmax = reinterpret_cast<int*>(buf + o_nm);
+    if (!dev) {
+        if ((e = cudaMemcpyAsync((void*)r, r_, nr * sizeof(double), cudaMemcpyHostToDevice, st)) ||
+            (e = cudaMemcpyAsync((void*)rab, rab_, nr * sizeof(double), cudaMemcpyHostToDevice, st)) ||
+            (e = cudaMemcpyAsync((void*)l, l_, n_proj * sizeof(int), cudaMemcpyHostToDevice, st)) ||
+            (e = cudaMemcpyAsync((void*)beta, beta_, (size_t)n_proj * nr * sizeof(double), cudaMemcpyHostToDevice, st)))
+            goto fail_cuda;
+    }
+    if ((e = launch_trim(nr, n_proj, beta, nmax, st)) ||
+        (e = launch_hess_tables(nr, r, rab, uniform_mesh, n_proj, l, nmax, beta, dq, nq, f, st)))
+        goto fail_cuda;
+    if (!dev && (e = cudaMemcpyAsync(f_out, f, (size_t)3 * n_proj * nq * sizeof(double), cudaMemcpyDeviceToHost, st)))
+        goto fail_cuda;
+    if ((e = cudaStreamSynchronize(st))) goto fail_cuda;
+    cudaFree(buf);
+    return HPSI_OK;
+fail_cuda:
+    cudaFree(buf);
+    return fail(nullptr, HPSI_ERR_CUDA, "Hessian tables: %s", cudaGetErrorString(e));
+}
+
+extern "C" int hpsi_set_hessian_tables(hpsi_ctx* c, int species, int nq, double dq, const double* f)
+{
+    if (!c) return HPSI_ERR_BAD_ARG;
+    const int nsp = (int)c->rad_off.size();
+    if (species < 0 || species >= nsp) return fail(c, HPSI_ERR_BAD_ARG, "species %d outside [0, %d)", species, nsp);
+    if (nq < 4 || !(dq > 0.0) || !f) return fail(c, HPSI_ERR_BAD_ARG, "need nq >= 4, dq > 0 and tables");
+    if (c->d_hess && (nq != c->hess_nq || dq != c->hess_dq))
+        return fail(c, HPSI_ERR_BAD_ARG, "all species need the same table grid (nq %d, dq %g)", c->hess_nq, c->hess_dq);
+    CUDA_TRY(c, cudaSetDevice(c->dev));
+    if (!c->d_hess) {
+        CUDA_TRY(c, dalloc(&c->d_hess, (size_t)std::max(c->nrad, 1) * 3 * nq));
+        CUDA_TRY(c, cudaMemset(c->d_hess, 0, (size_t)std::max(c->nrad, 1) * 3 * nq * sizeof(double)));
+        c->hess_nq = nq;
+        c->hess_dq = dq;
+        c->hess_set.assign(c->nrad, 0);
+    }
+    const int r0 = c->rad_off[species];
+    const int r1 = species + 1 < nsp ? c->rad_off[species + 1] : c->nrad;
+    const int np = r1 - r0;
+    // input [3][np][nq] -> stored [rad][3][nq]
+    std::vector<double> rows((size_t)np * 3 * nq);
+    for (int p = 0; p < np; ++p)
+        for (int t = 0; t < 3; ++t)
+            std::memcpy(&rows[((size_t)p * 3 + t) * nq], f + ((size_t)t * np + p) * nq, nq * sizeof(double));
+    CUDA_TRY(c, cudaMemcpy(c->d_hess + (size_t)r0 * 3 * nq, rows.data(), rows.size() * sizeof(double),
+                           cudaMemcpyHostToDevice));
+    for (int r = r0; r < r1; ++r) c->hess_set[r] = 1;
+    // slots bound before: their second-derivative rows are rebuilt on next use
+    for (auto& kv : c->slots) { dfree(kv.second.hess64); dfree(kv.second.hess32); }
+    return HPSI_OK;
+}
+
+template <typename C>
+static int ensure_hess(hpsi_ctx* c, KSlot& s, cudaStream_t st)
+{
+    C*& d2 = std::is_same<C, double2>::value ? reinterpret_cast<C*&>(s.hess64) : reinterpret_cast<C*&>(s.hess32);
+    if (d2 || s.P == 0 || s.npw == 0) return HPSI_OK;
+    for (int r = 0; r < c->nrad; ++r)
+        if (std::fabs(c->rad_lam[r]) >= 1e-15 && (c->hess_set.empty() || !c->hess_set[r]))
+            return fail(c, HPSI_ERR_STATE, "Hessian tables missing for radial function %d (hpsi_set_hessian_tables)", r);
+    // q range of the tables
+    const double qtop = c->hess_dq * (c->hess_nq - 3);
+    std::vector<double> q(s.npw);
+    CUDA_TRY(c, cudaMemcpy(q.data(), s.d_q, s.npw * sizeof(double), cudaMemcpyDeviceToHost));
+    for (double v : q)
+        if (v > qtop) return fail(c, HPSI_ERR_RANGE, "q=%.17g beyond the Hessian tables (%.17g)", v, qtop);
+    CUDA_TRY(c, dalloc(&d2, (size_t)6 * s.P * s.npw));
+    CUDA_TRY(c, launch_hess_assemble<C>(s.P, s.npw, s.d_rows, c->d_hess, c->hess_nq, c->hess_dq,
+                                        1.0 / std::sqrt(c->omega), s.d_kvec, s.d_sf, d2, st));
+    return HPSI_OK;
+}
+
+// out_c += d2H/dk_a dk_b psi for the requested components c (device pointers)
+template <typename C, typename Acc>
+static int hess_device(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* out[6], unsigned char* ws,
+                       const C* pr, const C* d2, cudaStream_t st)
+{
+    static const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+    const size_t nel = (size_t)nb * s.npw;
+    for (int k = 0; k < 6; ++k)
+        if (out[k] && pa[k] == pb[k]) CUDA_TRY(c, launch_add(nel, psi, out[k], st));  // kinetic: delta_ab
+    if (s.P == 0 || nb == 0) return HPSI_OK;
+    const int P = s.P, ns = split_for(6 * P, nb, s.npw), ns4 = split_for(4 * P, nb, s.npw);
+    Carver cv;
+    Acc* part = reinterpret_cast<Acc*>(ws + cv.take<Acc>(std::max((size_t)ns * 6, (size_t)ns4 * 4) * P * nb));
+    C* W4 = reinterpret_cast<C*>(ws + cv.take<C>((size_t)4 * P * nb));   // lambda <p|psi>, lambda <d_a p|psi>
+    C* W6 = reinterpret_cast<C*>(ws + cv.take<C>((size_t)6 * P * nb));   // lambda <d_ab p|psi>
+    CUDA_TRY(c, (launch_proj_gemm<C, double2, Acc>(4 * P, nb, s.npw, pr, (size_t)s.npw, psi, (size_t)s.npw, part, ns4,
+                                                   st)));
+    CUDA_TRY(c, (launch_reduce_splits<Acc, C>(4 * P, nb, ns4, part, s.d_lam, P, W4, (size_t)nb, st)));
+    CUDA_TRY(c, (launch_proj_gemm<C, double2, Acc>(6 * P, nb, s.npw, d2, (size_t)s.npw, psi, (size_t)s.npw, part, ns,
+                                                   st)));
+    CUDA_TRY(c, (launch_reduce_splits<Acc, C>(6 * P, nb, ns, part, s.d_lam, P, W6, (size_t)nb, st)));
+    const size_t PN = (size_t)P * s.npw, PB = (size_t)P * nb;
+    for (int k = 0; k < 6; ++k) {
+        if (!out[k]) continue;
+        const int a = pa[k], b = pb[k];
+        // |d_ab p> lambda <p|psi> + |d_a p> lambda <d_b p|psi> + |d_b p> lambda <d_a p|psi> + |p> lambda <d_ab p|psi>
+        CUDA_TRY(c, launch_expand_gemm<C>(P, nb, s.npw, W4, (size_t)nb, d2 + k * PN, (size_t)s.npw, out[k],
+                                          (size_t)s.npw, st));
+        CUDA_TRY(c, launch_expand_gemm<C>(P, nb, s.npw, W4 + (1 + b) * PB, (size_t)nb, pr + (1 + a) * PN,
+                                          (size_t)s.npw, out[k], (size_t)s.npw, st));
+        CUDA_TRY(c, launch_expand_gemm<C>(P, nb, s.npw, W4 + (1 + a) * PB, (size_t)nb, pr + (1 + b) * PN,
+                                          (size_t)s.npw, out[k], (size_t)s.npw, st));
+        CUDA_TRY(c, launch_expand_gemm<C>(P, nb, s.npw, W6 + k * PB, (size_t)nb, pr, (size_t)s.npw, out[k],
+                                          (size_t)s.npw, st));
+    }
+    return HPSI_OK;
+}
+
+extern "C" int hpsi_hess_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, double* xx, double* yy, double* zz,
+                               double* xy, double* xz, double* yz, int flags, void* stream)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, nb, &s, flags);
+    if (rc) return rc;
+    double* o_[6] = {xx, yy, zz, xy, xz, yz};
+    if (nb > 0 && !psi_) return fail(c, HPSI_ERR_BAD_ARG, "psi NULL");
+    if (nb == 0 || s->npw == 0) return HPSI_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = flags & HPSI_PREC_MASK;
+    const bool fp64 = prec == HPSI_PREC_FP64;
+    const bool dev = flags & HPSI_DEVICE_PTRS;
+    const size_t nel = (size_t)nb * s->npw;
+    int nout = 0;
+    for (double* o : o_) nout += o != nullptr;
+    if (nout == 0) return HPSI_OK;
+    // projector matrices with their first-derivative rows, and the second-derivative rows
+    if ((rc = prepare_slot(c, *s, fp64 ? HPSI_PREC_FP64 : HPSI_PREC_FP32, true, st))) return rc;
+    if ((rc = fp64 ? ensure_hess<double2>(c, *s, st) : ensure_hess<float2>(c, *s, st))) return rc;
+    Carver cv;
+    const size_t o_psi = dev ? 0 : cv.take<double2>(nel);
+    size_t o_out[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 6; ++k)
+        if (o_[k] && !dev) o_out[k] = cv.take<double2>(nel);
+    const size_t o_work = cv.off;
+    const int P = s->P;
+    const size_t nsp = std::max((size_t)split_for(6 * P, nb, s->npw) * 6, (size_t)split_for(4 * P, nb, s->npw) * 4);
+    const size_t work = (nsp * P * nb + (size_t)10 * P * nb) * sizeof(double2) + 4096;
+    if ((rc = ws_reserve(c, o_work + work))) return rc;
+    const double2* psi = dev ? (const double2*)psi_ : reinterpret_cast<const double2*>(c->ws + o_psi);
+    double2* out[6];
+    for (int k = 0; k < 6; ++k)
+        out[k] = !o_[k] ? nullptr : (dev ? (double2*)o_[k] : reinterpret_cast<double2*>(c->ws + o_out[k]));
+    if (!dev) {
+        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < 6; ++k)
+            if (out[k]) CUDA_TRY(c, cudaMemcpyAsync(out[k], o_[k], nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+    }
+    rc = fp64 ? hess_device<double2, double2>(c, *s, nb, psi, out, c->ws + o_work, s->pr64, s->hess64, st)
+              : hess_device<float2, float2>(c, *s, nb, psi, out, c->ws + o_work, s->pr32, s->hess32, st);
+    if (rc) return rc;
+    if (!dev)
+        for (int k = 0; k < 6; ++k)
+            if (out[k]) CUDA_TRY(c, cudaMemcpyAsync(o_[k], out[k], nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (!dev || (flags & HPSI_SYNC)) CUDA_TRY(c, cudaStreamSynchronize(st));
+    return HPSI_OK;
 }
 
 extern "C" int hpsi_density(hpsi_ctx* c, int kid, int nb, const double* psi_, const double* occ_, double* rho_,

@@ -260,3 +260,13 @@ cudaError_t launch_beta_tables(int nr, const double* r, const double* rab, int u
 cudaError_t launch_gs_count(const double* B, const double* kf, double ecut, int gmax, int* counts, cudaStream_t st);
 cudaError_t launch_gs_write(const double* B, const double* kf, double ecut, int gmax, const int* offsets, int* g,
                             double* kvec, double* kinetic, cudaStream_t st);
+
+// ---- projector second derivatives for the Hessian (hessian.cu) ---------------
+// f[t][p][iq]: F0, F1, F3 radial tables of the projectors (t = 0, 1, 2)
+cudaError_t launch_hess_tables(int nr, const double* r, const double* rab, int uniform, int np, const int* l,
+                               const int* nmax, const double* beta, double dq, int nq, double* f, cudaStream_t st);
+// d2[c][row][g], c = xx, yy, zz, xy, xz, yz; ftabs[rad][3][nq]
+template <typename C>
+cudaError_t launch_hess_assemble(int P, int npw, const ProjRow* rows, const double* ftabs, int nq, double dq,
+                                 double inv_sqrt_omega, const double* kvec, const double2* sf, C* d2, cudaStream_t st);
+cudaError_t launch_add(size_t n, const double2* x, double2* y, cudaStream_t st);

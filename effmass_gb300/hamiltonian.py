@@ -187,6 +187,27 @@ class Hamiltonian:
         check(st, self._ctx)
         return x, its.value, res
 
+    def set_hessian_tables(self, species: int, f, dq: float):
+        """Attach the [3][n_proj][nq] Hessian radial tables (hessian_tables) to a species."""
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        check(self._lib.hpsi_set_hessian_tables(self._ctx, species, f.shape[-1], dq,
+                                                f.ctypes.data_as(C.POINTER(C.c_double))), self._ctx)
+
+    def hess_apply(self, kid: int, nb: int, psi, out: dict, precision: Optional[str] = None):
+        """out[ab] += d2H/dk_a dk_b psi for ab in xx, yy, zz, xy, xz, yz (missing keys skipped)."""
+        npw = self.dim(kid)
+        p, dev = _ptr(psi, npw, nb, "psi")
+        ptrs = []
+        for name in ("xx", "yy", "zz", "xy", "xz", "yz"):
+            o = out.get(name)
+            q, d = _ptr(o, npw, nb, name)
+            if o is not None and d != dev:
+                raise HpsiError(abi.HPSI_ERR_BAD_ARG, "psi and outputs must live in the same memory")
+            ptrs.append(q)
+        check(self._lib.hpsi_hess_apply(self._ctx, kid, nb, p, *ptrs, self.flags(precision, dev), _stream_for(dev)),
+              self._ctx)
+        return out
+
     def density(self, kid: int, nb: int, psi, occ, rho=None, precision: Optional[str] = None):
         """rho += sum_b occ_b |psi_b(r)|^2 (the reference's buildDensity for one k-point), [n1, n2, n3]."""
         npw = self.dim(kid)
@@ -349,3 +370,17 @@ def gsphere(lattice, k_frac, ecut: float):
     check(L.hpsi_gsphere(A.ctypes.data_as(dp), kf.ctypes.data_as(dp), ecut, n.value, g.ctypes.data, K.ctypes.data,
                          kin.ctypes.data, C.byref(n), 0, None))
     return KPoint(npw=n.value, k_frac=kf.copy(), g_idx=g, kvec=K, kinetic=kin)
+
+
+def hessian_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float = 20.0):
+    """Hessian radial tables [3][n_proj][nq] (F0, F1, F3) of radial projectors, built on the device."""
+    L = load()
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    rab = np.ascontiguousarray(rab, dtype=np.float64)
+    l = np.ascontiguousarray(l, dtype=np.int32)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    nq = L.hpsi_beta_table_length(dq, q_max)
+    f = np.zeros((3, beta.shape[0], nq))
+    check(L.hpsi_hessian_tables(r.size, r.ctypes.data, rab.ctypes.data, int(uniform), beta.shape[0], l.ctypes.data,
+                                beta.ctypes.data, dq, q_max, f.ctypes.data, 0, None))
+    return f

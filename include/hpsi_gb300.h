@@ -20,6 +20,9 @@
  *   Gradient::Callable::operator()(psi, GradHPsi)
  *     (src/H_psi/hamiltonian.cppm:228-229;
  *      src/H_psi/hamiltonian_gradient.cpp:116-294)        hpsi_grad_apply
+ *   Hessian::Callable::operator()(psi, HessHPsi)
+ *     (declared, src/H_psi/hamiltonian.cppm:84-91; empty
+ *      body, src/H_psi/hamiltonian_hessian.cpp:48-50)      hpsi_hess_apply
  *   (no counterpart; band-pair <psi_m|dH/dk_a|psi_n>)     hpsi_velocity_matrix
  *   C++ exceptions (runtime_error, out_of_range,
  *     domain_error)                                       negative status + hpsi_last_error
@@ -152,6 +155,29 @@ int hpsi_beta_tables(int nr, const double* r, const double* rab, int uniform_mes
  * Output arrays host or device per HPSI_DEVICE_PTRS; synchronises stream. */
 int hpsi_gsphere(const double* lattice, const double* k_frac, double ecut, int max_npw, int* g_idx,
                  double* kvec, double* kinetic, int* npw_out, int flags, void* stream);
+
+/* Hessian d2H/dk_a dk_b |psi> (the reference declares it with six outputs,
+ * src/H_psi/hamiltonian.cppm:84-91, and leaves the operator empty,
+ * src/H_psi/hamiltonian_hessian.cpp:48-50):
+ *   out_ab += delta_ab psi + sum_p lambda_p (|d_ab p><p| + |d_a p><d_b p|
+ *                                            + |d_b p><d_a p| + |p><d_ab p|) psi
+ * for ab = xx, yy, zz, xy, xz, yz (NULL outputs are skipped).  The projector
+ * second derivatives come from radial tables, smooth at q = 0 (g_n(x) =
+ * j_n(x)/x^n):  F0 = 4 pi Int beta r^(l+1) g_l(qr) dr  (= beta/q^l),
+ * F1 = -4 pi Int beta r^(l+3) g_(l+1)(qr) dr  (= F0'/q),
+ * F3 = 4 pi Int beta r^(l+5) g_(l+2)(qr) dr  (= (F0'' - F0'/q)/q^2), times
+ * the solid harmonics R_lm = |K|^l Y_lm:
+ *   d_ab(beta Y) = F3 K_a K_b R + F1 (delta_ab R + K_a d_b R + K_b d_a R) + F0 d_ab R.
+ * hpsi_hessian_tables builds f = [3][n_proj][nq] (F0, F1, F3 on q_i = i dq,
+ * nq = hpsi_beta_table_length(dq, q_max)) from radial projectors as in
+ * hpsi_beta_tables; hpsi_set_hessian_tables attaches them to a species of ctx
+ * (the same dq and nq for all species).  hpsi_hess_apply runs FP64 for
+ * HPSI_PREC_FP64 and FP32 otherwise; HPSI_ERR_STATE without tables. */
+int hpsi_hessian_tables(int nr, const double* r, const double* rab, int uniform_mesh, int n_proj, const int* l,
+                        const double* beta, double dq, double q_max, double* f, int flags, void* stream);
+int hpsi_set_hessian_tables(hpsi_ctx* ctx, int species, int nq, double dq, const double* f);
+int hpsi_hess_apply(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* xx, double* yy, double* zz,
+                    double* xy, double* xz, double* yz, int flags, void* stream);
 
 /* Sternheimer equations for the k-derivative of the occupied bands (the
  * reference's roadmap item: conjugate-gradient solution of the linear

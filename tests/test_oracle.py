@@ -237,3 +237,24 @@ def test_beta_interp_rules(oracle_lib):
     assert v == cubic[0] * norm
     assert oracle_lib.beta_interp(cubic, dq, qmax, norm, 20.0000001)[0] == abi.HPSI_ERR_RANGE
     assert oracle_lib.beta_interp(cubic, dq, qmax, norm, -1e-9)[0] == abi.HPSI_ERR_RANGE
+
+
+def test_solid_harmonics_table_matches_reference_ylm(oracle_lib):
+    """effmass_gb300/csrc/solid_harmonics.inc (R_lm = |K|^l Y_lm, used by the
+    Hessian's projector derivatives) against the oracle's Y_lm, which is pinned to
+    the reference's RealSphericalHarmonicsEngine."""
+    import re
+    txt = open(os.path.join(os.path.dirname(__file__), "..", "effmass_gb300", "csrc", "solid_harmonics.inc")).read()
+    rows = re.findall(r"\{(\{.*?\})\},\s*// l=(\d+) m=(-?\d+)", txt)
+    assert len(rows) == 25
+    rng = np.random.default_rng(0)
+    K = rng.standard_normal((64, 3)) * rng.uniform(0.2, 3.0, (64, 1))
+    q = np.linalg.norm(K, axis=1)
+    Y = oracle_lib.ylm(4, np.arccos(K[:, 2] / q), np.arctan2(K[:, 1], K[:, 0]))[0]
+    for idx, (body, l, m) in enumerate(rows):
+        l = int(l)
+        assert idx == l * l + l + int(m)
+        R = np.zeros(len(q))
+        for c, a, b, cz in re.findall(r"\{([-0-9.e]+), (\d+), (\d+), (\d+)\}", body):
+            R += float(c) * K[:, 0] ** int(a) * K[:, 1] ** int(b) * K[:, 2] ** int(cz)
+        assert np.abs(R / q ** l - Y[idx]).max() <= 1e-14 * max(1.0, np.abs(Y[idx]).max()), (l, m)
