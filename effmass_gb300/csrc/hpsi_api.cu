@@ -403,7 +403,7 @@ static int chunk_bands(const KSlot& s, const hpsi_ctx* c, int nb, size_t csize)
 {
     size_t per = (size_t)s.nxs * c->n2 * c->n3 * csize;
     if (per == 0) return nb;
-    long ch = (long)((64ull << 20) / per);
+    long ch = (long)((512ull << 20) / per);
     return (int)std::max(1L, std::min((long)nb, ch));
 }
 

@@ -15,8 +15,9 @@
 //                   store the nxs sphere planes back into T in place.
 //   C  r2g_planes : per (plane, band): FFT along y then z (R2G), then gather
 //                   the sphere points: hpsi += kinetic*psi + grid/N.
-// T is sized for a chunk of bands so that it stays resident in L2 between
-// the passes.  Kinetic energy is fused into pass C.
+// T holds a chunk of bands of at most 512 MB: wide launches fill the 152 SMs
+// for every pass, which measured faster than chunks small enough to stay in
+// L2 between the passes.  Kinetic energy is fused into pass C.
 #include <type_traits>
 
 #include "fft.cuh"
@@ -459,10 +460,19 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
     const size_t budget = csize == 8 ? 48 * 1024 : 96 * 1024;
     int nlmax = (int)(budget / (2 * (size_t)a->n1 * csize));
     if (nlmax < 1) nlmax = 1;
-    a->kt = nlmax < 8 ? nlmax : 8;
-    if (a->kt > a->n3) a->kt = a->n3;
-    a->bb = nlmax / a->kt;
-    if (a->bb < 1) a->bb = 1;
+    if (csize == 8 && nlmax >= 8 && a->n3 >= 4) {
+        // complex64: 4 z-values and a power-of-two band group (<= 16) per block,
+        // the shape the batch plans' tuner picks for the 36^3 and 72^3 grids
+        a->kt = 4;
+        int bb = 1;
+        while (bb * 2 <= nlmax / 4 && bb * 2 <= 16) bb *= 2;
+        a->bb = bb;
+    } else {
+        a->kt = nlmax < 8 ? nlmax : 8;
+        if (a->kt > a->n3) a->kt = a->n3;
+        a->bb = nlmax / a->kt;
+        if (a->bb < 1) a->bb = 1;
+    }
     a->nl_z = make_fastdiv((uint32_t)a->n2);
     a->nl_y = make_fastdiv((uint32_t)a->n3);
     a->nl_x = make_fastdiv((uint32_t)(a->kt * a->bb));
@@ -521,7 +531,7 @@ static cudaError_t launch_local_batch_t(const LocalArgs& a, int nbands, int max_
 }
 
 // Kernel set of a launch: the wide-radix set, a compile-time two-stage plan
-// (complex64, the same plan on all three axes; with KT = 8 also a
+// (complex64, the same plan on all three axes; with KT = 4 also a
 // compile-time z-tile in the x pass), or the runtime-plan set.
 template <int K> using IntC = std::integral_constant<int, K>;
 template <typename C, typename F>
@@ -532,19 +542,19 @@ static cudaError_t with_kernels(const LocalArgs& a, F&& f)
     if constexpr (std::is_same<C, float2>::value) {
         const int id = fft_ct_id(a.Lx);
         if (id != FFT_CT_NONE && fft_ct_id(a.Ly) == id && fft_ct_id(a.Lz) == id) {
-            const bool k8 = a.kt == 8;
+            const bool k4 = a.kt == 4;
             switch (id) {
                 case FFT_CT_72:
-                    return k8 ? f(std::false_type{}, FftPlan2<8, 9>{}, IntC<8>{})
+                    return k4 ? f(std::false_type{}, FftPlan2<8, 9>{}, IntC<4>{})
                               : f(std::false_type{}, FftPlan2<8, 9>{}, IntC<0>{});
                 case FFT_CT_36:
-                    return k8 ? f(std::false_type{}, FftPlan2<9, 4>{}, IntC<8>{})
+                    return k4 ? f(std::false_type{}, FftPlan2<9, 4>{}, IntC<4>{})
                               : f(std::false_type{}, FftPlan2<9, 4>{}, IntC<0>{});
                 case FFT_CT_24:
-                    return k8 ? f(std::false_type{}, FftPlan2<8, 3>{}, IntC<8>{})
+                    return k4 ? f(std::false_type{}, FftPlan2<8, 3>{}, IntC<4>{})
                               : f(std::false_type{}, FftPlan2<8, 3>{}, IntC<0>{});
                 case FFT_CT_64:
-                    return k8 ? f(std::false_type{}, FftPlan2<8, 8>{}, IntC<8>{})
+                    return k4 ? f(std::false_type{}, FftPlan2<8, 8>{}, IntC<4>{})
                               : f(std::false_type{}, FftPlan2<8, 8>{}, IntC<0>{});
                 default: break;
             }
