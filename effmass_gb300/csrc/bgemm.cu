@@ -158,22 +158,26 @@ __global__ void __launch_bounds__(256) bexp_kernel(int P, const BGemmItem* __res
         }
         __syncthreads();
     }
+    // all loads of the read-modify-write first, so that they overlap
+    double2 o[TM][TN];
 #pragma unroll
-    for (int i = 0; i < TM; ++i) {
-        const int n = n0 + ty + 16 * i;
-        if (n >= I.nb) continue;
-        double2* out = I.hpsi + (size_t)n * I.npw;
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
         for (int j = 0; j < TN; ++j) {
-            const int g = g0 + tx + 16 * j;
-            if (g < I.npw) {
-                double2 o = out[g];
-                o.x += (double)ar[i][j];
-                o.y += (double)ai[i][j];
-                out[g] = o;
+            const int n = n0 + ty + 16 * i, g = g0 + tx + 16 * j;
+            o[i][j] = (n < I.nb && g < I.npw) ? I.hpsi[(size_t)n * I.npw + g] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int n = n0 + ty + 16 * i, g = g0 + tx + 16 * j;
+            if (n < I.nb && g < I.npw) {
+                o[i][j].x += (double)ar[i][j];
+                o[i][j].y += (double)ai[i][j];
+                I.hpsi[(size_t)n * I.npw + g] = o[i][j];
             }
         }
-    }
 }
 
 // (TM, TN) variants the tuner chooses from

@@ -199,21 +199,26 @@ __global__ void __launch_bounds__(256) expand_gemm_kernel(int M, int N, int K, c
         }
         __syncthreads();
     }
+    // all loads of the read-modify-write first, so that they overlap
+    double2 o[TM][TN];
 #pragma unroll
-    for (int i = 0; i < TM; ++i) {
-        const int n = n0 + ty + 16 * i;
-        if (n >= N) continue;
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
         for (int j = 0; j < TN; ++j) {
-            const int k = k0 + tx + 16 * j;
-            if (k < K) {
-                double2 o = out[(size_t)n * ldo + k];
-                o.x += (double)accr[i][j];
-                o.y += (double)acci[i][j];
-                out[(size_t)n * ldo + k] = o;
+            const int n = n0 + ty + 16 * i, k = k0 + tx + 16 * j;
+            o[i][j] = (n < N && k < K) ? out[(size_t)n * ldo + k] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int n = n0 + ty + 16 * i, k = k0 + tx + 16 * j;
+            if (n < N && k < K) {
+                o[i][j].x += (double)accr[i][j];
+                o[i][j].y += (double)acci[i][j];
+                out[(size_t)n * ldo + k] = o[i][j];
             }
         }
-    }
 }
 
 template <typename C>

@@ -254,11 +254,13 @@ __global__ void __launch_bounds__(192, 1)
                         for (int i = 0; i < 32; ++i) v[i] += w[i];
                     }
                     if (row < M) {
+                        // scales first: a load after a store to out would wait for it
+                        float sb[32];
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) {
-                            const int n = n0 + c0 + i;
-                            if (n < N) out[c0 + i] = v[i] * sa * ep.sb_scale[n];
-                        }
+                        for (int i = 0; i < 32; ++i) sb[i] = (n0 + c0 + i < N) ? ep.sb_scale[n0 + c0 + i] : 0.f;
+#pragma unroll
+                        for (int i = 0; i < 32; ++i)
+                            if (n0 + c0 + i < N) out[c0 + i] = v[i] * sa * sb[i];
                     }
                 }
             } else {
@@ -277,16 +279,28 @@ __global__ void __launch_bounds__(192, 1)
                         for (int i = 0; i < 32; ++i) im[i] += w[i];
                     }
                     if (row < M) {
+                        // read-modify-write of hpsi in groups of 16 bands: all loads
+                        // of a group are issued before its stores, so the HBM round
+                        // trips overlap instead of following one another band by band
+                        const int b0 = blockIdx.y * 128 + c0;
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) {
-                            const int b = blockIdx.y * 128 + c0 + i;
-                            if (b < ep.nb) {
-                                const float f = sa * ep.sb_scale[n0 + c0 + i];
-                                double2* h = ep.hpsi + (size_t)b * ep.ldh + row;
-                                double2 o = *h;
-                                o.x += (double)(re[i] * f);
-                                o.y += (double)(im[i] * f);
-                                *h = o;
+                        for (int h0 = 0; h0 < 32; h0 += 16) {
+                            double2 o[16];
+                            float f[16];
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) {
+                                const int b = b0 + h0 + i;
+                                f[i] = sa * ep.sb_scale[n0 + c0 + h0 + i];
+                                o[i] = b < ep.nb ? ep.hpsi[(size_t)b * ep.ldh + row] : make_double2(0.0, 0.0);
+                            }
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) {
+                                const int b = b0 + h0 + i;
+                                if (b < ep.nb) {
+                                    o[i].x += (double)(re[h0 + i] * f[i]);
+                                    o[i].y += (double)(im[h0 + i] * f[i]);
+                                    ep.hpsi[(size_t)b * ep.ldh + row] = o[i];
+                                }
                             }
                         }
                     }
