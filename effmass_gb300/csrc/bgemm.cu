@@ -7,7 +7,7 @@
 // written for item i (a k-point with its bands) as two GEMMs over the
 // projector matrix Pr_i[P][npw_i]:
 //   projection  part_i[s][P][nb_i] = conj(Pr_i) psi_i^T over the s-th K chunk
-//   reduction   W_i[P][nb_i]       = lambda . sum_s part_i[s]  (FP64 sum in split order,
+//   reduction   W_i[P][nb_i]       = lambda . sum_s part_i[s]  (sum in split order,
 //                                   as in the unbatched path)
 //   expansion   hpsi_i[nb_i][G]   += W_i^T Pr_i
 //
@@ -15,6 +15,7 @@
 // the tile is (16 TM) x (16 TN) and shared-memory reads of a warp are
 // conflict free.  The tile shape and the split count are chosen per batch by
 // the autotuner of the batch plan.
+#include <type_traits>
 #include "kernels.cuh"
 
 namespace {
@@ -90,8 +91,9 @@ __global__ void __launch_bounds__(256) bproj_kernel(int P, const BGemmItem* __re
     }
 }
 
-// W_i[m][n] = lam[m] * sum_s part_i[s][m][n] (FP64 sum in split order), one
-// thread per (m, n); grid (ceil(P nb_max / 256), items).
+// W_i[m][n] = lam[m] * sum_s part_i[s][m][n] in split order (FP64 for
+// complex128, compensated FP32 for complex64), one thread per (m, n);
+// grid (ceil(P nb_max / 256), items).
 template <typename C, typename Acc>
 __global__ void __launch_bounds__(256) bred_kernel(int P, const BGemmItem* __restrict__ items, int nsplit,
                                                    const Acc* __restrict__ part, C* __restrict__ W)
@@ -101,6 +103,17 @@ __global__ void __launch_bounds__(256) bred_kernel(int P, const BGemmItem* __res
     if (idx >= P * I.nb) return;
     const Acc* pw = part + I.part_off + idx;
     const size_t split_stride = (size_t)P * I.nb;
+    if constexpr (std::is_same<Acc, float2>::value && std::is_same<C, float2>::value) {
+        Sum2f re, im;  // complex64: compensated FP32, no FP64 pipe
+        for (int s = 0; s < nsplit; ++s) {
+            const float2 v = pw[s * split_stride];
+            re.add(v.x);
+            im.add(v.y);
+        }
+        const float l = d2f_bits(I.lam[idx / I.nb]);
+        W[I.w_off + idx] = make_float2(l * re.value(), l * im.value());
+        return;
+    }
     double sr = 0.0, si = 0.0;
     for (int s = 0; s < nsplit; ++s) {
         const double2 v = as_c128(pw[s * split_stride]);

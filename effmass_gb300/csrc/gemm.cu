@@ -11,6 +11,7 @@
 // Tiles: 64 x 64 outputs per 256-thread block, 16-deep K slices staged in
 // shared memory; each thread owns a 4 x 4 block of outputs at stride 16 so
 // that shared-memory reads of a warp are bank-conflict free.
+#include <type_traits>
 #include "kernels.cuh"
 
 template <typename Acc, typename T>
@@ -134,6 +135,17 @@ __global__ void reduce_splits_kernel(int M, int N, int nsplit, const Acc* __rest
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)M * N) return;
     const int m = (int)(idx / N), n = (int)(idx % N);
+    if constexpr (std::is_same<Acc, float2>::value && std::is_same<CW, float2>::value) {
+        Sum2f re, im;  // complex64: compensated FP32, no FP64 pipe
+        for (int s = 0; s < nsplit; ++s) {
+            const float2 v = part[(size_t)s * M * N + idx];
+            re.add(v.x);
+            im.add(v.y);
+        }
+        const float f = scale ? d2f_bits(scale[m % period]) : 1.f;
+        W[(size_t)m * ldw + n] = make_float2(f * re.value(), f * im.value());
+        return;
+    }
     double sr = 0.0, si = 0.0;
     for (int s = 0; s < nsplit; ++s) {
         double2 v = as_c128(part[(size_t)s * M * N + idx]);

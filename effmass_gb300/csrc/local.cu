@@ -409,17 +409,36 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     const double2* ps = psi + (size_t)b * npw;
     double2* hp = hpsi + (size_t)b * npw;
     const int e0 = plane_off[p], e1 = plane_off[p + 1];
-    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        int ig = ent_ig[e] & 0x7fffffff;
-        int jk = ent_jk[e];
-        int j = jk / n3, k = jk - j * n3;
-        double2 g = as_c128(res[j * n3p + k]);
-        double2 s = ps[ig];
-        double kin = kinetic[ig];
-        double2 h = hp[ig];
-        h.x += kin * s.x + g.x * a.inv_n;
-        h.y += kin * s.y + g.y * a.inv_n;
-        hp[ig] = h;
+    if constexpr (std::is_same<C, float2>::value) {
+        // complex64: kinetic*psi + grid/N in FP32 (conversions on the integer
+        // pipe), one FP64 add per component into hpsi
+        const float inv_n = (float)a.inv_n;
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            int ig = ent_ig[e] & 0x7fffffff;
+            int jk = ent_jk[e];
+            int j = jk / n3, k = jk - j * n3;
+            const float2 g = res[j * n3p + k];
+            const float2 s = to_c64(ps[ig]);
+            const float kin = d2f_bits(kinetic[ig]);
+            const float2 t = make_float2(fmaf(kin, s.x, g.x * inv_n), fmaf(kin, s.y, g.y * inv_n));
+            double2 h = hp[ig];
+            h.x += f2d_bits(t.x);
+            h.y += f2d_bits(t.y);
+            hp[ig] = h;
+        }
+    } else {
+        for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            int ig = ent_ig[e] & 0x7fffffff;
+            int jk = ent_jk[e];
+            int j = jk / n3, k = jk - j * n3;
+            double2 g = as_c128(res[j * n3p + k]);
+            double2 s = ps[ig];
+            double kin = kinetic[ig];
+            double2 h = hp[ig];
+            h.x += kin * s.x + g.x * a.inv_n;
+            h.y += kin * s.y + g.y * a.inv_n;
+            hp[ig] = h;
+        }
     }
 }
 

@@ -23,6 +23,7 @@
 // issues the MMAs from one thread, warps 2-5 drain TMEM.  Every mbarrier wait
 // is bounded; on timeout the CTA sets an error flag, drains and frees TMEM.
 #include <cuda.h>
+#include <type_traits>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
@@ -297,8 +298,8 @@ __global__ void __launch_bounds__(192, 1)
                             for (int i = 0; i < 16; ++i) {
                                 const int b = b0 + h0 + i;
                                 if (b < ep.nb) {
-                                    o[i].x += (double)(re[h0 + i] * f[i]);
-                                    o[i].y += (double)(im[h0 + i] * f[i]);
+                                    o[i].x += f2d_bits(re[h0 + i] * f[i]);
+                                    o[i].y += f2d_bits(im[h0 + i] * f[i]);
                                     ep.hpsi[(size_t)b * ep.ldh + row] = o[i];
                                 }
                             }
@@ -475,19 +476,47 @@ __device__ __forceinline__ double2 band_get(const S* src, int nb, int len, int b
     return as_c128(src[(size_t)b * len + i]);
 }
 
+// |x| of a complex128 or complex64 component as a non-negative float whose
+// binary exponent is that of |x| rounded to float: the row scale depends on
+// the exponent alone, so a truncated mantissa is enough (no FP64 arithmetic)
+__device__ __forceinline__ uint32_t abs_key(double x)
+{
+    const uint32_t hi = (uint32_t)__double2hiint(x) & 0x7fffffffu;
+    return __float_as_uint(d2f_bits(__hiloint2double((int)hi, 0)));
+}
+__device__ __forceinline__ uint32_t abs_key(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+
 template <typename S, bool FROM_W>
 __global__ void band_max_kernel(const S* __restrict__ src, int nb, int len, unsigned* rowmax)
 {
     const int b = blockIdx.y;
-    float mx = 0.f;
+    uint32_t mx = 0u;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
-        double2 v = band_get<S, FROM_W>(src, nb, len, b, i);
-        mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+        const S v = FROM_W ? src[(size_t)i * nb + b] : src[(size_t)b * len + i];
+        mx = max(mx, max(abs_key(v.x), abs_key(v.y)));
     }
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(rowmax + b, __float_as_uint(mx));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(rowmax + b, mx);
 }
 
+template <typename T>
+__device__ __forceinline__ void split2(float x, T& h, T& l);
+template <>
+__device__ __forceinline__ void split2<__half>(float x, __half& h, __half& l)
+{
+    h = __float2half_rn(x);
+    l = __float2half_rn(x - __half2float(h));
+}
+template <>
+__device__ __forceinline__ void split2<__nv_bfloat16>(float x, __nv_bfloat16& h, __nv_bfloat16& l)
+{
+    h = __float2bfloat16_rn(x);
+    l = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// Two complex elements per thread: k = 4t .. 4t+3 of both rows of band b,
+// written as one 8-byte store per row and piece (ldk is a multiple of BK, so
+// 4t < ldk implies 4t+3 < ldk).
 template <typename T, typename S, bool FROM_W>
 __global__ void band_write_kernel(const S* __restrict__ src, int nb, int len, size_t ldk, T* hi, T* lo,
                                   float* inv_scale, const unsigned* __restrict__ rowmax, bool fp16)
@@ -500,20 +529,30 @@ __global__ void band_write_kernel(const S* __restrict__ src, int nb, int len, si
         inv_scale[rre] = 1.f / sc;
         inv_scale[rim] = 1.f / sc;
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // complex element -> k = 2i, 2i+1
-    if ((size_t)(2 * i) >= ldk) return;
-    float a0 = 0.f, a1 = 0.f, c0 = 0.f, c1 = 0.f;
-    if (i < len) {
-        const double2 v = band_get<S, FROM_W>(src, nb, len, b, i);
-        const float r = (float)(v.x * (double)sc), m = (float)(v.y * (double)sc);
-        if (!FROM_W) { a0 = r; a1 = m; c0 = m; c1 = -r; }
-        else { a0 = r; a1 = -m; c0 = m; c1 = r; }
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t k = 4 * (size_t)q;
+    if (k >= ldk) return;
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int i = 2 * q + e;
+        if (i < len) {
+            const float2 v = to_c64(band_get<S, FROM_W>(src, nb, len, b, i));
+            const float r = v.x * sc, m = v.y * sc;  // sc: a power of two
+            if (!FROM_W) { a[2 * e] = r; a[2 * e + 1] = m; c[2 * e] = m; c[2 * e + 1] = -r; }
+            else { a[2 * e] = r; a[2 * e + 1] = -m; c[2 * e] = m; c[2 * e + 1] = r; }
+        }
     }
-    const size_t k = 2 * (size_t)i;
-    split_store<T>(a0, hi + rre * ldk + k, lo + rre * ldk + k);
-    split_store<T>(a1, hi + rre * ldk + k + 1, lo + rre * ldk + k + 1);
-    split_store<T>(c0, hi + rim * ldk + k, lo + rim * ldk + k);
-    split_store<T>(c1, hi + rim * ldk + k + 1, lo + rim * ldk + k + 1);
+    __align__(8) T ah[4], al[4], ch[4], cl[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        split2<T>(a[e], ah[e], al[e]);
+        split2<T>(c[e], ch[e], cl[e]);
+    }
+    *reinterpret_cast<uint2*>(hi + rre * ldk + k) = *reinterpret_cast<const uint2*>(ah);
+    *reinterpret_cast<uint2*>(lo + rre * ldk + k) = *reinterpret_cast<const uint2*>(al);
+    *reinterpret_cast<uint2*>(hi + rim * ldk + k) = *reinterpret_cast<const uint2*>(ch);
+    *reinterpret_cast<uint2*>(lo + rim * ldk + k) = *reinterpret_cast<const uint2*>(cl);
 }
 
 template <typename T, typename S, bool FROM_W>
@@ -523,7 +562,7 @@ static void band_rows(const S* src, int nb, int len, size_t ldk, T* hi, T* lo, f
     cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * nb, st);
     const int chunks = min(64, ceil_div(len, 256 * 4));
     band_max_kernel<S, FROM_W><<<dim3(chunks, nb), 256, 0, st>>>(src, nb, len, rowmax);
-    band_write_kernel<T, S, FROM_W><<<dim3(ceil_div((long)(ldk / 2), 256), nb), 256, 0, st>>>(
+    band_write_kernel<T, S, FROM_W><<<dim3(ceil_div((long)(ldk / 4), 256), nb), 256, 0, st>>>(
         src, nb, len, ldk, hi, lo, inv_scale, rowmax, fp16);
 }
 
@@ -554,6 +593,19 @@ __global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float
     const int p = (int)(idx / nb), b = (int)(idx % nb);
     const int t = b / 128, j = b % 128;
     const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
+    if constexpr (std::is_same<CW, float2>::value) {
+        if (!eterm) {
+            Sum2f re, im;  // complex64 W: compensated FP32 sums, no FP64 pipe
+            for (int z = 0; z < nsplit; ++z) {
+                const float* row = part + ((size_t)z * P + p) * N;
+                re.add(row[cre]);
+                im.add(row[cim]);
+            }
+            const float f = lam ? d2f_bits(lam[p % period]) : 1.f;
+            W[idx] = make_float2(f * re.value(), f * im.value());
+            return;
+        }
+    }
     double sr = 0.0, si = 0.0;
     for (int z = 0; z < nsplit; ++z) {
         const float* row = part + ((size_t)z * P + p) * N;

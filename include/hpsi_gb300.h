@@ -355,6 +355,12 @@ int hpsi_batch_info(const hpsi_batch* b, char* buf, size_t len);
 int hpsi_batch_destroy(hpsi_batch* b);
 const char* hpsi_batch_last_error(const hpsi_batch* b);
 
+/* Self-test of the integer-pipe FP64 <-> FP32 conversions the complex64
+ * kernels use: for n doubles x (host memory) returns the conversion to float
+ * by bit arithmetic (f_bits) and by the hardware (f_hw), and the conversion of
+ * f_hw back to double both ways (d_bits, d_hw).  No reference counterpart. */
+int hpsi_selftest_convert(const double* x, long n, float* f_bits, float* f_hw, double* d_bits, double* d_hw);
+
 /* Message of the last failed call on ctx (never NULL); with ctx == NULL the
  * message of the calling thread's last failed hpsi_ctx_create. */
 const char* hpsi_last_error(const hpsi_ctx* ctx);
