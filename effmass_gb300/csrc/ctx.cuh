@@ -92,6 +92,10 @@ struct hpsi_ctx {
     size_t ws_size = 0;
     Prof prof;
     int* d_err = nullptr;         // device-side error flag of the bounded waits (tcgen05 GEMMs)
+    // side stream of the tensor-core H|psi>: the projection chain runs there
+    // beside the FFT passes (fork/join by events on the caller's stream)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long gen_counter = 0;         // source of KSlot::gen
     double* d_hess = nullptr;     // Hessian radial tables [nrad][3][hess_nq] (F0, F1, F3), raw
     int hess_nq = 0;

@@ -39,6 +39,9 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     dfree(c->d_tables); dfree(c->d_rad_nq); dfree(c->d_rad_dq); dfree(c->d_tau); dfree(c->d_v64); dfree(c->d_v32);
     dfree(c->d_tw64); dfree(c->d_tw32); dfree(c->d_err); dfree(c->d_hess);
     if (c->ws) cudaFree(c->ws);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof.pool) cudaEventDestroy(e);
     delete c;
@@ -120,6 +123,9 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
         return fail(c, HPSI_ERR_BAD_ARG, "FFT grid %dx%dx%d: two complex128 n2*n3 planes exceed shared memory", c->n1, c->n2, c->n3);
 
     CUDA_TRY(c, cudaGetDevice(&c->dev));
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     CUDA_TRY(c, dalloc(&c->d_err, (size_t)1));
     CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
     const size_t N = (size_t)c->n1 * c->n2 * c->n3;
@@ -499,13 +505,15 @@ static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
     s.tc_fmt = -1;
     const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(2 * (size_t)s.P);
     Carver cv;
-    const size_t o1h = cv.take<uint16_t>((size_t)s.P * k1), o1l = cv.take<uint16_t>((size_t)s.P * k1);
+    const size_t rp = tc_rows_pad(s.P), rg = tc_rows_pad(s.npw);
+    const size_t o1h = cv.take<uint16_t>(rp * k1), o1l = cv.take<uint16_t>(rp * k1);
     const size_t o1s = cv.take<float>((size_t)s.P);
-    const size_t o2h = cv.take<uint16_t>((size_t)s.npw * k2), o2l = cv.take<uint16_t>((size_t)s.npw * k2);
+    const size_t o2h = cv.take<uint16_t>(rg * k2), o2l = cv.take<uint16_t>(rg * k2);
     const size_t o2s = cv.take<float>((size_t)s.npw);
     const size_t ocm = cv.take<float>((size_t)s.npw);
     CUDA_TRY(c, dalloc(&s.tc_mem, cv.off));
-    CUDA_TRY(c, cudaMemsetAsync(s.tc_mem + o2h, 0, o2s - o2h, st));  // K padding of Pr^T must read as zero
+    // padding rows and the K padding of Pr^T must read as zero
+    CUDA_TRY(c, cudaMemsetAsync(s.tc_mem, 0, cv.off, st));
     s.tc_proj = TcOperand{s.tc_mem + o1h, s.tc_mem + o1l, reinterpret_cast<float*>(s.tc_mem + o1s), k1};
     s.tc_expand = TcOperand{s.tc_mem + o2h, s.tc_mem + o2l, reinterpret_cast<float*>(s.tc_mem + o2s), k2};
     int h = c->prof.open(PH_BUILD, st);
@@ -551,35 +559,62 @@ static size_t tc_ws(const KSlot& s, int nb, bool energy = false)
     return cv.off;
 }
 
-static int tc_nonlocal(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
-                       cudaStream_t st, double* e_nl = nullptr)
+// Workspace of the tensor-core nonlocal term: split band operand, partials,
+// W and its split operand
+struct TcNl {
+    TcOperand B1, B2;
+    float* part;
+    float2* W;
+    unsigned* rowmax;
+    double* eterm;
+    int ns;
+};
+
+static TcNl tc_layout(const KSlot& s, int nb, unsigned char* ws, bool energy)
 {
-    if (s.P == 0 || nb == 0) return HPSI_OK;
-    const bool fp16 = s.tc_fmt == 0;
     const int NB = tc_band_rows(nb);
     const size_t k1 = s.tc_proj.ldk, k2 = s.tc_expand.ldk;
-    const int ns = tc_splits(s, nb, e_nl != nullptr);
+    TcNl t;
+    t.ns = tc_splits(s, nb, energy);
     Carver cv;
     const size_t ob1h = cv.take<uint16_t>((size_t)NB * k1), ob1l = cv.take<uint16_t>((size_t)NB * k1);
     const size_t ob1s = cv.take<float>((size_t)NB);
-    const size_t opart = cv.take<float>((size_t)ns * s.P * NB);
+    const size_t opart = cv.take<float>((size_t)t.ns * s.P * NB);
     const size_t ow = cv.take<float2>((size_t)s.P * nb);
     const size_t ob2h = cv.take<uint16_t>((size_t)NB * k2), ob2l = cv.take<uint16_t>((size_t)NB * k2);
     const size_t ob2s = cv.take<float>((size_t)NB);
-    unsigned* rowmax = reinterpret_cast<unsigned*>(ws + cv.take<unsigned>((size_t)nb));
-    double* eterm = e_nl ? reinterpret_cast<double*>(ws + cv.take<double>((size_t)s.P * nb)) : nullptr;
-    TcOperand B1{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
-    TcOperand B2{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
-    float2* W = reinterpret_cast<float2*>(ws + ow);
+    t.rowmax = reinterpret_cast<unsigned*>(ws + cv.take<unsigned>((size_t)nb));
+    t.eterm = energy ? reinterpret_cast<double*>(ws + cv.take<double>((size_t)s.P * nb)) : nullptr;
+    t.B1 = TcOperand{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
+    t.B2 = TcOperand{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
+    t.part = reinterpret_cast<float*>(ws + opart);
+    t.W = reinterpret_cast<float2*>(ws + ow);
+    return t;
+}
+
+// Projection half: split psi, W = lambda <p|psi> (+ nonlocal energies), split W
+static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, unsigned char* ws,
+                               cudaStream_t st, double* e_nl)
+{
+    const bool fp16 = s.tc_fmt == 0;
+    TcNl t = tc_layout(s, nb, ws, e_nl != nullptr);
     int h = c->prof.open(PH_OTHER, st);
-    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &B1, rowmax, st));
+    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &t.B1, t.rowmax, st));
     c->prof.close(h, st);
-    CUDA_TRY(c, tc_projection(s.tc_proj, s.P, B1, nb, ns, fp16, reinterpret_cast<float*>(ws + opart), s.d_lam, s.P, W,
-                              c->d_err, st, &c->prof, eterm, e_nl));
+    CUDA_TRY(c, tc_projection(s.tc_proj, s.P, t.B1, nb, t.ns, fp16, t.part, s.d_lam, s.P, t.W, c->d_err, st,
+                              &c->prof, t.eterm, e_nl));
     h = c->prof.open(PH_OTHER, st);
-    CUDA_TRY(c, tc_w_operand(W, s.P, nb, fp16, &B2, rowmax, st));
+    CUDA_TRY(c, tc_w_operand(t.W, s.P, nb, fp16, &t.B2, t.rowmax, st));
     c->prof.close(h, st);
-    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, B2, nb, fp16, hpsi, c->d_err, st, &c->prof));
+    return HPSI_OK;
+}
+
+// Expansion half: hpsi += P^T W
+static int tc_nonlocal_expand(hpsi_ctx* c, KSlot& s, int nb, double2* hpsi, unsigned char* ws, cudaStream_t st,
+                              bool energy)
+{
+    TcNl t = tc_layout(s, nb, ws, energy);
+    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, t.B2, nb, s.tc_fmt == 0, hpsi, c->d_err, st, &c->prof));
     return HPSI_OK;
 }
 
@@ -593,19 +628,18 @@ static int ensure_tc_grad(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
     s.tcg_fmt = -1;
     const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(4 * (size_t)s.P);
     Carver cv;
-    const size_t o1h = cv.take<uint16_t>((size_t)4 * s.P * k1), o1l = cv.take<uint16_t>((size_t)4 * s.P * k1);
+    const size_t rp = tc_rows_pad(4 * (size_t)s.P), rg = tc_rows_pad(s.npw);
+    const size_t o1h = cv.take<uint16_t>(rp * k1), o1l = cv.take<uint16_t>(rp * k1);
     const size_t o1s = cv.take<float>((size_t)4 * s.P);
     size_t oh[3], ol[3], os[3];
-    const size_t z0 = cv.off;
     for (int a = 0; a < 3; ++a) {
-        oh[a] = cv.take<uint16_t>((size_t)s.npw * k2);
-        ol[a] = cv.take<uint16_t>((size_t)s.npw * k2);
+        oh[a] = cv.take<uint16_t>(rg * k2);
+        ol[a] = cv.take<uint16_t>(rg * k2);
         os[a] = cv.take<float>((size_t)s.npw);
     }
-    const size_t z1 = cv.off;
     const size_t ocm = cv.take<float>((size_t)s.npw);
     CUDA_TRY(c, dalloc(&s.tcg_mem, cv.off));
-    CUDA_TRY(c, cudaMemsetAsync(s.tcg_mem + z0, 0, z1 - z0, st));  // K padding must read as zero
+    CUDA_TRY(c, cudaMemsetAsync(s.tcg_mem, 0, cv.off, st));  // padding rows and K padding read as zero
     s.tcg_proj = TcOperand{s.tcg_mem + o1h, s.tcg_mem + o1l, reinterpret_cast<float*>(s.tcg_mem + o1s), k1};
     for (int a = 0; a < 3; ++a)
         s.tcg_exp[a] = TcOperand{s.tcg_mem + oh[a], s.tcg_mem + ol[a], reinterpret_cast<float*>(s.tcg_mem + os[a]), k2};
@@ -789,14 +823,14 @@ static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec
 {
     const bool fp64 = prec == HPSI_PREC_FP64;
     size_t wl = local_ws(c, s, nb, fp64 ? sizeof(double2) : sizeof(float2));
-    size_t wn = fp64 ? nonlocal_ws<double2, double2>(s, nb, 1)
-                     : (is_tc(prec) ? tc_ws(s, nb, energy) : nonlocal_ws<float2, float2>(s, nb, 1));
+    if (is_tc(prec)) return wl + tc_ws(s, nb, energy);  // disjoint: the two halves run concurrently
+    size_t wn = fp64 ? nonlocal_ws<double2, double2>(s, nb, 1) : nonlocal_ws<float2, float2>(s, nb, 1);
     return std::max(wl, wn);
 }
 
 // hpsi += H psi on device pointers with an explicit workspace (prepare_slot first)
 static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, int prec, unsigned char* work,
-                     cudaStream_t st, double* epart = nullptr, double* e_nl = nullptr)
+                     cudaStream_t st, double* epart = nullptr, double* e_nl = nullptr, bool fork = true)
 {
     int rc;
     if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
@@ -804,8 +838,29 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         if ((rc = local_apply<double2, double>(c, s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st, epart))) return rc;
         return nonlocal_apply<double2, double2>(c, s, nb, psi, hpsi, s.pr64, work, st, e_nl);
     }
+    if (is_tc(prec) && s.P > 0 && nb > 0) {
+        // the projection chain on the side stream, beside the FFT passes; the
+        // expansion joins back after the r->G pass (both add into hpsi).  With
+        // fork false (the server's lanes already overlap) all runs on st.
+        unsigned char* wnl = work + local_ws(c, s, nb, sizeof(float2));
+        if (!fork) {
+            if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart)))
+                return rc;
+            if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, st, e_nl))) return rc;
+            return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr);
+        }
+        CUDA_TRY(c, cudaEventRecord(c->ev_fork, st));
+        CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, c->side, e_nl))) return rc;
+        CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
+        rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart);
+        // join even on failure, so that no work is left on the side stream unordered
+        const cudaError_t je = cudaStreamWaitEvent(st, c->ev_join, 0);
+        if (rc) return rc;
+        CUDA_TRY(c, je);
+        return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr);
+    }
     if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart))) return rc;
-    if (is_tc(prec)) return tc_nonlocal(c, s, nb, psi, hpsi, work, st, e_nl);
     return nonlocal_apply<float2, float2>(c, s, nb, psi, hpsi, s.pr32, work, st, e_nl);
 }
 
@@ -907,8 +962,8 @@ static VelWs vel_layout(const KSlot& s, int nb, int prec)
         w.k1 = tc_round_k(2 * (size_t)s.npw);
         // short FP32 accumulation chains in TMEM (FP64 sums of the splits)
         w.ns_tc = std::max(tc_proj_splits(nb, nb, w.k1), tc_chain_splits(w.k1, kVelocityChainK));
-        w.ah = g.take<uint16_t>((size_t)nb * w.k1);
-        w.al = g.take<uint16_t>((size_t)nb * w.k1);
+        w.ah = g.take<uint16_t>(tc_rows_pad(nb) * w.k1);
+        w.al = g.take<uint16_t>(tc_rows_pad(nb) * w.k1);
         w.as = g.take<float>((size_t)nb);
         w.bh = g.take<uint16_t>((size_t)NB * w.k1);
         w.bl = g.take<uint16_t>((size_t)NB * w.k1);
@@ -1991,7 +2046,7 @@ static int srv_issue(hpsi_server* S, SrvReq* r)
             r->err = cudaGetErrorString(e);
             return HPSI_ERR_CUDA;
         }
-        int rc = apply_dev(c, s, j.nb, psi, hpsi, S->prec, ws, st);
+        int rc = apply_dev(c, s, j.nb, psi, hpsi, S->prec, ws, st, nullptr, nullptr, false);
         if (!rc && j.vel) rc = velocity_dev(c, s, j.nb, psi, m, S->prec, ws, st);
         if (rc) { r->err = c->err; return rc; }
         if ((e = cudaMemcpyAsync(j.hpsi, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st))) {

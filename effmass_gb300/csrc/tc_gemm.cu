@@ -18,11 +18,11 @@
 // significand bits each, so hi+lo represents x to ~2^-22; BF16 pieces to ~2^-18.
 //
 // Kernel: one 128 x 256 output tile per CTA (cta_group::1, UMMA M=128, N=256,
-// K=16), 32-deep K stages loaded by TMA (SWIZZLE_64B) into four pipeline
-// stages of A_hi, A_lo, B_hi, B_lo; warp 0 issues TMA, warp 1 owns TMEM and
-// issues the MMAs from one thread, warps 2-5 drain TMEM.  Every mbarrier wait
-// is bounded; on timeout the CTA sets an error flag, drains and frees TMEM.
-#include <cuda.h>
+// K=16), 32-deep K stages of A_hi, A_lo, B_hi, B_lo in four pipeline stages,
+// filled by bulk copies of the pre-tiled operands (see tile_off); warp 0
+// issues the copies, warp 1 owns TMEM and issues the MMAs from one thread,
+// warps 2-5 drain TMEM.  Every mbarrier wait is bounded; on timeout the CTA
+// sets an error flag, drains and frees TMEM.
 #include <type_traits>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -39,6 +39,20 @@ constexpr int MAX_CHAIN_K = 3072;     // K depth of one split (FP32 accumulation
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr uint32_t TMEM_COLS = 512;  // two 256-column FP32 accumulators, alternating by k-tile
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
+static_assert(BK == 32 && BM == 128 && BN == 2 * BM, "tile_off assumes 128-row x 32-deep tiles");
+
+// Tiled operand layout.  The K-major operands are stored as 128-row x BK
+// tiles of 8 KB, each in the byte order that a TMA SWIZZLE_64B load would
+// leave in shared memory (row r at 64 r bytes, its 16-byte chunk c at chunk
+// c ^ ((r >> 1) & 3)), tiles ordered (row block, k block) with k fastest.  A
+// pipeline stage then fills with six 8 KB bulk copies of contiguous HBM
+// instead of tensor-map boxes of 64-byte rows a whole row stride apart.
+__host__ __device__ __forceinline__ size_t tile_off(size_t row, size_t k, size_t ldk)
+{
+    const size_t r = row & 127, kk = k & 31;
+    const size_t c = (kk >> 3) ^ ((r >> 1) & 3);
+    return (((row >> 7) * (ldk >> 5) + (k >> 5)) << 12) + (r << 5) + (c << 3) + (kk & 7);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -73,19 +87,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
     return false;
 }
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar)
+// bulk copy of bytes (multiple of 16, both addresses 16-byte aligned) from
+// global to shared memory, completing on an mbarrier transaction count
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
 {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// SMEM matrix descriptor for a K-major tile written by TMA with SWIZZLE_64B:
+// SMEM matrix descriptor for a K-major tile in the SWIZZLE_64B layout:
 // 8-row x 64-byte swizzle atoms stacked along M/N every 512 bytes (SBO);
 // LBO is not used by swizzled K-major layouts (encoded as 1).
 __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr)
@@ -149,9 +164,9 @@ struct TcSmem {
 //   1: expansion            hpsi[b][g] += (C[g][re] + i C[g][im]) * 2^-(sa[g] + sb[b])
 template <int MODE>
 __global__ void __launch_bounds__(192, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
-                   const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl, TcEpilogue ep,
-                   int M, int N, int ktiles_total, int ktiles_per_split, uint32_t idesc, int* err)
+    tc_gemm_kernel(const unsigned char* __restrict__ Ah, const unsigned char* __restrict__ Al,
+                   const unsigned char* __restrict__ Bh, const unsigned char* __restrict__ Bl, TcEpilogue ep, int M,
+                   int N, int ktiles_total, int ktiles_per_split, uint32_t idesc, int* err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned tile area
@@ -185,7 +200,12 @@ __global__ void __launch_bounds__(192, 1)
     const uint32_t tmem = sh->tmem_base;
 
     if (warp == 0 && lane == 0) {
-        // ---- TMA producer
+        // ---- bulk-copy producer: tiles (row block, k block) of the tiled operands
+        const size_t KT = (size_t)ktiles_total;
+        const unsigned char* ah = Ah + (size_t)blockIdx.x * KT * A_TILE;
+        const unsigned char* al = Al + (size_t)blockIdx.x * KT * A_TILE;
+        const unsigned char* bh = Bh + (size_t)(2 * blockIdx.y) * KT * A_TILE;  // 128-row blocks n0/128, +1
+        const unsigned char* bl = Bl + (size_t)(2 * blockIdx.y) * KT * A_TILE;
         int issued = 0;
         for (int it = 0; it < nk; ++it) {
             const int s = it % STAGES;
@@ -194,11 +214,13 @@ __global__ void __launch_bounds__(192, 1)
             if (*(volatile uint32_t*)&sh->abort_flag) break;
             unsigned char* st = tiles + s * STAGE_BYTES;
             mbar_arrive_expect_tx(&sh->full[s], STAGE_BYTES);
-            const int kx = (kt0 + it) * BK;
-            tma_load_2d(st, &tmAh, kx, m0, &sh->full[s]);
-            tma_load_2d(st + A_TILE, &tmAl, kx, m0, &sh->full[s]);
-            tma_load_2d(st + 2 * A_TILE, &tmBh, kx, n0, &sh->full[s]);
-            tma_load_2d(st + 2 * A_TILE + B_TILE, &tmBl, kx, n0, &sh->full[s]);
+            const size_t kt = (size_t)(kt0 + it);
+            bulk_load(st, ah + kt * A_TILE, A_TILE, &sh->full[s]);
+            bulk_load(st + A_TILE, al + kt * A_TILE, A_TILE, &sh->full[s]);
+            bulk_load(st + 2 * A_TILE, bh + kt * A_TILE, A_TILE, &sh->full[s]);
+            bulk_load(st + 3 * A_TILE, bh + (KT + kt) * A_TILE, A_TILE, &sh->full[s]);
+            bulk_load(st + 2 * A_TILE + B_TILE, bl + kt * A_TILE, A_TILE, &sh->full[s]);
+            bulk_load(st + 3 * A_TILE + B_TILE, bl + (KT + kt) * A_TILE, A_TILE, &sh->full[s]);
             issued = it + 1;
         }
         // drain: copies in flight must land before the CTA exits (bounded)
@@ -405,15 +427,14 @@ __global__ void split_rows_kernel(const S* __restrict__ pr, int npw, size_t ldk,
     mx = block_max(mx, red);
     const float sc = row_scale(mx, fp16);
     if (threadIdx.x == 0) inv_scale[p] = 1.f / sc;
-    T* h = hi + (size_t)p * ldk;
-    T* l = lo + (size_t)p * ldk;
     for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
         R x = 0;
         if (k < 2 * (size_t)npw) {
             S v = row[k >> 1];
             x = (k & 1) ? v.y : v.x;
         }
-        split_any(x, sc, h + k, l + k);
+        const size_t o = tile_off(p, k, ldk);
+        split_any(x, sc, hi + o, lo + o);
     }
 }
 
@@ -458,8 +479,9 @@ __global__ void transpose_split_kernel(const float2* __restrict__ pr, int P, int
         const int p = p0 + tx;
         const size_t k = koff + 2 * (size_t)p;
         if (k + 1 < ldk) {
-            split_store<T>(v.x * sc, hi + (size_t)g * ldk + k, lo + (size_t)g * ldk + k);
-            split_store<T>(v.y * sc, hi + (size_t)g * ldk + k + 1, lo + (size_t)g * ldk + k + 1);
+            const size_t o = tile_off(g, k, ldk);  // k even: k + 1 sits at o + 1
+            split_store<T>(v.x * sc, hi + o, lo + o);
+            split_store<T>(v.y * sc, hi + o + 1, lo + o + 1);
         }
     }
 }
@@ -549,10 +571,12 @@ __global__ void band_write_kernel(const S* __restrict__ src, int nb, int len, si
         split2<T>(a[e], ah[e], al[e]);
         split2<T>(c[e], ch[e], cl[e]);
     }
-    *reinterpret_cast<uint2*>(hi + rre * ldk + k) = *reinterpret_cast<const uint2*>(ah);
-    *reinterpret_cast<uint2*>(lo + rre * ldk + k) = *reinterpret_cast<const uint2*>(al);
-    *reinterpret_cast<uint2*>(hi + rim * ldk + k) = *reinterpret_cast<const uint2*>(ch);
-    *reinterpret_cast<uint2*>(lo + rim * ldk + k) = *reinterpret_cast<const uint2*>(cl);
+    // k = 4q .. 4q+3 lie in one 16-byte chunk of the tiled layout
+    const size_t ore = tile_off(rre, k, ldk), oim = tile_off(rim, k, ldk);
+    *reinterpret_cast<uint2*>(hi + ore) = *reinterpret_cast<const uint2*>(ah);
+    *reinterpret_cast<uint2*>(lo + ore) = *reinterpret_cast<const uint2*>(al);
+    *reinterpret_cast<uint2*>(hi + oim) = *reinterpret_cast<const uint2*>(ch);
+    *reinterpret_cast<uint2*>(lo + oim) = *reinterpret_cast<const uint2*>(cl);
 }
 
 template <typename T, typename S, bool FROM_W>
@@ -577,8 +601,8 @@ __global__ void zero_rows_kernel(int nb, int nbp, size_t ldk, T* hi, T* lo, floa
         const size_t r = (size_t)t * 256 + c * 128 + j;
         if (threadIdx.x == 0) inv_scale[r] = 1.f;
         for (size_t k = threadIdx.x; k < ldk; k += blockDim.x) {
-            hi[r * ldk + k] = T(0.f);
-            lo[r * ldk + k] = T(0.f);
+            hi[tile_off(r, k, ldk)] = T(0.f);
+            lo[tile_off(r, k, ldk)] = T(0.f);
         }
     }
 }
@@ -635,43 +659,11 @@ __global__ void __launch_bounds__(256) eterm_sum_kernel(int P, int nb, const dou
     }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn()
-{
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
-    return fn;
-}
-
-// 2-D map over a [rows][ldk] 16-bit matrix, box {64, box_rows}, 128B swizzle
-bool make_map(CUtensorMap* m, const void* base, size_t rows, size_t ldk, int box_rows, bool fp16)
-{
-    EncodeTiledFn fn = encode_fn();
-    if (!fn) return false;
-    cuuint64_t dims[2] = {(cuuint64_t)ldk, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)(ldk * 2)};
-    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(m, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
-                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
-
 }  // namespace
 
 size_t tc_round_k(size_t k) { return (k + BK - 1) / BK * BK; }
 int tc_band_rows(int nb) { return (nb + 127) / 128 * 256; }
+size_t tc_rows_pad(size_t rows) { return (rows + BM - 1) / BM * BM; }
 
 size_t tc_gemm_smem_bytes() { return (size_t)STAGES * STAGE_BYTES + 1024 + sizeof(TcSmem) + 64; }
 
@@ -795,28 +787,28 @@ int tc_proj_splits(int P, int nb, size_t ldk)
 }
 
 // A: rows M, B: rows N (= tc_band_rows(nb)); one launch
+// A: rows M, B: rows N (= tc_band_rows(nb)); one launch
 static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperand& B, int N, int nsplit, bool fp16,
                              const TcEpilogue& ep, int* err, cudaStream_t st)
 {
-    CUtensorMap mah, mal, mbh, mbl;
-    if (!make_map(&mah, A.hi, M, A.ldk, BM, fp16) || !make_map(&mal, A.lo, M, A.ldk, BM, fp16) ||
-        !make_map(&mbh, B.hi, N, B.ldk, BN, fp16) || !make_map(&mbl, B.lo, N, B.ldk, BN, fp16))
-        return cudaErrorInvalidValue;
+    if (A.ldk != B.ldk || A.ldk % BK) return cudaErrorInvalidValue;
     const int ktiles = (int)(A.ldk / BK);
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
     const size_t smem = tc_gemm_smem_bytes();
     dim3 grid(ceil_div(M, BM), N / BN, nz);
     const uint32_t idesc = idesc_f16(BM, BN, fp16 ? 0u : 1u);
+    const unsigned char *ah = (const unsigned char*)A.hi, *al = (const unsigned char*)A.lo;
+    const unsigned char *bh = (const unsigned char*)B.hi, *bl = (const unsigned char*)B.lo;
     cudaError_t e;
     if (mode == 0) {
         if ((e = cudaFuncSetAttribute(tc_gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
             return e;
-        tc_gemm_kernel<0><<<grid, 192, smem, st>>>(mah, mal, mbh, mbl, ep, M, N, ktiles, per, idesc, err);
+        tc_gemm_kernel<0><<<grid, 192, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err);
     } else {
         if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
             return e;
-        tc_gemm_kernel<1><<<grid, 192, smem, st>>>(mah, mal, mbh, mbl, ep, M, N, ktiles, per, idesc, err);
+        tc_gemm_kernel<1><<<grid, 192, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err);
     }
     return cudaGetLastError();
 }

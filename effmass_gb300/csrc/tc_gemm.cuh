@@ -3,8 +3,9 @@
 
 #include "kernels.cuh"
 
-// One split operand: hi and lo halves ([rows][ldk] FP16 or BF16, ldk a
-// multiple of 64) and the per-row factor that undoes its power-of-two scale.
+// One split operand: hi and lo halves (FP16 or BF16, tc_rows_pad(rows) x ldk
+// values in the tiled layout of tc_gemm.cu, ldk a multiple of 32) and the
+// per-row factor that undoes its power-of-two scale.
 struct TcOperand {
     void* hi = nullptr;
     void* lo = nullptr;
@@ -24,6 +25,7 @@ struct TcEpilogue {
 size_t tc_round_k(size_t k);   // K padded to the K depth of a pipeline stage
 int tc_chain_splits(size_t ldk, int chain_k);  // splits that keep every split's K depth <= chain_k
 int tc_band_rows(int nb);      // B rows for nb bands (re/im blocks of 128)
+size_t tc_rows_pad(size_t rows);  // rows of an operand allocation (whole 128-row tiles)
 size_t tc_gemm_smem_bytes();
 int tc_proj_splits(int P, int nb, size_t ldk);
 
