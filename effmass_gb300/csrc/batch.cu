@@ -363,6 +363,7 @@ static int build_group(hpsi_batch* b, Group& g)
         li.plane_off = pl + s.nxs;
         li.ent_ig = pl + 2 * s.nxs + 1;
         li.ent_jk = pl + 2 * s.nxs + 1 + s.npw;
+        li.plane_jr = pl + 2 * s.nxs + 1 + 2 * s.npw;
         li.kinetic = s.d_kin;
         li.psi = b->psi + it.off;
         li.hpsi = b->hpsi + it.off;

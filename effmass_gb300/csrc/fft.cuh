@@ -364,6 +364,63 @@ HPSI_D void fft_lines_cc(const LD& ld, const ST& st, const AB& A, const C* tw, i
     fft_stage_ct<C, PL::n, PL::r1, PL::r0, NLC>(A, st, unused, tw, sign);
 }
 
+// ---- pruned plane transforms --------------------------------------------
+// A sphere plane holds G-vectors only in the rows j with |G_y| <= jr: rows
+// 0..jr and n-jr..n-1.  The z-lines of the other rows are zero on input to
+// G->r and not read after r->G, so these transforms visit the nl = 2 jr + 1
+// rows in use: line L is row L (L <= jr) or row L + n - nl.
+template <typename C, int LS, int ES>
+struct SmemRowsC {
+    C* b;
+    int jr, gap;
+    HPSI_D int row(int L) const { return L + (L > jr ? gap : 0); }
+    HPSI_D C operator()(int L, int e) const { return b[row(L) * LS + e * ES]; }
+    HPSI_D void operator()(int L, int e, C v) const { b[row(L) * LS + e * ES] = v; }
+};
+
+// fft_stage_ct with a run-time line count nl: t / nl from one multiply by
+// rinv = 1/nl, exact for t < 2^12 and nl <= 2^8 (relative error of the
+// product <= 2^-23, so the absolute error <= 2^-11 < 0.5 / nl, the distance
+// of (t + 1/2) / nl from an integer)
+template <typename C, int N, int P, int NS, typename LD, typename ST>
+HPSI_D void fft_stage_rows(const LD& ld, const ST& st, int nl, float rinv, const C* tw, int sign)
+{
+    constexpr int nbf = N / P;
+    constexpr int tstep = N / (NS * P);
+    const int total = nl * nbf;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int i = (int)(((float)t + 0.5f) * rinv);
+        const int L = t - i * nl;
+        const int hi = i / NS;
+        const int k = i - hi * NS;
+        C v[HPSI_FFT_MAXR];
+#pragma unroll
+        for (int q = 0; q < P; ++q) v[q] = ld(L, i + q * nbf);
+        if (NS > 1 && k > 0) {
+#pragma unroll
+            for (int q = 1; q < P; ++q) v[q] = cmul(v[q], tw_get(tw, q * k * tstep, sign));
+        }
+        dft_small<C, P>(v, tw, N, sign);
+        const int base = hi * NS * P + k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) st(L, base + q * NS, v[q]);
+    }
+}
+
+// Two-stage transform of the rows in use (jr as above; 2 jr + 1 < n) of a
+// plane with line stride LS and element stride ES: in -> A -> out (in may be out)
+template <typename C, typename PL, int LS, int ES>
+HPSI_D void fft_rows_cc(C* in, C* out, C* A, int jr, const C* tw, int sign)
+{
+    const int nl = 2 * jr + 1, gap = PL::n - nl;
+    const float rinv = 1.0f / (float)nl;
+    fft_stage_rows<C, PL::n, PL::r0, 1>(SmemRowsC<C, LS, ES>{in, jr, gap}, SmemRowsC<C, LS, ES>{A, jr, gap}, nl, rinv,
+                                        tw, sign);
+    __syncthreads();
+    fft_stage_rows<C, PL::n, PL::r1, PL::r0>(SmemRowsC<C, LS, ES>{A, jr, gap}, SmemRowsC<C, LS, ES>{out, jr, gap}, nl,
+                                             rinv, tw, sign);
+}
+
 // Plan ids the host selects (0 = runtime plan)
 enum { FFT_CT_NONE = 0, FFT_CT_72 = 1, FFT_CT_36 = 2, FFT_CT_24 = 3, FFT_CT_64 = 4 };
 static inline int fft_ct_id(const FftLen& L)

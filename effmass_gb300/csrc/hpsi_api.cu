@@ -269,6 +269,13 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
         ent_jk[e] = jk[ig];
         aliased = aliased || !scatter;
     }
+    // rows in use per plane: |G_y| <= plane_jr[p], i.e. j <= jr or j >= n2 - jr
+    std::vector<int> plane_jr(nxs, 0);
+    for (int p = 0; p < nxs; ++p)
+        for (int e = plane_off[p]; e < plane_off[p + 1]; ++e) {
+            const int j = ent_jk[e] / n[2];
+            plane_jr[p] = std::max(plane_jr[p], std::min(j, n[1] - j));
+        }
 
     // --- projector rows
     std::vector<ProjRow> rows;
@@ -304,7 +311,7 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
         CUDA_TRY(c, dalloc(&s.d_q, (size_t)npw));
         CUDA_TRY(c, dalloc(&s.d_trig, (size_t)4 * npw));
         CUDA_TRY(c, dalloc(&s.d_ylm, (size_t)(grads ? 3 : 1) * nlm * npw));
-        CUDA_TRY(c, dalloc(&s.d_plane, (size_t)2 * nxs + 1 + 2 * (size_t)npw));
+        CUDA_TRY(c, dalloc(&s.d_plane, (size_t)3 * nxs + 1 + 2 * (size_t)npw));
         CUDA_TRY(c, cudaMemcpy(s.d_kin, kp->kinetic, npw * sizeof(double), cudaMemcpyHostToDevice));
         CUDA_TRY(c, cudaMemcpy(s.d_kvec, kp->kvec, 3 * npw * sizeof(double), cudaMemcpyHostToDevice));
         CUDA_TRY(c, cudaMemcpy(s.d_g, kp->g_idx, 3 * npw * sizeof(int), cudaMemcpyHostToDevice));
@@ -313,6 +320,7 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
         pl.insert(pl.end(), plane_off.begin(), plane_off.end());
         pl.insert(pl.end(), ent_ig.begin(), ent_ig.end());
         pl.insert(pl.end(), ent_jk.begin(), ent_jk.end());
+        pl.insert(pl.end(), plane_jr.begin(), plane_jr.end());
         CUDA_TRY(c, cudaMemcpy(s.d_plane, pl.data(), pl.size() * sizeof(int), cudaMemcpyHostToDevice));
 
         GTabArgs ga{npw, c->lmax, s.d_kvec, s.d_q, s.d_trig, s.d_ylm, grads ? s.d_ylm + (size_t)nlm * npw : nullptr,
@@ -429,6 +437,7 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     a.plane_off = pl + s.nxs;
     a.ent_ig = pl + 2 * s.nxs + 1;
     a.ent_jk = pl + 2 * s.nxs + 1 + s.npw;
+    a.plane_jr = pl + 2 * s.nxs + 1 + 2 * s.npw;
     a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
     const int ch = chunk_bands(s, c, nb, sizeof(C));
     C* T = reinterpret_cast<C*>(ws);
@@ -460,6 +469,7 @@ static int density_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, cons
     a.plane_off = pl + s.nxs;
     a.ent_ig = pl + 2 * s.nxs + 1;
     a.ent_jk = pl + 2 * s.nxs + 1 + s.npw;
+    a.plane_jr = pl + 2 * s.nxs + 1 + 2 * s.npw;
     a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
     const int ch = chunk_bands(s, c, nb, sizeof(C));
     C* T = reinterpret_cast<C*>(ws);
@@ -1812,6 +1822,7 @@ static int apply_noalloc_impl(hpsi_ctx* c, KSlot& s, int nb, const double2* psi,
         a.plane_off = s.d_plane + s.nxs;
         a.ent_ig = s.d_plane + 2 * s.nxs + 1;
         a.ent_jk = s.d_plane + 2 * s.nxs + 1 + s.npw;
+        a.plane_jr = s.d_plane + 2 * s.nxs + 1 + 2 * s.npw;
         a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
         const int ch = (int)std::min<size_t>((size_t)nb, cap / plane_bytes);
         for (int b0 = 0; b0 < nb; b0 += ch) {

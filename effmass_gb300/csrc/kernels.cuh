@@ -57,6 +57,7 @@ struct LocalItem {
     const int* plane_off;   // [nxs+1]
     const int* ent_ig;      // [npw]
     const int* ent_jk;      // [npw]
+    const int* plane_jr;    // [nxs] rows in use of plane p: |G_y| <= plane_jr[p]
     const double* kinetic;  // [npw]
     const double2* psi;     // [nb][npw]
     double2* hpsi;          // [nb][npw], accumulated
@@ -76,6 +77,7 @@ struct LocalArgs {
     const int* plane_off;   // [nxs+1] entry range of plane p
     const int* ent_ig;      // [npw] caller-order G index; negative = gather only
     const int* ent_jk;      // [npw] j*n3 + k of the entry
+    const int* plane_jr;    // [nxs] rows in use of plane p: |G_y| <= plane_jr[p] (null: all)
     FftLen Lx, Ly, Lz;
     FastDiv nl_z;           // z-lines of a plane: n2
     FastDiv nl_y;           // y-lines of a plane: n3

@@ -87,13 +87,13 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     const int p = blockIdx.x;
     int b = blockIdx.y;
     int npw = a.npw, nxs = a.nxs;
-    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk;
+    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk, *plane_jr = a.plane_jr;
     if (a.items) {  // batched: the band's item (uniform per block, before any barrier)
         const LocalItem I = a.items[a.band_item[b]];
         if (p >= I.nxs) return;
         b -= I.band0;
         npw = I.npw; nxs = I.nxs;
-        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk;
+        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk; plane_jr = I.plane_jr;
         psi = I.psi;
         T += I.t_off;
     }
@@ -126,7 +126,14 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
                            +1);
     } else {
         constexpr int N = PL::n, NP = PL::n + 1;  // n2 = n3 = N lines per axis
-        fft_lines_cc<C, PL, N>(SmemLinesC<C, NP, 1>{b0}, SmemLinesC<C, NP, 1>{zo}, SmemLinesC<C, NP, 1>{b1}, twz, +1);
+        // z-lines of the rows in use only: the other rows of b0 are zero and
+        // stay zero in zo (= b0 for these two-stage plans)
+        const int jr = plane_jr ? plane_jr[p] : N;
+        if (2 * jr + 1 < N && zo == b0)
+            fft_rows_cc<C, PL, NP, 1>(b0, zo, b1, jr, twz, +1);
+        else
+            fft_lines_cc<C, PL, N>(SmemLinesC<C, NP, 1>{b0}, SmemLinesC<C, NP, 1>{zo}, SmemLinesC<C, NP, 1>{b1}, twz,
+                                   +1);
         __syncthreads();
         fft_lines_cc<C, PL, N>(SmemLinesC<C, 1, NP>{zo}, PlaneGlobalC<C, N>{Tp}, SmemLinesC<C, 1, NP>{zother}, twy,
                                +1);
@@ -371,13 +378,13 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     const int p = blockIdx.x;
     int b = blockIdx.y;
     int npw = a.npw, nxs = a.nxs;
-    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk;
+    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk, *plane_jr = a.plane_jr;
     if (a.items) {  // batched: the band's item (uniform per block, before any barrier)
         const LocalItem I = a.items[a.band_item[b]];
         if (p >= I.nxs) return;
         b -= I.band0;
         npw = I.npw; nxs = I.nxs;
-        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk;
+        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk; plane_jr = I.plane_jr;
         psi = I.psi; hpsi = I.hpsi; kinetic = I.kinetic;
         T += I.t_off;
     }
@@ -401,8 +408,13 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
         constexpr int N = PL::n, NP = PL::n + 1;
         fft_lines_cc<C, PL, N>(PlaneGlobalC<C, N>{Tp}, SmemLinesC<C, 1, NP>{yo}, SmemLinesC<C, 1, NP>{b0}, twy, -1);
         __syncthreads();
-        fft_lines_cc<C, PL, N>(SmemLinesC<C, NP, 1>{yo}, SmemLinesC<C, NP, 1>{zo}, SmemLinesC<C, NP, 1>{yother}, twz,
-                               -1);
+        // z-lines of the rows in use only: the gather reads no other row
+        const int jr = plane_jr ? plane_jr[p] : N;
+        if (2 * jr + 1 < N)
+            fft_rows_cc<C, PL, NP, 1>(yo, zo, yother, jr, twz, -1);
+        else
+            fft_lines_cc<C, PL, N>(SmemLinesC<C, NP, 1>{yo}, SmemLinesC<C, NP, 1>{zo}, SmemLinesC<C, NP, 1>{yother},
+                                   twz, -1);
     }
     __syncthreads();
     const C* res = zo;
