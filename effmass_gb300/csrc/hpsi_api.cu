@@ -423,7 +423,8 @@ static int chunk_bands(const KSlot& s, const hpsi_ctx* c, int nb, size_t csize)
 
 template <typename C, typename V>
 static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
-                       const V* vloc, const C* tw, cudaStream_t st, double* epart = nullptr)
+                       const V* vloc, const C* tw, cudaStream_t st, double* epart = nullptr,
+                       float2* out32 = nullptr)
 {
     if (nb == 0 || s.npw == 0) return HPSI_OK;
     const int* pl = s.d_plane;
@@ -445,6 +446,7 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
         int nbc = std::min(ch, nb - b0);
         a.epart = epart;
         a.e_band0 = b0;
+        a.out32 = out32 ? out32 + (size_t)b0 * s.npw : nullptr;
         a.v64e = (epart && sizeof(V) == sizeof(float)) ? c->d_v64 : nullptr;
         CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
                                         tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
@@ -619,12 +621,12 @@ static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi
     return HPSI_OK;
 }
 
-// Expansion half: hpsi += P^T W
+// Expansion half: hpsi += P^T W (+ add32, the local term in complex64)
 static int tc_nonlocal_expand(hpsi_ctx* c, KSlot& s, int nb, double2* hpsi, unsigned char* ws, cudaStream_t st,
-                              bool energy)
+                              bool energy, const float2* add32)
 {
     TcNl t = tc_layout(s, nb, ws, energy);
-    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, t.B2, nb, s.tc_fmt == 0, hpsi, c->d_err, st, &c->prof));
+    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, t.B2, nb, s.tc_fmt == 0, hpsi, c->d_err, st, &c->prof, add32));
     return HPSI_OK;
 }
 
@@ -833,7 +835,12 @@ static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec
 {
     const bool fp64 = prec == HPSI_PREC_FP64;
     size_t wl = local_ws(c, s, nb, fp64 ? sizeof(double2) : sizeof(float2));
-    if (is_tc(prec)) return wl + tc_ws(s, nb, energy);  // disjoint: the two halves run concurrently
+    // disjoint: the two halves run concurrently; then the complex64 local term
+    if (is_tc(prec)) {
+        Carver cv;
+        cv.take<float2>((size_t)nb * s.npw);
+        return wl + tc_ws(s, nb, energy) + (s.P > 0 ? cv.off : 0);
+    }
     size_t wn = fp64 ? nonlocal_ws<double2, double2>(s, nb, 1) : nonlocal_ws<float2, float2>(s, nb, 1);
     return std::max(wl, wn);
 }
@@ -852,23 +859,27 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         // the projection chain on the side stream, beside the FFT passes; the
         // expansion joins back after the r->G pass (both add into hpsi).  With
         // fork false (the server's lanes already overlap) all runs on st.
-        unsigned char* wnl = work + local_ws(c, s, nb, sizeof(float2));
+        // The local term goes to a complex64 buffer (loc32) that the expansion
+        // adds with its own product: one FP64 read-modify-write of hpsi.
+        const size_t wl = local_ws(c, s, nb, sizeof(float2));
+        unsigned char* wnl = work + wl;
+        float2* loc32 = reinterpret_cast<float2*>(work + wl + tc_ws(s, nb, e_nl != nullptr));
         if (!fork) {
-            if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart)))
+            if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32)))
                 return rc;
             if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, st, e_nl))) return rc;
-            return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr);
+            return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32);
         }
         CUDA_TRY(c, cudaEventRecord(c->ev_fork, st));
         CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
         if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, c->side, e_nl))) return rc;
         CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
-        rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart);
+        rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32);
         // join even on failure, so that no work is left on the side stream unordered
         const cudaError_t je = cudaStreamWaitEvent(st, c->ev_join, 0);
         if (rc) return rc;
         CUDA_TRY(c, je);
-        return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr);
+        return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32);
     }
     if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart))) return rc;
     return nonlocal_apply<float2, float2>(c, s, nb, psi, hpsi, s.pr32, work, st, e_nl);

@@ -73,6 +73,8 @@ struct LocalArgs {
     int kt;                 // z-values per block in the x pass
     int bb;                 // bands per block in the x pass
     double inv_n;           // 1/(n1*n2*n3): the R2G normalisation
+    float2* out32;          // complex64 r->G gather: write kinetic*psi + grid/N here
+                            // ([nb][npw]) instead of adding it into hpsi (null: add)
     const int* plane_x;     // [nxs] grid x index of plane p
     const int* plane_off;   // [nxs+1] entry range of plane p
     const int* ent_ig;      // [npw] caller-order G index; negative = gather only

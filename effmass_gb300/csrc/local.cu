@@ -423,8 +423,9 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
     const int e0 = plane_off[p], e1 = plane_off[p + 1];
     if constexpr (std::is_same<C, float2>::value) {
         // complex64: kinetic*psi + grid/N in FP32 (conversions on the integer
-        // pipe), one FP64 add per component into hpsi
+        // pipe), one FP64 add per component into hpsi, or stored to out32
         const float inv_n = (float)a.inv_n;
+        float2* o32 = (a.out32 && !a.items) ? a.out32 + (size_t)b * npw : nullptr;
         for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
             int ig = ent_ig[e] & 0x7fffffff;
             int jk = ent_jk[e];
@@ -433,10 +434,14 @@ __global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plan
             const float2 s = to_c64(ps[ig]);
             const float kin = d2f_bits(kinetic[ig]);
             const float2 t = make_float2(fmaf(kin, s.x, g.x * inv_n), fmaf(kin, s.y, g.y * inv_n));
-            double2 h = hp[ig];
-            h.x += f2d_bits(t.x);
-            h.y += f2d_bits(t.y);
-            hp[ig] = h;
+            if (o32) {
+                o32[ig] = t;  // the tensor-core expansion adds it into hpsi
+            } else {
+                double2 h = hp[ig];
+                h.x += f2d_bits(t.x);
+                h.y += f2d_bits(t.y);
+                hp[ig] = h;
+            }
         }
     } else {
         for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {

@@ -288,6 +288,7 @@ __global__ void __launch_bounds__(192, 1)
                 }
             } else {
                 // columns [0,128): real parts of bands 128*blockIdx.y + j, [128,256): imaginary
+                const bool add = ep.add32 != nullptr;
 #pragma unroll 1
                 for (int c0 = 0; c0 < 128; c0 += 32) {
                     float re[32], im[32], w[32];
@@ -309,19 +310,23 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
                         for (int h0 = 0; h0 < 32; h0 += 16) {
                             double2 o[16];
+                            float2 ad[16];
                             float f[16];
+                            // loads only (predicated, no use), so that they all overlap
 #pragma unroll
                             for (int i = 0; i < 16; ++i) {
                                 const int b = b0 + h0 + i;
+                                const size_t at = (size_t)b * ep.ldh + row;
                                 f[i] = sa * ep.sb_scale[n0 + c0 + h0 + i];
-                                o[i] = b < ep.nb ? ep.hpsi[(size_t)b * ep.ldh + row] : make_double2(0.0, 0.0);
+                                o[i] = b < ep.nb ? ep.hpsi[at] : make_double2(0.0, 0.0);
+                                ad[i] = (add && b < ep.nb) ? ep.add32[at] : make_float2(0.f, 0.f);
                             }
 #pragma unroll
                             for (int i = 0; i < 16; ++i) {
                                 const int b = b0 + h0 + i;
                                 if (b < ep.nb) {
-                                    o[i].x += f2d_bits(re[h0 + i] * f[i]);
-                                    o[i].y += f2d_bits(im[h0 + i] * f[i]);
+                                    o[i].x += f2d_bits(fmaf(re[h0 + i], f[i], ad[i].x));
+                                    o[i].y += f2d_bits(fmaf(im[h0 + i], f[i], ad[i].y));
                                     ep.hpsi[(size_t)b * ep.ldh + row] = o[i];
                                 }
                             }
@@ -618,17 +623,20 @@ __global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float
     const int t = b / 128, j = b % 128;
     const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
     if constexpr (std::is_same<CW, float2>::value) {
-        if (!eterm) {
-            Sum2f re, im;  // complex64 W: compensated FP32 sums, no FP64 pipe
-            for (int z = 0; z < nsplit; ++z) {
-                const float* row = part + ((size_t)z * P + p) * N;
-                re.add(row[cre]);
-                im.add(row[cim]);
-            }
-            const float f = lam ? d2f_bits(lam[p % period]) : 1.f;
-            W[idx] = make_float2(f * re.value(), f * im.value());
-            return;
+        Sum2f re, im;  // complex64 W: compensated FP32 sums, no FP64 pipe
+        for (int z = 0; z < nsplit; ++z) {
+            const float* row = part + ((size_t)z * P + p) * N;
+            re.add(row[cre]);
+            im.add(row[cim]);
         }
+        const float f = lam ? d2f_bits(lam[p % period]) : 1.f;
+        W[idx] = make_float2(f * re.value(), f * im.value());
+        if (eterm) {
+            // lambda_p |<p|psi_b>|^2 in FP64 from the two-float sums
+            const double sr = f2d_bits(re.s) + f2d_bits(re.c), si = f2d_bits(im.s) + f2d_bits(im.c);
+            eterm[idx] = (lam ? lam[p % period] : 1.0) * (sr * sr + si * si);
+        }
+        return;
     }
     double sr = 0.0, si = 0.0;
     for (int z = 0; z < nsplit; ++z) {
@@ -867,11 +875,12 @@ cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, 
 }
 
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi,
-                         int* err, cudaStream_t st, Prof* prof)
+                         int* err, cudaStream_t st, Prof* prof, const float2* add32)
 {
     const int N = tc_band_rows(nb);
     TcEpilogue ep{};
     ep.hpsi = hpsi;
+    ep.add32 = add32;
     ep.ldh = npw;
     ep.nb = nb;
     ep.sa_scale = A.inv_scale;

@@ -20,6 +20,7 @@ struct TcEpilogue {
     int nb;
     const float* sa_scale;     // per A row
     const float* sb_scale;     // per B row
+    const float2* add32;       // mode 1: optional [nb][ldh] term added with the product
 };
 
 size_t tc_round_k(size_t k);   // K padded to the K depth of a pipeline stage
@@ -53,6 +54,6 @@ cudaError_t tc_rows_operand(const double2* x, int rows, int npw, bool fp16, TcOp
 // out[m][n] = sum_G conj(A[m][G]) B[n][G] in complex128 (B a band operand of nb rows)
 cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                          double2* out, int* err, cudaStream_t st);
-// hpsi[b][G] += sum_p W[p][b] Pr[p][G]
+// hpsi[b][G] += sum_p W[p][b] Pr[p][G] (+ add32[b][G] when given, summed in FP32 first)
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
-                         cudaStream_t st, Prof* prof);
+                         cudaStream_t st, Prof* prof, const float2* add32 = nullptr);
