@@ -284,10 +284,14 @@ def run_gb300(args, rank, world, local):
     steps = args.steps
     N = sysm.n1 * sysm.n2 * sysm.n3
     alg = {
-        # bytes the pass must move per step (band block) — see DESIGN.md, "Roofline units"
+        # bytes the pass must move per step (band block): g2r reads psi (16 B per
+        # G) and writes the sphere planes of T; the x pass reads and writes them
+        # (+ V once); r2g reads them, psi and the kinetic energies (8 B) and, on
+        # the tensor-core path, writes the complex64 local term (8 B) that the
+        # expansion adds into hpsi, else reads and writes hpsi (2 x 16 B)
         "g2r_planes": ("hbm", steps * nb * (npw * 16 + plane)),
         "x_pass": ("hbm", steps * (nb * 2 * plane + N * csz // 2)),
-        "r2g_planes": ("hbm", steps * nb * (plane + 3 * npw * 16 + npw * 8)),
+        "r2g_planes": ("hbm", steps * nb * (plane + npw * (16 + 8 + (8 if args.prec.startswith("tc") else 32)))),
         # algorithmic flops: 8 real flops per complex multiply-add
         "proj_gemm": ("tensor", steps * 8.0 * P * npw * nb),
         "expand_gemm": ("tensor", steps * 8.0 * P * npw * nb),
@@ -303,15 +307,15 @@ def run_gb300(args, rank, world, local):
         ach = work / (tms * 1e-3) / 1e12
         roof = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "peak_source": src + " dense bf16 tensor peak"}
-    # DRAM bytes (read + write) of one launch from the ncu capture summarised in
-    # profiles/ncu_full_fft_tc_sc64_nb32.md (same kernel, 32 bands per launch,
-    # which is also the x pass's per-launch band chunk here)
-    ncu_traffic = {"x_pass": 58.1e6}
+    # DRAM bytes (read + write) of one launch of this workload (128 bands per
+    # launch, 64-atom cell, tensor-core path) from an ncu --set full capture of
+    # this bench command: x pass 219.2 MB read + 162.3 MB written
+    ncu_traffic = {"x_pass": 381.45e6}
     roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec != "fp64") else None
     if roof["traffic"] is not None and bound == "hbm":
         roof["algorithmic_bytes_per_launch"] = alg[dom][1] / prof[dom][1]
         roof["traffic_note"] = "ncu dram__bytes_read+write of one launch; below the algorithmic bytes because " \
-                               "the launch's writes are still in the 129 MB L2 when it ends"
+                               "part of the launch's writes are still in the 129 MB L2 when it ends"
     # the tensor-core projection GEMM, reported beside the dominant phase
     roof_gemm = None
     if prof["proj_gemm"][1]:
