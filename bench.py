@@ -17,6 +17,7 @@ With --gpus N > 1 (launched under torchrun) every rank runs an independent
 replica of the workload (no collective on the data path); value is the sum.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -71,36 +72,75 @@ def workload(name, nb):
 class Clocks:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 50
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
+
+    def _rows(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        return rows
 
     def start(self):
+        """Start sampling and wait (at most 5 s) for the first sample, so that the
+        sampler is running when the timed region begins."""
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        t_end = time.time() + 5.0
+        while time.time() < t_end and not self._rows():
+            time.sleep(0.02)
+
+    def mark(self, begin: bool):
+        if begin:
+            self.t0 = datetime.datetime.now()
+        else:
+            self.t1 = datetime.datetime.now()
 
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        # one more interval, so that a sample follows the end of the region
+        time.sleep(2 * self.INTERVAL_MS / 1000)
         self.proc.terminate()
         self.proc.wait()
-        rows = []
-        for line in open(self.path):
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
+        all_rows = self._rows()
         os.unlink(self.path)
+        # samples inside the timed region, widened by one interval on each side
+        # (a region of a few ms falls between two samples)
+        rows = []
+        parsed = 0
+        pad = datetime.timedelta(milliseconds=self.INTERVAL_MS)
+        for r in all_rows:
+            try:
+                t = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                continue
+            parsed += 1
+            if self.t0 is None or self.t1 is None or self.t0 - pad <= t <= self.t1 + pad:
+                rows.append(r)
+        window = "timed region +- %d ms" % self.INTERVAL_MS
+        if not parsed:  # unreadable timestamps: every sample taken while sampling ran
+            rows, window = all_rows, "whole sampling run"
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -108,7 +148,7 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "window": window}
 
 
 def peaks():
@@ -158,11 +198,13 @@ def run_gb300(args, rank, world, local):
     clocks = Clocks(local)
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.mark(True)
     e0.record(stream)
     for _ in range(args.steps):
         step(args.prec)
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark(False)
     clk = clocks.stop()
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
@@ -172,10 +214,13 @@ def run_gb300(args, rank, world, local):
         ms = float(t.item())
     value = world * nb / (ms * 1e-3)
 
-    # per-phase CUDA-event profile over the same number of steps
+    # per-phase CUDA-event profile over the same number of steps, with the
+    # tensor-core projection chain on the launching stream (HPSI_ONE_STREAM):
+    # on its side stream its events would also count the time it waits for
+    # SMs behind the FFT passes
     H.profile(True)
     for _ in range(args.steps):
-        step(args.prec)
+        H.apply(0, nb, psi_d, hpsi_d, args.prec, one_stream=True)
     prof = H.profile_read()
     H.profile(False)
     launches = sum(n for _, n in prof.values())

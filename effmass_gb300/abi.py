@@ -26,6 +26,7 @@ HPSI_PREC_TC = 2
 HPSI_PREC_TC_BF16 = 3
 HPSI_DEVICE_PTRS = 0x10
 HPSI_SYNC = 0x20
+HPSI_ONE_STREAM = 0x40
 HPSI_BATCH_NO_GRAPH = 0x100
 HPSI_BATCH_NO_TUNE = 0x200
 HPSI_NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024

@@ -910,7 +910,7 @@ static EnergyWs energy_layout(const hpsi_ctx* c, int nb, int prec)
 
 // hpsi += H psi and e[b] = <psi_b|H|psi_b> with FP64 reductions, device pointers
 static int energies_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, double* e, int prec,
-                        unsigned char* ws, cudaStream_t st)
+                        unsigned char* ws, cudaStream_t st, bool fork = true)
 {
     int rc;
     if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
@@ -932,7 +932,7 @@ static int energies_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, doubl
     int h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, launch_kin_norm(s.npw, nb, psi, s.d_kin, kn, st));
     c->prof.close(h, st);
-    if ((rc = apply_dev(c, s, nb, psi, hpsi, prec, ws + w.work, st, epart, enl))) return rc;
+    if ((rc = apply_dev(c, s, nb, psi, hpsi, prec, ws + w.work, st, epart, enl, fork))) return rc;
     h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, launch_local_sums(nb, w.nslots, epart, loc, st));
     CUDA_TRY(c, launch_energy_combine(nb, kn, loc, s.P > 0 ? enl : nullptr, e, st));
@@ -1080,7 +1080,9 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
         CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
     }
-    if ((rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st))) return rc;
+    if ((rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st, nullptr, nullptr,
+                        !(flags & HPSI_ONE_STREAM))))
+        return rc;
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
     if (!dev || (flags & HPSI_SYNC)) {
         CUDA_TRY(c, cudaStreamSynchronize(st));
@@ -1123,7 +1125,8 @@ extern "C" int hpsi_apply_energies(hpsi_ctx* c, int kid, int nb, const double* p
         CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
     }
-    if ((rc = energies_dev(c, *s, nb, psi, hpsi, e, prec, c->ws + o_work, st))) return rc;
+    if ((rc = energies_dev(c, *s, nb, psi, hpsi, e, prec, c->ws + o_work, st, !(flags & HPSI_ONE_STREAM))))
+        return rc;
     if (!dev) {
         CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(c, cudaMemcpyAsync(eout, e, nb * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -142,14 +142,16 @@ class Hamiltonian:
         return {name: (ms[i], int(n[i])) for i, name in enumerate(self.PHASES)}
 
     # -- raw calls --
-    def apply(self, kid: int, nb: int, psi, hpsi, precision: Optional[str] = None):
+    def apply(self, kid: int, nb: int, psi, hpsi, precision: Optional[str] = None, one_stream: bool = False):
+        """hpsi += H psi.  one_stream: keep the tensor-core projection chain on the
+        caller's stream (HPSI_ONE_STREAM) instead of the side stream."""
         npw = self.dim(kid)
         p, dev_p = _ptr(psi, npw, nb, "psi")
         h, dev_h = _ptr(hpsi, npw, nb, "hpsi")
         if dev_p != dev_h:
             raise HpsiError(abi.HPSI_ERR_BAD_ARG, "psi and hpsi must both be host or both be device arrays")
-        check(self._lib.hpsi_apply(self._ctx, kid, nb, p, h, self.flags(precision, dev_p), _stream_for(dev_p)),
-              self._ctx)
+        f = self.flags(precision, dev_p) | (abi.HPSI_ONE_STREAM if one_stream else 0)
+        check(self._lib.hpsi_apply(self._ctx, kid, nb, p, h, f, _stream_for(dev_p)), self._ctx)
 
     def apply_energies(self, kid: int, nb: int, psi, hpsi, precision: Optional[str] = None, e=None):
         """hpsi += H psi and return e[b] = <psi_b|H|psi_b> (FP64 reductions on the device)."""

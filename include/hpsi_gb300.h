@@ -71,6 +71,9 @@ extern "C" {
 #define HPSI_PREC_MASK    0xF
 #define HPSI_DEVICE_PTRS  0x10 /* psi/outputs are device pointers (else host memory) */
 #define HPSI_SYNC         0x20 /* synchronise `stream` before returning */
+#define HPSI_ONE_STREAM   0x40 /* tensor-core hpsi_apply / hpsi_apply_energies: run the
+                                * projection chain on `stream` too instead of on the
+                                * context's side stream beside the FFT passes */
 
 /* One pseudopotential species after the per-l diagonalisation of D
  * (src/pseudo/ncpp_advance.cppm:65-153): projector i has angular momentum

@@ -137,3 +137,16 @@ def test_invalid_system_rejected_before_device_use(lib):
         Hamiltonian(sysm)
     assert ei.value.status == abi.HPSI_ERR_BAD_ARG
     assert "FFT length" in str(ei.value)
+
+
+def test_header_constants_match_abi():
+    """Every numeric #define of include/hpsi_gb300.h that abi.py mirrors has the same value."""
+    import re
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "hpsi_gb300.h")).read()
+    found = 0
+    for name, val in re.findall(r"#define\s+(HPSI_\w+)\s+(0x[0-9A-Fa-f]+|-?\d+)", hdr):
+        if hasattr(abi, name):
+            assert getattr(abi, name) == int(val, 0), name
+            found += 1
+    assert found >= 10
