@@ -30,9 +30,23 @@ template <typename C> struct Cfg;
 template <> struct Cfg<float2> { static constexpr int plane_threads = 512, plane_min = 2, x_min = 4; };
 template <> struct Cfg<double2> { static constexpr int plane_threads = 256, plane_min = 1, x_min = 1; };
 
+// Plan tag of the kernels that run the runtime FFT plans
+struct NoPlan {};
+
+// Resident x-pass blocks per SM (the launch-bounds minimum): the complex64
+// compile-time plans fit 48 registers without spills, so five 256-thread
+// blocks (62.5% of the warp slots; ~39 KB of shared memory each) share an
+// SM; the runtime-plan and wide-radix kernels keep their larger budgets.
+template <typename C, bool WIDE, typename PL>
+constexpr int xpass_min()
+{
+    if constexpr (WIDE) return (Cfg<C>::x_min + 1) / 2;
+    else if constexpr (std::is_same<C, float2>::value && !std::is_same<PL, NoPlan>::value) return 5;
+    else return Cfg<C>::x_min;
+}
+
 // Transform of a kernel's lines: the runtime plan (NoPlan) or a compile-time
 // two-stage plan (FftPlan2) chosen by the host for common grid lengths.
-struct NoPlan {};
 template <typename C, bool WIDE, typename PL, typename LD, typename ST>
 HPSI_D void lines(const LD& ld, const ST& st, C* bufA, C* bufB, const FftLen& L, const FastDiv& nlf, int ls, int es,
                   const C* tw, int sign)
@@ -200,7 +214,7 @@ struct XStore {
 };
 
 template <typename C, typename V, bool WIDE, bool ENERGY, typename PL, int KTC>
-__global__ void __launch_bounds__(256, WIDE ? (Cfg<C>::x_min + 1) / 2 : Cfg<C>::x_min) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
+__global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArgs a, int nb, C* __restrict__ T, const V* __restrict__ vloc,
                                               const C* __restrict__ tw_x_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
