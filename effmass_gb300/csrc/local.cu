@@ -23,12 +23,18 @@
 #include "fft.cuh"
 #include "kernels.cuh"
 
-// Launch shape per precision: complex64 kernels run 512-thread plane blocks
-// (two per SM) and four x-pass blocks per SM; complex128 kernels keep the
-// register budget of one block per SM.
+// Launch shape per precision: complex64 kernels run two plane blocks per SM
+// (768-thread G->r, 512-thread r->G) and four or five x-pass blocks per SM;
+// complex128 kernels keep the register budget of one block per SM.
 template <typename C> struct Cfg;
-template <> struct Cfg<float2> { static constexpr int plane_threads = 512, plane_min = 2, x_min = 4; };
-template <> struct Cfg<double2> { static constexpr int plane_threads = 256, plane_min = 1, x_min = 1; };
+template <> struct Cfg<float2> {
+    // g2r_planes fits 40 registers without spills at 768 threads (two blocks,
+    // 48 warps per SM); r2g_planes would spill there and keeps 512
+    static constexpr int plane_threads = 512, g2r_threads = 768, plane_min = 2, x_min = 4;
+};
+template <> struct Cfg<double2> {
+    static constexpr int plane_threads = 256, g2r_threads = 256, plane_min = 1, x_min = 1;
+};
 
 // Plan tag of the kernels that run the runtime FFT plans
 struct NoPlan {};
@@ -89,7 +95,7 @@ HPSI_D int plan_n(int runtime)
 }
 
 template <typename C, bool WIDE, typename PL>
-__global__ void __launch_bounds__(Cfg<C>::plane_threads, WIDE ? 1 : Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
+__global__ void __launch_bounds__(Cfg<C>::g2r_threads, WIDE ? 1 : Cfg<C>::plane_min) g2r_planes(LocalArgs a, const double2* __restrict__ psi, C* __restrict__ T,
                                                   const C* __restrict__ tw_y_g, const C* __restrict__ tw_z_g)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -545,8 +551,9 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
     dim3 gp(a.nxs, nb);
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
+    const int ptg = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::g2r_threads;
     int h = prof->open(PH_G2R, st);
-    g2r<<<gp, pt, sp, st>>>(a, psi, T, twy, twz);
+    g2r<<<gp, ptg, sp, st>>>(a, psi, T, twy, twz);
     prof->close(h, st);
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
@@ -644,8 +651,8 @@ static cudaError_t launch_density_t(const LocalArgs& a, int nb, const double2* p
     if ((e = cudaFuncSetAttribute(g2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))) return e;
     if ((e = cudaFuncSetAttribute(xd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
-    const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
-    g2r<<<dim3(a.nxs, nb), pt, sp, st>>>(a, psi, T, twy, twz);
+    const int ptg = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::g2r_threads;
+    g2r<<<dim3(a.nxs, nb), ptg, sp, st>>>(a, psi, T, twy, twz);
     xd<<<dim3(ceil_div(a.n3, a.kt), a.n2), 256, sx, st>>>(a, nb, T, occ, rho, twx);
     return cudaGetLastError();
 }
