@@ -96,6 +96,10 @@ struct hpsi_ctx {
     // beside the FFT passes (fork/join by events on the caller's stream)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // copy stream of hpsi_apply with host buffers: the H2D copy of hpsi, which
+    // only the tensor-core expansion reads, runs beside the FFT passes
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_copy_after = nullptr, ev_copy_done = nullptr;
     long gen_counter = 0;         // source of KSlot::gen
     double* d_hess = nullptr;     // Hessian radial tables [nrad][3][hess_nq] (F0, F1, F3), raw
     int hess_nq = 0;

@@ -42,6 +42,9 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     if (c->side) cudaStreamDestroy(c->side);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->ev_copy_after) cudaEventDestroy(c->ev_copy_after);
+    if (c->ev_copy_done) cudaEventDestroy(c->ev_copy_done);
     for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof.pool) cudaEventDestroy(e);
     delete c;
@@ -126,6 +129,9 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
     CUDA_TRY(c, cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_copy_after, cudaEventDisableTiming));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_copy_done, cudaEventDisableTiming));
     CUDA_TRY(c, dalloc(&c->d_err, (size_t)1));
     CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
     const size_t N = (size_t)c->n1 * c->n2 * c->n3;
@@ -846,8 +852,11 @@ static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec
 }
 
 // hpsi += H psi on device pointers with an explicit workspace (prepare_slot first)
+// hpsi_ready: an event after which hpsi holds its input (an H2D copy on
+// another stream); only the tensor-core expansion reads hpsi, so only it waits
 static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, int prec, unsigned char* work,
-                     cudaStream_t st, double* epart = nullptr, double* e_nl = nullptr, bool fork = true)
+                     cudaStream_t st, double* epart = nullptr, double* e_nl = nullptr, bool fork = true,
+                     cudaEvent_t hpsi_ready = nullptr)
 {
     int rc;
     if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
@@ -855,6 +864,8 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         if ((rc = local_apply<double2, double>(c, s, nb, psi, hpsi, work, c->d_v64, c->d_tw64, st, epart))) return rc;
         return nonlocal_apply<double2, double2>(c, s, nb, psi, hpsi, s.pr64, work, st, e_nl);
     }
+    if (hpsi_ready && !(is_tc(prec) && s.P > 0 && nb > 0 && fork))
+        CUDA_TRY(c, cudaStreamWaitEvent(st, hpsi_ready, 0));  // the other paths read hpsi from the start
     if (is_tc(prec) && s.P > 0 && nb > 0) {
         // the projection chain on the side stream, beside the FFT passes; the
         // expansion joins back after the r->G pass (both add into hpsi).  With
@@ -877,8 +888,10 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32);
         // join even on failure, so that no work is left on the side stream unordered
         const cudaError_t je = cudaStreamWaitEvent(st, c->ev_join, 0);
+        const cudaError_t ce = hpsi_ready ? cudaStreamWaitEvent(st, hpsi_ready, 0) : cudaSuccess;
         if (rc) return rc;
         CUDA_TRY(c, je);
+        CUDA_TRY(c, ce);
         return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32);
     }
     if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart))) return rc;
@@ -1074,15 +1087,30 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
     if ((rc = ws_reserve(c, o_work + apply_ws_bytes(c, *s, nb, prec)))) return rc;
     const double2* psi = (const double2*)psi_;
     double2* hpsi = (double2*)hpsi_;
+    const bool fork = !(flags & HPSI_ONE_STREAM);
+    cudaEvent_t hpsi_ready = nullptr;
     if (!dev) {
         psi = reinterpret_cast<const double2*>(c->ws + o_psi);
         hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
         CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        if (fork && is_tc(prec) && s->P > 0) {
+            // hpsi is read only by the expansion at the end: copy it on the copy
+            // stream, after the work already queued on st (which may still use
+            // the staging area), beside the FFT passes
+            CUDA_TRY(c, cudaEventRecord(c->ev_copy_after, st));
+            CUDA_TRY(c, cudaStreamWaitEvent(c->copy, c->ev_copy_after, 0));
+            CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, c->copy));
+            CUDA_TRY(c, cudaEventRecord(c->ev_copy_done, c->copy));
+            hpsi_ready = c->ev_copy_done;
+        } else {
+            CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+        }
     }
-    if ((rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st, nullptr, nullptr,
-                        !(flags & HPSI_ONE_STREAM))))
+    rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st, nullptr, nullptr, fork, hpsi_ready);
+    if (rc) {
+        if (hpsi_ready) cudaStreamWaitEvent(st, hpsi_ready, 0);  // leave no copy unordered behind st
         return rc;
+    }
     if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
     if (!dev || (flags & HPSI_SYNC)) {
         CUDA_TRY(c, cudaStreamSynchronize(st));
