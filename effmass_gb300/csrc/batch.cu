@@ -258,14 +258,18 @@ static int tune_group(hpsi_batch* b, Group& g)
     }
     set_xshape(g, bk, bbb);
     if ((rc = upload_xblk(b, g))) return rc;
+    // plane blocks: a candidate replaces the default block size (timed in the
+    // x-pass search above, bpt = 0) only when it is faster
     int bpt = 0;
-    const int pmax = fp64(b) ? 256 : 512;
-    for (int pt : {pmax / 4, pmax / 2, pmax}) {
+    static const int kPlaneThreads64[] = {64, 128, 256, 0}, kPlaneThreads32[] = {128, 256, 512, 768};
+    const int* cand = fp64(b) ? kPlaneThreads64 : kPlaneThreads32;
+    for (int ci = 0; ci < 4 && cand[ci] > 0; ++ci) {
+        const int pt = cand[ci];
         g.la.plane_threads = pt;
         double ms;
         if ((rc = time_ms(b, st, reps, [&] { return launch_group_local(b, g, st); }, &ms))) return rc;
         ++t.candidates;
-        if (ms < best || bpt == 0) { best = std::min(best, ms); bpt = pt; }
+        if (ms < best) { best = ms; bpt = pt; }
     }
     g.la.plane_threads = bpt;
     t.kt = bk; t.bb = bbb; t.plane_threads = bpt; t.local_ms = best;
