@@ -430,7 +430,7 @@ static int chunk_bands(const KSlot& s, const hpsi_ctx* c, int nb, size_t csize)
 template <typename C, typename V>
 static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
                        const V* vloc, const C* tw, cudaStream_t st, double* epart = nullptr,
-                       float2* out32 = nullptr)
+                       float2* out32 = nullptr, unsigned* rowmax = nullptr, cudaEvent_t after_g2r = nullptr)
 {
     if (nb == 0 || s.npw == 0) return HPSI_OK;
     const int* pl = s.d_plane;
@@ -453,6 +453,8 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
         a.epart = epart;
         a.e_band0 = b0;
         a.out32 = out32 ? out32 + (size_t)b0 * s.npw : nullptr;
+        a.rowmax = rowmax ? rowmax + b0 : nullptr;
+        a.after_g2r = b0 == 0 ? after_g2r : nullptr;
         a.v64e = (epart && sizeof(V) == sizeof(float)) ? c->d_v64 : nullptr;
         CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
                                         tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
@@ -612,12 +614,12 @@ static TcNl tc_layout(const KSlot& s, int nb, unsigned char* ws, bool energy)
 
 // Projection half: split psi, W = lambda <p|psi> (+ nonlocal energies), split W
 static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, unsigned char* ws,
-                               cudaStream_t st, double* e_nl)
+                               cudaStream_t st, double* e_nl, bool have_max = false)
 {
     const bool fp16 = s.tc_fmt == 0;
     TcNl t = tc_layout(s, nb, ws, e_nl != nullptr);
     int h = c->prof.open(PH_OTHER, st);
-    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &t.B1, t.rowmax, st));
+    CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &t.B1, t.rowmax, st, have_max));
     c->prof.close(h, st);
     CUDA_TRY(c, tc_projection(s.tc_proj, s.P, t.B1, nb, t.ns, fp16, t.part, s.d_lam, s.P, t.W, c->d_err, st,
                               &c->prof, t.eterm, e_nl));
@@ -875,23 +877,33 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         const size_t wl = local_ws(c, s, nb, sizeof(float2));
         unsigned char* wnl = work + wl;
         float2* loc32 = reinterpret_cast<float2*>(work + wl + tc_ws(s, nb, e_nl != nullptr));
+        // The G->r pass takes the per-band maxima of psi that scale the band
+        // operand when it covers all bands in one launch
+        unsigned* rowmax = tc_layout(s, nb, wnl, e_nl != nullptr).rowmax;
+        const bool g2r_max = chunk_bands(s, c, nb, sizeof(float2)) >= nb;
+        if (g2r_max) CUDA_TRY(c, cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * nb, st));
+        unsigned* rm = g2r_max ? rowmax : nullptr;
         if (!fork) {
-            if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32)))
+            if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32,
+                                                 rm)))
                 return rc;
-            if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, st, e_nl))) return rc;
+            if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, st, e_nl, g2r_max))) return rc;
             return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32);
         }
-        CUDA_TRY(c, cudaEventRecord(c->ev_fork, st));
-        CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
-        if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, c->side, e_nl))) return rc;
-        CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
-        rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32);
-        // join even on failure, so that no work is left on the side stream unordered
-        const cudaError_t je = cudaStreamWaitEvent(st, c->ev_join, 0);
-        const cudaError_t ce = hpsi_ready ? cudaStreamWaitEvent(st, hpsi_ready, 0) : cudaSuccess;
+        // fork after the G->r pass when it takes the maxima, else right away
+        if (!g2r_max) CUDA_TRY(c, cudaEventRecord(c->ev_fork, st));
+        rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32, rm,
+                                        g2r_max ? c->ev_fork : nullptr);
         if (rc) return rc;
-        CUDA_TRY(c, je);
-        CUDA_TRY(c, ce);
+        CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, c->side, e_nl, g2r_max))) {
+            cudaEventRecord(c->ev_join, c->side);  // still join, so that no work is left unordered
+            cudaStreamWaitEvent(st, c->ev_join, 0);
+            return rc;
+        }
+        CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
+        CUDA_TRY(c, cudaStreamWaitEvent(st, c->ev_join, 0));
+        if (hpsi_ready) CUDA_TRY(c, cudaStreamWaitEvent(st, hpsi_ready, 0));
         return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32);
     }
     if ((rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart))) return rc;

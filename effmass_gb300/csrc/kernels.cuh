@@ -75,6 +75,9 @@ struct LocalArgs {
     double inv_n;           // 1/(n1*n2*n3): the R2G normalisation
     float2* out32;          // complex64 r->G gather: write kinetic*psi + grid/N here
                             // ([nb][npw]) instead of adding it into hpsi (null: add)
+    unsigned* rowmax;       // complex64 G->r: per band, atomicMax of the float bits of
+                            // |re|, |im| of psi (zeroed before; null: not taken)
+    cudaEvent_t after_g2r;  // host side: recorded on the stream after the G->r launch
     const int* plane_x;     // [nxs] grid x index of plane p
     const int* plane_off;   // [nxs+1] entry range of plane p
     const int* ent_ig;      // [npw] caller-order G index; negative = gather only

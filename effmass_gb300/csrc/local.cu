@@ -124,12 +124,31 @@ __global__ void __launch_bounds__(Cfg<C>::g2r_threads, WIDE ? 1 : Cfg<C>::plane_
     __syncthreads();
     const double2* ps = psi + (size_t)b * npw;
     const int e0 = plane_off[p], e1 = plane_off[p + 1];
+    uint32_t mx = 0u;  // float bits of the largest |re|, |im| this thread scattered
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         int ig = ent_ig[e];
         if (ig >= 0) {
             int jk = ent_jk[e];
             int j = jk / n3, k = jk - j * n3;
-            b0[j * n3p + k] = from_c128<C>(ps[ig]);
+            const C v = from_c128<C>(ps[ig]);
+            b0[j * n3p + k] = v;
+            if constexpr (std::is_same<C, float2>::value)
+                mx = max(mx, max(__float_as_uint(v.x) & 0x7fffffffu, __float_as_uint(v.y) & 0x7fffffffu));
+        } else if constexpr (std::is_same<C, float2>::value) {
+            // a G that shares its grid point with a later one: not scattered,
+            // but its coefficient is still a row element of the band operand
+            if (a.rowmax && !a.items) {
+                const float2 v = to_c64(ps[ig & 0x7fffffff]);
+                mx = max(mx, max(__float_as_uint(v.x) & 0x7fffffffu, __float_as_uint(v.y) & 0x7fffffffu));
+            }
+        }
+    }
+    if constexpr (std::is_same<C, float2>::value) {
+        // the band operand's row scale: every G of the band is in exactly one
+        // plane, so the blocks of band b together see all of its coefficients
+        if (a.rowmax && !a.items) {
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if ((threadIdx.x & 31) == 0 && mx) atomicMax(a.rowmax + b, mx);
         }
     }
     __syncthreads();
@@ -556,6 +575,7 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     int h = prof->open(PH_G2R, st);
     g2r<<<gp, ptg, sp, st>>>(a, psi, T, twy, twz);
     prof->close(h, st);
+    if (a.after_g2r && (e = cudaEventRecord(a.after_g2r, st))) return e;
     dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
     xp<<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);

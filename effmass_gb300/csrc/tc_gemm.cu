@@ -586,11 +586,13 @@ __global__ void band_write_kernel(const S* __restrict__ src, int nb, int len, si
 
 template <typename T, typename S, bool FROM_W>
 static void band_rows(const S* src, int nb, int len, size_t ldk, T* hi, T* lo, float* inv_scale, unsigned* rowmax,
-                      bool fp16, cudaStream_t st)
+                      bool fp16, cudaStream_t st, bool have_max = false)
 {
-    cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * nb, st);
-    const int chunks = min(64, ceil_div(len, 256 * 4));
-    band_max_kernel<S, FROM_W><<<dim3(chunks, nb), 256, 0, st>>>(src, nb, len, rowmax);
+    if (!have_max) {
+        cudaMemsetAsync(rowmax, 0, sizeof(unsigned) * nb, st);
+        const int chunks = min(64, ceil_div(len, 256 * 4));
+        band_max_kernel<S, FROM_W><<<dim3(chunks, nb), 256, 0, st>>>(src, nb, len, rowmax);
+    }
     band_write_kernel<T, S, FROM_W><<<dim3(ceil_div((long)(ldk / 4), 256), nb), 256, 0, st>>>(
         src, nb, len, ldk, hi, lo, inv_scale, rowmax, fp16);
 }
@@ -732,15 +734,15 @@ cudaError_t tc_build_grad_operands(const float2* pr4, int P, int npw, bool fp16,
 }
 
 cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, unsigned* rowmax,
-                            cudaStream_t st)
+                            cudaStream_t st, bool have_max)
 {
     const int nbp = tc_band_rows(nb) / 2;
     if (fp16)
         band_rows<__half, double2, false>(psi, nb, npw, B->ldk, (__half*)B->hi, (__half*)B->lo, B->inv_scale, rowmax,
-                                          true, st);
+                                          true, st, have_max);
     else
         band_rows<__nv_bfloat16, double2, false>(psi, nb, npw, B->ldk, (__nv_bfloat16*)B->hi,
-                                                 (__nv_bfloat16*)B->lo, B->inv_scale, rowmax, false, st);
+                                                 (__nv_bfloat16*)B->lo, B->inv_scale, rowmax, false, st, have_max);
     if (nbp > nb) {
         if (fp16)
             zero_rows_kernel<__half><<<nbp - nb, 256, 0, st>>>(nb, nbp, B->ldk, (__half*)B->hi, (__half*)B->lo,

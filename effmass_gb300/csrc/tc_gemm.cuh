@@ -39,9 +39,10 @@ cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, 
 // expansion operand [npw][4P] = (Pr^T | dPr_alpha^T) (buffers must be zeroed).
 cudaError_t tc_build_grad_operands(const float2* pr4, int P, int npw, bool fp16, TcOperand* proj4, TcOperand* exp3,
                                    float* cmax_scratch, cudaStream_t st);
-// Band operand of the projection from psi (complex128 [nb][npw]); rowmax: nb scratch words.
+// Band operand of the projection from psi (complex128 [nb][npw]); rowmax: nb scratch words,
+// or, with have_max, the per-band maxima already taken (float bits of max |re|, |im|).
 cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOperand* B, unsigned* rowmax,
-                            cudaStream_t st);
+                            cudaStream_t st, bool have_max = false);
 // Band operand of the expansion from W (complex64 [P][nb]).
 cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, unsigned* rowmax, cudaStream_t st);
 // W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null); with e_nl also
