@@ -560,27 +560,38 @@ static int tc_splits(const KSlot& s, int nb, bool energy)
     return std::max(ns, tc_chain_splits(k1, kEnergyChainK));
 }
 
-static size_t tc_ws(const KSlot& s, int nb, bool energy = false)
+// Workspace of the tensor-core nonlocal term: split band operand, partials,
+// W and its split operand, per-band maxima, nonlocal energy terms
+struct TcNlOffsets {
+    size_t b1h, b1l, b1s, part, w, b2h, b2l, b2s, rowmax, eterm, bytes;
+    size_t k1, k2;
+    int ns;
+};
+
+static TcNlOffsets tc_offsets(const KSlot& s, int nb, bool energy)
 {
     const int NB = tc_band_rows(nb);
-    const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(2 * (size_t)s.P);
-    const int ns = tc_splits(s, nb, energy);
+    TcNlOffsets o;
+    o.k1 = tc_round_k(2 * (size_t)s.npw);
+    o.k2 = tc_round_k(2 * (size_t)s.P);
+    o.ns = tc_splits(s, nb, energy);
     Carver cv;
-    cv.take<uint16_t>((size_t)NB * k1);
-    cv.take<uint16_t>((size_t)NB * k1);
-    cv.take<float>((size_t)NB);
-    cv.take<float>((size_t)ns * s.P * NB);
-    cv.take<float2>((size_t)s.P * nb);
-    cv.take<uint16_t>((size_t)NB * k2);
-    cv.take<uint16_t>((size_t)NB * k2);
-    cv.take<float>((size_t)NB);
-    cv.take<unsigned>((size_t)nb);
-    if (energy) cv.take<double>((size_t)s.P * nb);
-    return cv.off;
+    o.b1h = cv.take<uint16_t>((size_t)NB * o.k1);
+    o.b1l = cv.take<uint16_t>((size_t)NB * o.k1);
+    o.b1s = cv.take<float>((size_t)NB);
+    o.part = cv.take<float>((size_t)o.ns * s.P * NB);
+    o.w = cv.take<float2>((size_t)s.P * nb);
+    o.b2h = cv.take<uint16_t>((size_t)NB * o.k2);
+    o.b2l = cv.take<uint16_t>((size_t)NB * o.k2);
+    o.b2s = cv.take<float>((size_t)NB);
+    o.rowmax = cv.take<unsigned>((size_t)nb);
+    o.eterm = energy ? cv.take<double>((size_t)s.P * nb) : 0;
+    o.bytes = cv.off;
+    return o;
 }
 
-// Workspace of the tensor-core nonlocal term: split band operand, partials,
-// W and its split operand
+static size_t tc_ws(const KSlot& s, int nb, bool energy = false) { return tc_offsets(s, nb, energy).bytes; }
+
 struct TcNl {
     TcOperand B1, B2;
     float* part;
@@ -592,23 +603,15 @@ struct TcNl {
 
 static TcNl tc_layout(const KSlot& s, int nb, unsigned char* ws, bool energy)
 {
-    const int NB = tc_band_rows(nb);
-    const size_t k1 = s.tc_proj.ldk, k2 = s.tc_expand.ldk;
+    const TcNlOffsets o = tc_offsets(s, nb, energy);
     TcNl t;
-    t.ns = tc_splits(s, nb, energy);
-    Carver cv;
-    const size_t ob1h = cv.take<uint16_t>((size_t)NB * k1), ob1l = cv.take<uint16_t>((size_t)NB * k1);
-    const size_t ob1s = cv.take<float>((size_t)NB);
-    const size_t opart = cv.take<float>((size_t)t.ns * s.P * NB);
-    const size_t ow = cv.take<float2>((size_t)s.P * nb);
-    const size_t ob2h = cv.take<uint16_t>((size_t)NB * k2), ob2l = cv.take<uint16_t>((size_t)NB * k2);
-    const size_t ob2s = cv.take<float>((size_t)NB);
-    t.rowmax = reinterpret_cast<unsigned*>(ws + cv.take<unsigned>((size_t)nb));
-    t.eterm = energy ? reinterpret_cast<double*>(ws + cv.take<double>((size_t)s.P * nb)) : nullptr;
-    t.B1 = TcOperand{ws + ob1h, ws + ob1l, reinterpret_cast<float*>(ws + ob1s), k1};
-    t.B2 = TcOperand{ws + ob2h, ws + ob2l, reinterpret_cast<float*>(ws + ob2s), k2};
-    t.part = reinterpret_cast<float*>(ws + opart);
-    t.W = reinterpret_cast<float2*>(ws + ow);
+    t.ns = o.ns;
+    t.B1 = TcOperand{ws + o.b1h, ws + o.b1l, reinterpret_cast<float*>(ws + o.b1s), o.k1};
+    t.B2 = TcOperand{ws + o.b2h, ws + o.b2l, reinterpret_cast<float*>(ws + o.b2s), o.k2};
+    t.part = reinterpret_cast<float*>(ws + o.part);
+    t.W = reinterpret_cast<float2*>(ws + o.w);
+    t.rowmax = reinterpret_cast<unsigned*>(ws + o.rowmax);
+    t.eterm = energy ? reinterpret_cast<double*>(ws + o.eterm) : nullptr;
     return t;
 }
 
