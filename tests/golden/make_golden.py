@@ -33,9 +33,10 @@ CASES = {
     "tiny": ("tiny", (0.25, 0.25, 0.25), 3, None),
     # non-cubic 15x16x18 grid (radices 3,5 / 2,4 / 2,3), s+p+d, general k
     "tinyd": ("tinyd", (0.1, -0.2, 0.3), 3, None),
-    # 6^3 grid too small for the sphere: several G alias to one grid point
-    # (the reference's scatter keeps the last one, its gather reads it for all)
-    "alias": ("tiny", (0.25, 0.25, 0.25), 2, (6, 6, 6)),
+    # 4^3 grid too small for the sphere: 40 of its 104 G-vectors share a grid
+    # point with another (the reference's scatter keeps the last one, its
+    # gather reads it for all)
+    "alias": ("tiny", (0.25, 0.25, 0.25), 2, (4, 4, 4)),
     # the 2-atom fcc cell at Ecut 15 Ha, 24^3, 8 bands (the plain FP64 configuration)
     "fcc2": ("fcc2", (0.25, 0.25, 0.25), 8, None),
     # 8-atom simple-cubic cell, 36^3, off-Gamma k

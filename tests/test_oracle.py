@@ -37,7 +37,7 @@ def test_oracle_matches_reference_grad(oracle_lib, case):
 @pytest.mark.parametrize("case", CASES)
 def test_oracle_matches_reference_density(oracle_lib, case):
     """rho from the reference's buildDensity (src/support/density.cppm:41-94),
-    occupations with one empty band, aliasing included (the 6^3 case)."""
+    occupations with one empty band, aliasing included (the 4^3 case)."""
     import numpy as np
     sysm, kp, psi, _, _ = load_case(case)
     z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{case}.npz"))
