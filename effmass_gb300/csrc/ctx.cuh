@@ -84,6 +84,7 @@ struct hpsi_ctx {
     double* d_tau = nullptr;
     double* d_v64 = nullptr;
     float* d_v32 = nullptr;
+    float* d_dv32 = nullptr;      // V64 - V32 per grid point (the energy sums' FP64 correction)
     double2* d_tw64 = nullptr;    // twiddles x, y, z consecutive
     float2* d_tw32 = nullptr;
     FftLen L[3];

@@ -36,7 +36,7 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     if (!c) return HPSI_ERR_BAD_ARG;
     cudaSetDevice(c->dev);
     for (auto& kv : c->slots) slot_free(kv.second);
-    dfree(c->d_tables); dfree(c->d_rad_nq); dfree(c->d_rad_dq); dfree(c->d_tau); dfree(c->d_v64); dfree(c->d_v32);
+    dfree(c->d_tables); dfree(c->d_rad_nq); dfree(c->d_rad_dq); dfree(c->d_tau); dfree(c->d_v64); dfree(c->d_v32); dfree(c->d_dv32);
     dfree(c->d_tw64); dfree(c->d_tw32); dfree(c->d_err); dfree(c->d_hess);
     if (c->ws) cudaFree(c->ws);
     if (c->side) cudaStreamDestroy(c->side);
@@ -137,11 +137,16 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
     const size_t N = (size_t)c->n1 * c->n2 * c->n3;
     CUDA_TRY(c, dalloc(&c->d_v64, N));
     CUDA_TRY(c, dalloc(&c->d_v32, N));
+    CUDA_TRY(c, dalloc(&c->d_dv32, N));
     CUDA_TRY(c, cudaMemcpy(c->d_v64, s->v_loc, N * sizeof(double), cudaMemcpyHostToDevice));
     {
-        std::vector<float> v32(N);
-        for (size_t i = 0; i < N; ++i) v32[i] = (float)s->v_loc[i];
+        std::vector<float> v32(N), dv32(N);
+        for (size_t i = 0; i < N; ++i) {
+            v32[i] = (float)s->v_loc[i];
+            dv32[i] = (float)(s->v_loc[i] - (double)v32[i]);
+        }
         CUDA_TRY(c, cudaMemcpy(c->d_v32, v32.data(), N * sizeof(float), cudaMemcpyHostToDevice));
+        CUDA_TRY(c, cudaMemcpy(c->d_dv32, dv32.data(), N * sizeof(float), cudaMemcpyHostToDevice));
     }
     const int ntw = c->n1 + c->n2 + c->n3;
     std::vector<double2> tw64(ntw);
@@ -455,7 +460,7 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
         a.out32 = out32 ? out32 + (size_t)b0 * s.npw : nullptr;
         a.rowmax = rowmax ? rowmax + b0 : nullptr;
         a.after_g2r = b0 == 0 ? after_g2r : nullptr;
-        a.v64e = (epart && sizeof(V) == sizeof(float)) ? c->d_v64 : nullptr;
+        a.dv32 = (epart && sizeof(V) == sizeof(float)) ? c->d_dv32 : nullptr;
         CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
                                         tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
     }

@@ -99,7 +99,8 @@ struct LocalArgs {
     // epart[((e_band0 + band) * nslots + slot) * 2 + {0, 1}]
     double* epart;
     int e_band0;
-    const double* v64e;     // FP64 V(r) for those sums (null: the launch's own V)
+    const float* dv32;      // for those sums: V64(r) - V(r) of the launch's FP32 V,
+                            // the part of the FP64 potential it misses (null: none)
 };
 // (j, k-tile) blocks of the x pass: the energy slots per band
 inline int local_energy_slots(const LocalArgs& a) { return ((a.n3 + a.kt - 1) / a.kt) * a.n2; }

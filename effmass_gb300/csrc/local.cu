@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
         for (int t = threadIdx.x; t < n1 * KT; t += blockDim.x) {
             int x = t / KT, kk = t % KT;
             float d = 0.f;
-            if (a.v64e && kk < kt) d = (float)(a.v64e[((size_t)x * n2 + j) * n3 + k0 + kk] - (double)vt[t]);
+            if (a.dv32 && kk < kt) d = a.dv32[((size_t)x * n2 + j) * n3 + k0 + kk];
             dvt[t] = d;
         }
     }
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
         // psi(r) unscaled; sums of V|psi|^2 and |psi|^2 per line, then psi <- V psi.
         // Each of TPL threads per line accumulates a strided slice of x in the
         // working precision (with the FP64 part of V as dV); the slices are
-        // combined in FP64 in a fixed order.
+        // combined in a fixed order, in FP64 or (complex64) compensated FP32.
         lines<C, WIDE, PL>(ld, SmemLines<C>{vo, 1, NL}, b0, b1, a.Lx, a.nl_x, 1, NL, twx, +1);
         __syncthreads();
         for (int t = threadIdx.x; t < NL * TPL; t += blockDim.x) {
@@ -323,14 +323,28 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
         }
         __syncthreads();
         for (int L = threadIdx.x; L < NL; L += blockDim.x) {
-            double s1 = 0.0, s0 = 0.0;
-            for (int part = 0; part < TPL; ++part) {
-                const int t = part * NL + L;
-                s1 += (double)psum[3 * t] + (double)psum[3 * t + 1];
-                s0 += (double)psum[3 * t + 2];
+            if constexpr (std::is_same<R, float>::value) {
+                // compensated FP32 (two-sum) in part order: GB300's FP64 rate
+                // made the FP64 version of this loop a third of the pass
+                Sum2f s1, s0;
+                for (int part = 0; part < TPL; ++part) {
+                    const int t = part * NL + L;
+                    s1.add(psum[3 * t]);
+                    s1.add(psum[3 * t + 1]);
+                    s0.add(psum[3 * t + 2]);
+                }
+                lsum[2 * L] = f2d_bits(s1.s) + f2d_bits(s1.c);
+                lsum[2 * L + 1] = f2d_bits(s0.s) + f2d_bits(s0.c);
+            } else {
+                double s1 = 0.0, s0 = 0.0;
+                for (int part = 0; part < TPL; ++part) {
+                    const int t = part * NL + L;
+                    s1 += (double)psum[3 * t] + (double)psum[3 * t + 1];
+                    s0 += (double)psum[3 * t + 2];
+                }
+                lsum[2 * L] = s1;
+                lsum[2 * L + 1] = s0;
             }
-            lsum[2 * L] = s1;
-            lsum[2 * L + 1] = s0;
         }
         __syncthreads();
         double* sums = lsum;
