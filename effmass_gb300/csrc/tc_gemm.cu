@@ -774,21 +774,32 @@ cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B
     return cudaGetLastError();
 }
 
+// SMs of the current device (one CTA of the GEMM per SM); 152 on GB300
+static int sm_count()
+{
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || n <= 0)
+        return 152;
+    return n;
+}
+
 // Split-K of the projection: at most MAX_CHAIN_K of K per CTA (short FP32
 // accumulation chains: with the two alternating accumulators at most half of
 // that, 288 MMAs, add into one accumulator), rounded up so that the CTAs fill
-// whole waves of the 148 SMs the kernel plans for.
+// whole waves of the device's SMs.
 int tc_proj_splits(int P, int nb, size_t ldk)
 {
+    const int sms = sm_count();
     const int tiles = ceil_div(P, BM) * (tc_band_rows(nb) / BN);
     const int ktiles = (int)(ldk / BK);
     int s = ceil_div(ktiles, MAX_CHAIN_K / BK);
-    if (tiles * s < 148) s = ceil_div(148, tiles);
+    if (tiles * s < sms) s = ceil_div(sms, tiles);
     // cost model: waves x K per split (in 64-deep units), plus the partial-sum reduction
     int best = s;
     double best_cost = 1e300;
     for (int c = s; c <= 2 * s && c <= ktiles; ++c) {
-        const double cost = (double)ceil_div(tiles * c, 148) * ceil_div(ktiles, c) * (BK / 64.0) + c / 8.0;
+        const double cost = (double)ceil_div(tiles * c, sms) * ceil_div(ktiles, c) * (BK / 64.0) + c / 8.0;
         if (cost < best_cost) { best = c; best_cost = cost; }
     }
     if (best > ktiles) best = ktiles;
@@ -796,7 +807,6 @@ int tc_proj_splits(int P, int nb, size_t ldk)
     return best;
 }
 
-// A: rows M, B: rows N (= tc_band_rows(nb)); one launch
 // A: rows M, B: rows N (= tc_band_rows(nb)); one launch
 static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperand& B, int N, int nsplit, bool fp16,
                              const TcEpilogue& ep, int* err, cudaStream_t st)
