@@ -250,7 +250,7 @@ static int tune_group(hpsi_batch* b, Group& g)
             if (!xshape_ok(b, g, kt, bb)) continue;
             set_xshape(g, kt, bb);
             if ((rc = upload_xblk(b, g))) return rc;
-            double ms;
+            double ms = 0.0;
             if ((rc = time_ms(b, st, reps, [&] { return launch_group_local(b, g, st); }, &ms))) return rc;
             ++t.candidates;
             if (ms < best) { best = ms; bk = kt; bbb = bb; }
@@ -266,7 +266,7 @@ static int tune_group(hpsi_batch* b, Group& g)
     for (int ci = 0; ci < 4 && cand[ci] > 0; ++ci) {
         const int pt = cand[ci];
         g.la.plane_threads = pt;
-        double ms;
+        double ms = 0.0;
         if ((rc = time_ms(b, st, reps, [&] { return launch_group_local(b, g, st); }, &ms))) return rc;
         ++t.candidates;
         if (ms < best) { best = ms; bpt = pt; }
@@ -280,7 +280,7 @@ static int tune_group(hpsi_batch* b, Group& g)
         if ((long)g.gitems.size() * ns > kGridYZ) continue;
         if ((rc = upload_gitems(b, g, ns))) return rc;
         for (int tile = 0; tile < bgemm_tile_count(); ++tile) {
-            double ms;
+            double ms = 0.0;
             if ((rc = time_ms(b, st, reps, [&] { return launch_group_proj(b, g, tile, ns, st); }, &ms))) return rc;
             ++t.candidates;
             if (ms < best) { best = ms; t.proj_tile = tile; t.nsplit = ns; }
@@ -292,7 +292,7 @@ static int tune_group(hpsi_batch* b, Group& g)
     BCUDA(b, launch_group_proj(b, g, t.proj_tile, t.nsplit, st));
     best = 1e30;
     for (int tile = 0; tile < bgemm_tile_count(); ++tile) {
-        double ms;
+        double ms = 0.0;
         if ((rc = time_ms(b, st, reps, [&] { return launch_group_exp(b, g, tile, t.nsplit, st); }, &ms))) return rc;
         ++t.candidates;
         if (ms < best) { best = ms; t.exp_tile = tile; }

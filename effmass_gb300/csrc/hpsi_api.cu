@@ -362,11 +362,19 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
     return HPSI_OK;
 }
 
+// The slot's projector matrix and projector second derivatives in complex type C
+template <typename C> static C*& slot_pr(KSlot& s);
+template <> double2*& slot_pr<double2>(KSlot& s) { return s.pr64; }
+template <> float2*& slot_pr<float2>(KSlot& s) { return s.pr32; }
+template <typename C> static C*& slot_hess(KSlot& s);
+template <> double2*& slot_hess<double2>(KSlot& s) { return s.hess64; }
+template <> float2*& slot_hess<float2>(KSlot& s) { return s.hess32; }
+
 // Build (once) the projector matrices of slot s in complex type C.
 template <typename C>
 static int ensure_proj(hpsi_ctx* c, KSlot& s, bool grad, cudaStream_t st)
 {
-    C*& pr = std::is_same<C, double2>::value ? reinterpret_cast<C*&>(s.pr64) : reinterpret_cast<C*&>(s.pr32);
+    C*& pr = slot_pr<C>(s);
     bool& has_grad = std::is_same<C, double2>::value ? s.pr64_grad : s.pr32_grad;
     if (s.P == 0 || s.npw == 0) return HPSI_OK;
     if (pr && (has_grad || !grad)) return HPSI_OK;
@@ -1541,7 +1549,7 @@ extern "C" int hpsi_set_hessian_tables(hpsi_ctx* c, int species, int nq, double 
 template <typename C>
 static int ensure_hess(hpsi_ctx* c, KSlot& s, cudaStream_t st)
 {
-    C*& d2 = std::is_same<C, double2>::value ? reinterpret_cast<C*&>(s.hess64) : reinterpret_cast<C*&>(s.hess32);
+    C*& d2 = slot_hess<C>(s);
     if (d2 || s.P == 0 || s.npw == 0) return HPSI_OK;
     for (int r = 0; r < c->nrad; ++r)
         if (std::fabs(c->rad_lam[r]) >= 1e-15 && (c->hess_set.empty() || !c->hess_set[r]))
