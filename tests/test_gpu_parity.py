@@ -224,6 +224,28 @@ def test_full_size_grad_mixed_vs_fp64(sc64):
         assert rel_err(g, g64) <= TOL[prec], (prec, rel_err(g, g64))
 
 
+def test_full_size_band_chunks(sc64):
+    """320 bands of the 64-atom cell: their sphere planes (519 MB) exceed the
+    512 MB band chunk, so the local term runs in two chunks and the tensor-core
+    band operand takes its row maxima in a separate pass.  The first and last
+    bands agree with separate FP64 calls."""
+    import torch
+    from effmass_gb300 import system as S
+    H, kp, _ = sc64
+    nb = 320
+    psi = S.make_bands(kp, nb, seed=5)
+    p = torch.from_numpy(psi).cuda()
+    for prec in ("tc", "fp32"):
+        h = torch.zeros_like(p)
+        H.apply(0, nb, p, h, prec)
+        torch.cuda.synchronize()
+        out = h.cpu().numpy()
+        for lo in (0, nb - 8):
+            ref = np.zeros((8, kp.npw), dtype=np.complex128)
+            H.apply(0, 8, np.ascontiguousarray(psi[lo:lo + 8]), ref, "fp64")
+            assert rel_err(out[lo:lo + 8], ref) <= TOL[prec], (prec, lo, rel_err(out[lo:lo + 8], ref))
+
+
 def test_full_size_linearity(sc64):
     H, kp, psi = sc64
     a, b = 0.3 - 1.1j, -0.7 + 0.2j
