@@ -61,6 +61,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest x over the replicas (all-reduce MAX in the process group's
+    backend: a CUDA tensor for NCCL, a host tensor otherwise).  With one
+    process, x itself."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_rate(units_per_rank: int, ms_per_rank: float, world: int) -> float:
+    """Whole-job units/s of `world` replicas: all units over the slowest rank's time."""
+    return world * units_per_rank / (max_over_ranks(ms_per_rank, world) * 1e-3)
+
+
 def workload(name, nb):
     from effmass_gb300 import system as S
     sysm = S.make_system(name)
@@ -207,12 +226,8 @@ def run_gb300(args, rank, world, local):
     clocks.mark(False)
     clk = clocks.stop()
     barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * nb / (ms * 1e-3)
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    value = replicas_rate(nb, ms, world)
 
     # per-phase CUDA-event profile over the same number of steps, with the
     # tensor-core projection chain on the launching stream (HPSI_ONE_STREAM):
@@ -296,7 +311,7 @@ def run_gb300(args, rank, world, local):
         H.grad_apply(0, nb, psi_d, gout, args.prec)
     q1.record(stream)
     torch.cuda.synchronize()
-    grad_value = world * nb / (q0.elapsed_time(q1) / args.steps * 1e-3)
+    grad_value = replicas_rate(nb, q0.elapsed_time(q1) / args.steps, world)
     del gx, gy, gz, gout
 
     # end to end through the public API with pinned host buffers
@@ -313,12 +328,7 @@ def run_gb300(args, rank, world, local):
         H.apply(0, nb, psi_np, hpsi_np, args.prec)
     g1.record(dstream)
     torch.cuda.synchronize()
-    e2e_ms = g0.elapsed_time(g1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": world * nb / (e2e_ms * 1e-3), "unit": "band-apps/s",
+    e2e = {"value": replicas_rate(nb, g0.elapsed_time(g1) / args.steps, world), "unit": "band-apps/s",
            "h2d_bytes_per_step": 2 * psi.nbytes, "d2h_bytes_per_step": psi.nbytes}
 
     # roofline of the dominant phase
