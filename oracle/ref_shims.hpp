@@ -7,7 +7,7 @@
 //    project's own mixed-radix FFT (oracle/mrfft.h) because the reference's
 //    vendor/pocketfft submodule is empty;
 //  * an empty pugi::xml_node so the UPF class declaration compiles (the
-//    pugixml parser itself is removed by oracle/refgen.py; the driver fills
+//    pugixml parser itself is removed by oracle/refgen.py; oracle/ref_driver.cpp fills
 //    UPF objects from an in-memory registry instead).
 #pragma once
 

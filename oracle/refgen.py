@@ -119,7 +119,7 @@ def transform(path, text):
         cut = text.find("\nnamespace {")
         if cut < 0:
             raise SystemExit("refgen: could not find UPF parser body")
-        text = text[:cut] + "\n// [refgen] pugixml-based UPF parser body removed; UPF::UPF is defined by the driver\n"
+        text = text[:cut] + "\n// [refgen] pugixml-based UPF parser body removed; UPF::UPF is defined by oracle/ref_driver.cpp\n"
     if path.endswith("pseudo/ncpp_advance.cppm"):
         text = text.replace("\nprivate:\n", "\npublic:  // [refgen] opened for table export\n")
     return text
