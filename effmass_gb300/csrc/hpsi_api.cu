@@ -71,7 +71,7 @@ extern "C" int hpsi_profile_read(hpsi_ctx* c, double* ms, long long* launches)
         float t = 0.f;
         CUDA_TRY(c, cudaEventElapsedTime(&t, r.a, r.b));
         ms[r.phase] += t;
-        launches[r.phase] += 1;
+        launches[r.phase] += r.kernels;
     }
     return HPSI_OK;
 }
@@ -634,14 +634,17 @@ static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi
 {
     const bool fp16 = s.tc_fmt == 0;
     TcNl t = tc_layout(s, nb, ws, e_nl != nullptr);
+    // kernels of the operand builders: band maxima (unless taken), split rows,
+    // and zero rows when the last 128-band block is partial
+    const int zero_rows = tc_band_rows(nb) / 2 > nb ? 1 : 0;
     int h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &t.B1, t.rowmax, st, have_max));
-    c->prof.close(h, st);
+    c->prof.close(h, st, (have_max ? 1 : 2) + zero_rows);
     CUDA_TRY(c, tc_projection(s.tc_proj, s.P, t.B1, nb, t.ns, fp16, t.part, s.d_lam, s.P, t.W, c->d_err, st,
                               &c->prof, t.eterm, e_nl));
     h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_w_operand(t.W, s.P, nb, fp16, &t.B2, t.rowmax, st));
-    c->prof.close(h, st);
+    c->prof.close(h, st, 2 + zero_rows);
     return HPSI_OK;
 }
 

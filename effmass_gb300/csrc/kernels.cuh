@@ -25,7 +25,7 @@ enum HpsiPhase {
 // Event pairs around launches; read back and summed by hpsi_profile_read.
 struct Prof {
     bool on = false;
-    struct Rec { int phase; cudaEvent_t a, b; };
+    struct Rec { int phase; cudaEvent_t a, b; int kernels; };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
     cudaEvent_t take()
@@ -38,14 +38,17 @@ struct Prof {
     int open(int phase, cudaStream_t st)
     {
         if (!on) return -1;
-        Rec r{phase, take(), take()};
+        Rec r{phase, take(), take(), 1};
         cudaEventRecord(r.a, st);
         recs.push_back(r);
         return (int)recs.size() - 1;
     }
-    void close(int h, cudaStream_t st)
+    // kernels: the kernel launches the range holds (its count in hpsi_profile_read)
+    void close(int h, cudaStream_t st, int kernels = 1)
     {
-        if (h >= 0) cudaEventRecord(recs[h].b, st);
+        if (h < 0) return;
+        recs[h].kernels = kernels;
+        cudaEventRecord(recs[h].b, st);
     }
 };
 

@@ -853,7 +853,7 @@ cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb,
     proj_reduce_kernel<float2><<<ceil_div((long)P * nb, 256), 256, 0, st>>>(P, nb, N, nz, part, lam, period, W,
                                                                             e_nl ? eterm : nullptr);
     if (e_nl) eterm_sum_kernel<<<nb, 256, 0, st>>>(P, nb, eterm, e_nl);
-    prof->close(h, st);
+    prof->close(h, st, e_nl ? 2 : 1);
     return cudaGetLastError();
 }
 
