@@ -28,6 +28,21 @@ def _reference(sysm, kp, psi):
         return S.read_golden(gold)
 
 
+def _reference_density(sysm, kp, psi, occ):
+    """The reference's buildDensity of the bands with occupations occ."""
+    with tempfile.TemporaryDirectory() as td:
+        spec, occ_txt, rho_bin = (os.path.join(td, f) for f in ("spec.bin", "occ.txt", "rho.bin"))
+        S.write_spec(spec, sysm, [kp], [psi])
+        np.savetxt(occ_txt, occ, fmt="%.17g")
+        subprocess.run([O.REF_DRIVER, "density", spec, occ_txt, rho_bin, os.path.join(td, "wd")], check=True,
+                       stderr=subprocess.DEVNULL, timeout=600)
+        raw = open(rho_bin, "rb").read()
+    assert raw[:8] == b"RHOREF01"
+    dims = tuple(np.frombuffer(raw[8:20], dtype=np.int32))
+    assert dims == (sysm.n1, sysm.n2, sysm.n3)
+    return np.frombuffer(raw[20:], dtype=np.float64).copy()
+
+
 def _as_used(sysm, g):
     """System and k-point as the reference used them: its own beta/dbeta tables
     and lambda (after its per-l diagonalisation), its G-sphere views."""
@@ -62,3 +77,7 @@ def test_oracle_matches_live_reference(name, k_frac, grid, seed):
     assert rel_err(h, gk["hpsi"]) <= 1e-14
     grad = O.grad(used, kp_used, psi)
     assert rel_err(grad, np.transpose(gk["grad"], (1, 0, 2))) <= 1e-14
+    # charge density with one empty band (the reference skips it)
+    occ = np.array([2.0, 0.0, 0.7])
+    rho = O.density(used, kp_used, psi, occ)
+    assert rel_err(rho.ravel(), _reference_density(sysm, kp, psi, occ)) <= 1e-14
