@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import json
 import os
+import platform
+import statistics
 import subprocess
 import tempfile
 import time
@@ -20,8 +22,28 @@ from effmass_gb300 import system as S
 from oracle import oracle as O
 
 
+def cpu_model() -> str:
+    """The host CPU's name from /proc/cpuinfo (model name, else the Arm part
+    number), with the machine type."""
+    name = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            key, _, val = line.partition(":")
+            key = key.strip().lower()
+            if key == "model name" and val.strip():
+                name = val.strip()
+                break
+            if key == "cpu part" and not name:
+                name = "CPU part " + val.strip()
+    except OSError:
+        pass
+    return f"{name or 'unknown'} ({platform.machine()}, {os.cpu_count()} logical CPUs)"
+
+
 def run(sysm, kp, psi, bands_per_worker: int = 2, workers: int = 0):
-    """Returns dict(value=band-apps/s, cores, kind, sample, seconds)."""
+    """Returns dict(value=band-apps/s of all workers, per_core_value=band-apps/s
+    of one single-threaded worker while all run, cores, kind, sample, seconds,
+    cpu)."""
     workers = workers or os.cpu_count() or 1
     nb = psi.shape[0]
     if O.build_ref():
@@ -41,7 +63,8 @@ def run(sysm, kp, psi, bands_per_worker: int = 2, workers: int = 0):
                     raise RuntimeError("reference driver failed")
                 secs.append(json.loads(out.strip().splitlines()[-1])["seconds"])
         t = max(secs)
-        return dict(value=workers * bands_per_worker / t, cores=workers, kind="reference", seconds=t,
+        return dict(value=workers * bands_per_worker / t, per_core_value=bands_per_worker / statistics.median(secs),
+                    cores=workers, kind="reference", seconds=t, cpu=cpu_model(),
                     sample=f"{workers} single-threaded reference processes x {bands_per_worker} bands "
                            f"(npw={kp.npw}), H|psi> time only")
     # fallback: the oracle port, threads over bands
@@ -50,5 +73,5 @@ def run(sysm, kp, psi, bands_per_worker: int = 2, workers: int = 0):
     t0 = time.perf_counter()
     O.hpsi(sysm, kp, psi[:nbs], threads=workers)
     t = time.perf_counter() - t0
-    return dict(value=nbs / t, cores=workers, kind="port", seconds=t,
-                sample=f"oracle port on {workers} threads x {nbs} bands (npw={kp.npw})")
+    return dict(value=nbs / t, per_core_value=nbs / t / workers, cores=workers, kind="port", seconds=t,
+                cpu=cpu_model(), sample=f"oracle port on {workers} threads x {nbs} bands (npw={kp.npw})")
