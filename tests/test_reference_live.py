@@ -81,3 +81,27 @@ def test_oracle_matches_live_reference(name, k_frac, grid, seed):
     occ = np.array([2.0, 0.0, 0.7])
     rho = O.density(used, kp_used, psi, occ)
     assert rel_err(rho.ravel(), _reference_density(sysm, kp, psi, occ)) <= 1e-14
+
+
+@pytest.mark.parametrize("name,dr,r_max", [("tinyd", 0.02, 10.0), ("sc8", 0.005, 14.0)])
+def test_oracle_beta_tables_match_live_reference(name, dr, r_max):
+    """beta(q) and dbeta/dq tables: the reference integrates radial projectors
+    written on a mesh the fixtures do not use; the oracle, given the radial
+    inputs the reference reports, builds the same tables bit for bit."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import read_tables
+    sysm = S.make_system(name)
+    kp = S.g_sphere(sysm.lattice, (0.1, 0.2, 0.3), sysm.ecut)
+    psi = S.make_bands(kp, 1, seed=7)
+    with tempfile.TemporaryDirectory() as td:
+        spec, tab = os.path.join(td, "spec.bin"), os.path.join(td, "tab.bin")
+        S.write_spec(spec, sysm, [kp], [psi], dr=dr, r_max=r_max)
+        subprocess.run([O.REF_DRIVER, "tables", spec, tab, os.path.join(td, "wd")], check=True,
+                       stderr=subprocess.DEVNULL, timeout=600)
+        rad = read_tables(tab)
+    # the reference's finalize builds its tables at its defaults dq = 0.01,
+    # q_max = 20 (src/H_psi/hamiltonian.cpp:307-309): 2004 points
+    bq, dbq = O.beta_tables(rad["r"], rad["rab"], bool(rad["uniform"]), rad["l"], rad["beta"], 0.01, 20.0)
+    assert bq.shape == rad["beta_q"].shape
+    assert np.array_equal(bq, rad["beta_q"]) and np.array_equal(dbq, rad["dbeta_q"])
