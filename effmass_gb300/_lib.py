@@ -20,7 +20,9 @@ EXPORTS = ["hpsi_abi_version", "hpsi_ctx_create", "hpsi_ctx_destroy", "hpsi_set_
            "hpsi_apply_noalloc", "hpsi_server_create", "hpsi_server_submit", "hpsi_server_wait",
            "hpsi_server_stats", "hpsi_server_destroy", "hpsi_server_last_error", "hpsi_batch_create",
            "hpsi_batch_buffers", "hpsi_batch_offset", "hpsi_batch_run", "hpsi_batch_apply", "hpsi_batch_info",
-           "hpsi_batch_destroy", "hpsi_batch_last_error", "hpsi_selftest_convert", "hpsi_last_error"]
+           "hpsi_batch_destroy", "hpsi_batch_last_error", "hpsi_selftest_convert", "hpsi_selftest_wait_limit",
+           "hpsi_selftest_fft3d", "hpsi_selftest_kpoint_tables",
+           "hpsi_last_error"]
 
 _lib = None
 
@@ -71,6 +73,9 @@ def load():
     L.hpsi_profile.argtypes = [ctxp, C.c_int]
     L.hpsi_profile_read.argtypes = [ctxp, dp, C.POINTER(C.c_longlong)]
     L.hpsi_selftest_convert.argtypes = [dp, C.c_long] + [C.c_void_p] * 4
+    L.hpsi_selftest_wait_limit.argtypes = [C.c_long]
+    L.hpsi_selftest_fft3d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int]
+    L.hpsi_selftest_kpoint_tables.argtypes = [ctxp, C.c_int, C.c_void_p, C.c_void_p]
     L.hpsi_last_error.argtypes = [ctxp]
     L.hpsi_last_error.restype = C.c_char_p
     for name in EXPORTS:

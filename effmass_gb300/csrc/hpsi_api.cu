@@ -939,9 +939,11 @@ static EnergyWs energy_layout(const hpsi_ctx* c, int nb, int prec)
 {
     LocalArgs a{};
     a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
-    local_xpass_shape(&a, prec == HPSI_PREC_FP64 ? sizeof(double2) : sizeof(float2));
+    a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
+    const size_t csize = prec == HPSI_PREC_FP64 ? sizeof(double2) : sizeof(float2);
+    local_xpass_shape(&a, csize);
     EnergyWs w;
-    w.nslots = local_energy_slots(a);
+    w.nslots = local_energy_slots(a, csize);
     Carver cv;
     w.kn = cv.take<double>((size_t)kin_norm_words(nb));
     w.loc = cv.take<double>(2 * (size_t)nb);
@@ -1822,6 +1824,26 @@ extern "C" int hpsi_velocity_matrix(hpsi_ctx* c, int kid, int nb, const double* 
     return HPSI_OK;
 }
 
+// Self-test: the device tables of a bound k-point as the projector build
+// reads them — Y_lm, dY_lm/dtheta and (1/sin theta) dY_lm/dphi for
+// l <= l_max ([3][(l_max+1)^2][npw], the last two only with dbeta tables) and
+// the structure factors S_a(G) ([n_atoms][npw] complex) — copied to host
+// buffers (either may be NULL), for known-answer tests of the kernels that
+// build them.
+extern "C" int hpsi_selftest_kpoint_tables(hpsi_ctx* c, int kid, double* ylm, double* sf)
+{
+    KSlot* s = nullptr;
+    int rc = check_call(c, kid, 0, &s, 0);
+    if (rc) return rc;
+    if (s->npw == 0) return HPSI_OK;
+    const size_t nlm = (size_t)(c->lmax + 1) * (c->lmax + 1);
+    if (ylm) CUDA_TRY(c, cudaMemcpy(ylm, s->d_ylm, (c->have_dbeta ? 3 : 1) * nlm * s->npw * sizeof(double),
+                                    cudaMemcpyDeviceToHost));
+    if (sf && c->natom > 0)
+        CUDA_TRY(c, cudaMemcpy(sf, s->d_sf, (size_t)c->natom * s->npw * sizeof(double2), cudaMemcpyDeviceToHost));
+    return HPSI_OK;
+}
+
 // ---------------------------------------------------------------------------
 // hpsi_apply_noalloc — H|psi> for callers that cannot allocate device memory.
 //
@@ -1830,22 +1852,27 @@ extern "C" int hpsi_velocity_matrix(hpsi_ctx* c, int kid, int nb, const double* 
 // at start-up, a host runtime whose own allocator owns all device memory and
 // forbids other allocations, or code that must not add the implicit device
 // synchronisation an allocation can cause between its kernels.  For them this
-// entry point computes exactly what hpsi_apply computes, but all per-call
-// scratch (the FFT planes of the local term, the split-K partial sums and the
-// projected coefficients of the nonlocal term) lives in one file-scope device
-// array of HPSI_NOALLOC_SCRATCH_BYTES (32 MiB).  Every GPU that loads this
-// library holds that array until the process exits.
+// entry point computes what hpsi_apply computes at FP64 or FP32, but all
+// per-call scratch (the FFT planes of the local term, the split-K partial sums
+// and the projected coefficients of the nonlocal term) lives in one
+// file-scope device array of HPSI_NOALLOC_SCRATCH_BYTES (32 MiB).  Every GPU
+// that loads this library holds that array until the process exits.
 //
 // Rules:
 //  * psi and hpsi are device pointers (HPSI_DEVICE_PTRS is required);
+//  * precision HPSI_PREC_FP64 or HPSI_PREC_FP32; the tensor-core precisions
+//    need operand buffers per call and are refused with HPSI_ERR_BAD_ARG;
 //  * the projector matrices of the requested precision must already exist:
 //    the first hpsi_apply / hpsi_grad_apply at that precision on the k-point
 //    builds them (that call allocates); otherwise HPSI_ERR_STATE;
-//  * sizes beyond the scratch (one band's FFT planes, or one band's
-//    projection partials) are rejected with HPSI_ERR_BAD_ARG;
+//  * the whole chunk plan (bands per local-term chunk, bands per nonlocal
+//    chunk and its last, shorter chunk) is checked against the scratch before
+//    the first launch: a call that does not fit is refused with
+//    HPSI_ERR_BAD_ARG and leaves hpsi untouched;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (which may load the module); make that first call
-//    before any stream capture;
+//    cudaGetSymbolAddress (which may load the module) and keeps it for the
+//    process; make that first call before any stream capture.  The kept
+//    address is not valid after cudaDeviceReset;
 //  * every call shares the one array and leaves its contents behind (each
 //    call writes all scratch it reads, so nothing needs clearing); calls that
 //    overlap on the GPU — on two streams, or from two threads — race.
@@ -1872,18 +1899,56 @@ static int noalloc_scratch(hpsi_ctx* c, unsigned char** out)
     return HPSI_OK;
 }
 
+// Scratch bytes of one nonlocal chunk of nbc bands (split-K partials, then the
+// projected coefficients), and its split count.
+template <typename C, typename Acc>
+static size_t noalloc_nl_bytes(const KSlot& s, int nbc, int* ns)
+{
+    *ns = split_for(s.P, nbc, s.npw);
+    Carver cv;
+    cv.take<Acc>((size_t)*ns * s.P * nbc);
+    cv.take<C>((size_t)s.P * nbc);
+    return cv.off;
+}
+
+// Bands per nonlocal chunk such that every chunk, the last (shorter) one
+// included, fits the scratch: the split count, and with it the bytes, is not
+// monotone in the band count, so both chunk sizes are checked.  0: none fits.
+template <typename C, typename Acc>
+static int noalloc_nl_chunk(const KSlot& s, int nb, size_t cap)
+{
+    int ns = 0;
+    for (int nbc = nb; nbc >= 1; nbc = (nbc == 1) ? 0 : (nbc + 1) / 2) {
+        if (noalloc_nl_bytes<C, Acc>(s, nbc, &ns) > cap) continue;
+        const int rem = nb % nbc;
+        if (rem && noalloc_nl_bytes<C, Acc>(s, rem, &ns) > cap) continue;
+        return nbc;
+    }
+    return 0;
+}
+
 template <typename C, typename Acc, typename V>
 static int apply_noalloc_impl(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, const C* pr,
                               const V* vloc, const C* tw, unsigned char* scratch, cudaStream_t st)
 {
     const size_t cap = HPSI_NOALLOC_SCRATCH_BYTES;
     Prof off;  // never records: creating events is not allowed here
-    // local term: bands in chunks whose FFT planes fit the scratch
+    // the whole plan first: no launch before every chunk is known to fit
     const size_t plane_bytes = (size_t)s.nxs * c->n2 * c->n3 * sizeof(C);
     if (plane_bytes > cap)
         return fail(c, HPSI_ERR_BAD_ARG,
                     "hpsi_apply_noalloc: one band's FFT planes need %zu bytes, above the %zu-byte scratch", plane_bytes,
                     cap);
+    int nbc = 0;
+    if (s.P > 0) {
+        nbc = noalloc_nl_chunk<C, Acc>(s, nb, cap);
+        int ns = 0;
+        if (nbc == 0)
+            return fail(c, HPSI_ERR_BAD_ARG,
+                        "hpsi_apply_noalloc: %d projectors need %zu bytes of partial sums per band, above the %zu-byte "
+                        "scratch", s.P, noalloc_nl_bytes<C, Acc>(s, 1, &ns), cap);
+    }
+    // local term: bands in chunks whose FFT planes fit the scratch
     if (plane_bytes > 0) {
         LocalArgs a{};
         a.n1 = c->n1; a.n2 = c->n2; a.n3 = c->n3;
@@ -1899,31 +1964,18 @@ static int apply_noalloc_impl(hpsi_ctx* c, KSlot& s, int nb, const double2* psi,
         a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
         const int ch = (int)std::min<size_t>((size_t)nb, cap / plane_bytes);
         for (int b0 = 0; b0 < nb; b0 += ch) {
-            const int nbc = std::min(ch, nb - b0);
-            CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin,
+            const int n = std::min(ch, nb - b0);
+            CUDA_TRY(c, (launch_local<C, V>(a, n, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin,
                                             reinterpret_cast<C*>(scratch), vloc, tw, tw + c->n1, tw + c->n1 + c->n2,
                                             st, &off)));
         }
     }
-    // nonlocal term: bands in chunks whose partials and coefficients fit
+    // nonlocal term: bands in chunks of nbc (checked above)
     if (s.P == 0) return HPSI_OK;
-    auto need = [&](int nbc, int* ns) {
-        *ns = split_for(s.P, nbc, s.npw);
-        Carver cv;
-        cv.take<Acc>((size_t)*ns * s.P * nbc);
-        cv.take<C>((size_t)s.P * nbc);
-        return cv.off;
-    };
-    int nbc = nb, ns = 1;
-    while (nbc > 1 && need(nbc, &ns) > cap) nbc = (nbc + 1) / 2;
-    if (need(nbc, &ns) > cap)
-        return fail(c, HPSI_ERR_BAD_ARG,
-                    "hpsi_apply_noalloc: %d projectors need %zu bytes of partial sums per band, above the %zu-byte "
-                    "scratch", s.P, need(1, &ns), cap);
     for (int b0 = 0; b0 < nb; b0 += nbc) {
         const int n = std::min(nbc, nb - b0);
-        if (need(n, &ns) > cap)
-            return fail(c, HPSI_ERR_BAD_ARG, "hpsi_apply_noalloc: %d bands of partial sums exceed the scratch", n);
+        int ns = 0;
+        noalloc_nl_bytes<C, Acc>(s, n, &ns);
         Carver cv;
         const size_t o_part = cv.take<Acc>((size_t)ns * s.P * n);
         const size_t o_w = cv.take<C>((size_t)s.P * n);
@@ -1944,11 +1996,16 @@ extern "C" int hpsi_apply_noalloc(hpsi_ctx* c, int kid, int nb, const double* ps
     KSlot* s = nullptr;
     int rc = check_call(c, kid, nb, &s, flags);
     if (rc) return rc;
+    const int prec = flags & HPSI_PREC_MASK;
+    if (prec != HPSI_PREC_FP64 && prec != HPSI_PREC_FP32)
+        return fail(c, HPSI_ERR_BAD_ARG,
+                    "hpsi_apply_noalloc: precision %d is not offered; HPSI_PREC_FP64 or HPSI_PREC_FP32 only (the "
+                    "tensor-core path needs per-call operand buffers)", prec);
     if (!(flags & HPSI_DEVICE_PTRS))
         return fail(c, HPSI_ERR_BAD_ARG, "hpsi_apply_noalloc: psi/hpsi must be device pointers (HPSI_DEVICE_PTRS)");
     if (nb > 0 && (!psi_ || !hpsi_)) return fail(c, HPSI_ERR_BAD_ARG, "psi/hpsi NULL");
     if (nb == 0 || s->npw == 0) return HPSI_OK;
-    const bool fp64 = (flags & HPSI_PREC_MASK) == HPSI_PREC_FP64;
+    const bool fp64 = prec == HPSI_PREC_FP64;
     if (s->P > 0 && !(fp64 ? (void*)s->pr64 : (void*)s->pr32))
         return fail(c, HPSI_ERR_STATE,
                     "hpsi_apply_noalloc: projector matrices of this precision are not built yet; one hpsi_apply or "

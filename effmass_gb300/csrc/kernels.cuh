@@ -105,8 +105,9 @@ struct LocalArgs {
     const float* dv32;      // for those sums: V64(r) - V(r) of the launch's FP32 V,
                             // the part of the FP64 potential it misses (null: none)
 };
-// (j, k-tile) blocks of the x pass: the energy slots per band
-inline int local_energy_slots(const LocalArgs& a) { return ((a.n3 + a.kt - 1) / a.kt) * a.n2; }
+// energy slots per band of the x pass that runs for complex size csize (a.kt
+// set by local_xpass_shape, a.Lx/Ly/Lz by the caller): one per x-pass block
+int local_energy_slots(const LocalArgs& a, size_t csize);
 
 size_t local_smem_bytes(const LocalArgs& a, bool fp64);
 // choose kt/bb of the x pass for complex size csize (bytes)

@@ -21,6 +21,7 @@
 #include <type_traits>
 
 #include "fft.cuh"
+#include "fft_reg.cuh"
 #include "kernels.cuh"
 
 // Launch shape per precision: complex64 kernels run two 768-thread plane
@@ -367,6 +368,118 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
     lines<C, WIDE, PL>(SmemLines<C>{vo, 1, NL}, stT, vother, vo, a.Lx, a.nl_x, 1, NL, twx, -1);
 }
 
+// Register x pass (complex64, compile-time plans N = N1*N2 on all axes): one
+// thread per x-line (band, j, k).  The thread loads the line's sphere planes
+// from T (consecutive threads take consecutive (j, k), so every load and
+// store of a warp is one coalesced 256-byte access), transforms it G->r in
+// registers, multiplies by V (read at the transform's split positions, no
+// reordering), transforms it r->G and stores the sphere planes back.  No
+// shared memory but the block's plane mask, no barrier inside the line work.
+// Blocks never straddle bands (grid.y = band), so the plane set is uniform.
+// Resident blocks per SM by line length: two for N >= 64 (72: up to 255
+// registers; a 168-register bound, three blocks, spilled and measured slower,
+// 0.142 vs 0.129 ms on the 64-atom cell), three for 36, four for 24.
+//
+// ENERGY: after the G->r transform each thread also sums, in compensated FP32
+// over its line's N points, V|psi(r)|^2 (+ dV |psi(r)|^2, the FP64 part of V
+// the FP32 table misses) and |psi(r)|^2; the block adds its lines' sums in
+// FP64 in a fixed order and writes one slot per (band, block):
+// epart[((e_band0 + band) * gridDim.x + blockIdx.x) * 2 + {0, 1}].
+constexpr int XREG_THREADS = 128;
+constexpr int xreg_minb(int n) { return n >= 64 ? 2 : (n >= 36 ? 3 : 4); }
+
+template <typename PL, bool ENERGY>
+__global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n)) x_pass_reg(LocalArgs a, float2* __restrict__ T,
+                                                              const float* __restrict__ vloc)
+{
+    constexpr int N1 = PL::r0, N2 = PL::r1, N = PL::n, N23 = N * N, W = (N + 31) / 32;
+    __shared__ uint32_t msk[W];
+    __shared__ double red[2][XREG_THREADS / 32];
+    int b = blockIdx.y;
+    int nxs = a.nxs;
+    const int* plane_x = a.plane_x;
+    if (a.items) {  // batched: the band's item (uniform per block)
+        const LocalItem I = a.items[a.band_item[b]];
+        b -= I.band0;
+        nxs = I.nxs;
+        plane_x = I.plane_x;
+        T += I.t_off;
+    }
+    if (threadIdx.x < W) msk[threadIdx.x] = 0u;
+    __syncthreads();
+    for (int t = threadIdx.x; t < nxs; t += blockDim.x) atomicOr(&msk[plane_x[t] >> 5], 1u << (plane_x[t] & 31));
+    __syncthreads();
+    const int jk = blockIdx.x * XREG_THREADS + threadIdx.x;
+    const bool valid = jk < N23;
+    if (!ENERGY && !valid) return;
+    uint32_t m[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) m[w] = valid ? msk[w] : 0u;  // an idle energy thread loads and stores nothing
+    float2* line = T + (size_t)b * nxs * N23 + jk;
+    float2 v[N];
+    {
+        const float2* p = line;
+#pragma unroll
+        for (int x = 0; x < N; ++x) {
+            const bool on = (m[x >> 5] >> (x & 31)) & 1u;
+            v[x] = on ? __ldcs(p) : make_float2(0.f, 0.f);
+            if (on) p += N23;
+        }
+    }
+    fftreg::fft_nat_to_split<+1, N1, N2>(v);
+    Sum2f s1, s0;
+    {
+        const float* vp = vloc + jk;
+#pragma unroll
+        for (int x = 0; x < N; ++x) {
+            const float w = valid ? __ldg(vp + (size_t)x * N23) : 0.f;
+            float2& e = v[fftreg::split_pos<N1, N2>(x)];
+            if constexpr (ENERGY) {
+                const float mm = e.x * e.x + e.y * e.y;
+                const float dv = (valid && a.dv32) ? __ldg(a.dv32 + jk + (size_t)x * N23) : 0.f;
+                s1.add(w * mm);
+                s1.add(dv * mm);
+                s0.add(mm);
+            }
+            e = make_float2(e.x * w, e.y * w);
+        }
+    }
+    if constexpr (ENERGY) {
+        double t1 = f2d_bits(s1.s) + f2d_bits(s1.c), t0 = f2d_bits(s0.s) + f2d_bits(s0.c);
+        for (int o = 16; o > 0; o >>= 1) {
+            t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+            t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red[0][threadIdx.x >> 5] = t1;
+            red[1][threadIdx.x >> 5] = t0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double u1 = 0.0, u0 = 0.0;
+            for (int w = 0; w < XREG_THREADS / 32; ++w) {
+                u1 += red[0][w];
+                u0 += red[1][w];
+            }
+            double* e = a.epart + ((size_t)(a.e_band0 + b) * gridDim.x + blockIdx.x) * 2;
+            e[0] = u1;
+            e[1] = u0;
+        }
+        if (!valid) return;
+    }
+    fftreg::fft_split_to_nat<-1, N1, N2>(v);
+    {
+        float2* p = line;
+#pragma unroll
+        for (int x = 0; x < N; ++x) {
+            if ((m[x >> 5] >> (x & 31)) & 1u) {
+                __stcs(p, v[x]);
+                p += N23;
+            }
+        }
+    }
+}
+
 // Density x pass: a block owns (j, k0..k0+KT) and loops over all bands of the
 // chunk in groups of BB: G->r along x, then
 //   rho[x][j][k0+kk] += sum_b occ_b |psi_b(x, j, k0+kk)|^2
@@ -569,6 +682,19 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
     a->kt_f = make_fastdiv((uint32_t)a->kt);
 }
 
+#define XREG_LAUNCH(PL, G)                                                                    \
+    do {                                                                                      \
+        if (a.epart) x_pass_reg<PL, true><<<G, XREG_THREADS, 0, st>>>(a, T, vloc);           \
+        else x_pass_reg<PL, false><<<G, XREG_THREADS, 0, st>>>(a, T, vloc);                  \
+    } while (0)
+
+// the register x pass serves the complex64 compile-time plans
+template <typename C, typename PL>
+constexpr bool xreg_plan()
+{
+    return std::is_same<C, float2>::value && !std::is_same<PL, NoPlan>::value;
+}
+
 template <typename C, typename V, bool WIDE, typename PL, int KTC>
 static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic,
                                   C* T, const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st,
@@ -590,9 +716,13 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     g2r<<<gp, ptg, sp, st>>>(a, psi, T, twy, twz);
     prof->close(h, st);
     if (a.after_g2r && (e = cudaEventRecord(a.after_g2r, st))) return e;
-    dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
     h = prof->open(PH_XPASS, st);
-    xp<<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    if constexpr (xreg_plan<C, PL>()) {
+        XREG_LAUNCH(PL, dim3(ceil_div(PL::n * PL::n, XREG_THREADS), nb));
+    } else {
+        dim3 gx(ceil_div(a.n3, a.kt), a.n2, ceil_div(nb, a.bb));
+        xp<<<gx, 256, sx, st>>>(a, nb, T, vloc, twx);
+    }
     prof->close(h, st);
     h = prof->open(PH_R2G, st);
     r2g<<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
@@ -616,8 +746,12 @@ static cudaError_t launch_local_batch_t(const LocalArgs& a, int nbands, int max_
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     dim3 gp(max_nxs, nbands);
     g2r<<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
-    dim3 gx(ceil_div(a.n3, a.kt), a.n2, nxblk);
-    xp<<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
+    if constexpr (xreg_plan<C, PL>()) {
+        XREG_LAUNCH(PL, dim3(ceil_div(PL::n * PL::n, XREG_THREADS), nbands));
+    } else {
+        dim3 gx(ceil_div(a.n3, a.kt), a.n2, nxblk);
+        xp<<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
+    }
     r2g<<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
     return cudaGetLastError();
 }
@@ -700,6 +834,16 @@ cudaError_t launch_density(const LocalArgs& a, int nb, const double2* psi, const
     return with_kernels<C>(a, [&](auto wide, auto pl, auto) {
         return launch_density_t<C, decltype(wide)::value, decltype(pl)>(a, nb, psi, occ, rho, T, twx, twy, twz, st);
     });
+}
+
+int local_energy_slots(const LocalArgs& a, size_t csize)
+{
+    if (csize == sizeof(float2) && !fft_needs_wide(a.Lx) && !fft_needs_wide(a.Ly) && !fft_needs_wide(a.Lz)) {
+        const int id = fft_ct_id(a.Lx);
+        if (id != FFT_CT_NONE && fft_ct_id(a.Ly) == id && fft_ct_id(a.Lz) == id)
+            return ceil_div(a.n2 * a.n3, XREG_THREADS);  // the register x pass: one slot per block of a band
+    }
+    return ((a.n3 + a.kt - 1) / a.kt) * a.n2;  // the shared-memory x pass: one slot per (j, k-tile) block
 }
 
 size_t local_xpass_smem(const LocalArgs& a, bool fp64)

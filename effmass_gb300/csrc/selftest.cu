@@ -4,6 +4,7 @@
 
 #include "hpsi_gb300.h"
 #include "common.cuh"
+#include "tc_gemm.cuh"
 
 namespace {
 
@@ -46,4 +47,12 @@ extern "C" int hpsi_selftest_convert(const double* x, long n, float* f_bits, flo
     if (!e) e = cudaMemcpy(d_hw, dh, nd, cudaMemcpyDeviceToHost);
     cudaFree(m);
     return e ? HPSI_ERR_CUDA : HPSI_OK;
+}
+
+// Test hook of the bounded pipeline waits: lowers the poll limit of the
+// tensor-core GEMMs' MMA issuer (0: it gives up at once) so that a test can
+// watch a wait run out and the error reach the caller as HPSI_ERR_TIMEOUT.
+extern "C" int hpsi_selftest_wait_limit(long polls)
+{
+    return tc_set_issue_wait_limit(polls) == cudaSuccess ? HPSI_OK : HPSI_ERR_CUDA;
 }

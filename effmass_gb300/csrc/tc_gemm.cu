@@ -87,6 +87,34 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
     return false;
 }
 
+// bounded wait with a given poll limit (0: give up at once, without polling)
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t limit)
+{
+    for (uint32_t i = 0; i < limit; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (i > 32) __nanosleep(40);
+    }
+    return false;
+}
+
+// bounded wait that also gives up as soon as another thread of the CTA has
+// set *abort (the producer's wait for a stage the MMA issuer will not free)
+__device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, const uint32_t* abort)
+{
+    for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*(const volatile uint32_t*)abort) return false;
+        if (i > 32) __nanosleep(40);
+    }
+    return false;
+}
+
+// Poll limit of the MMA issuer's wait for a loaded stage.  WAIT_LIMIT unless a
+// test lowers it (tc_set_issue_wait_limit) to make that wait run out: the
+// kernel then takes its error path (flag, abort, bounded drain of the copies
+// in flight, TMEM freed), which no fault or trap is needed to reach.
+__device__ uint32_t g_tc_issue_wait_limit = WAIT_LIMIT;
+
 // bulk copy of bytes (multiple of 16, both addresses 16-byte aligned) from
 // global to shared memory, completing on an mbarrier transaction count
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
@@ -210,7 +238,10 @@ __global__ void __launch_bounds__(192, 1)
         for (int it = 0; it < nk; ++it) {
             const int s = it % STAGES;
             const uint32_t ph = (it / STAGES) & 1;
-            if (!mbar_wait(&sh->empty[s], ph ^ 1)) { atomicExch(err, 1); sh->abort_flag = 1; break; }
+            if (!mbar_wait_abort(&sh->empty[s], ph ^ 1, &sh->abort_flag)) {
+                if (!*(volatile uint32_t*)&sh->abort_flag) { atomicExch(err, 1); sh->abort_flag = 1; }
+                break;
+            }
             if (*(volatile uint32_t*)&sh->abort_flag) break;
             unsigned char* st = tiles + s * STAGE_BYTES;
             mbar_arrive_expect_tx(&sh->full[s], STAGE_BYTES);
@@ -229,10 +260,11 @@ __global__ void __launch_bounds__(192, 1)
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer
         bool ok = true;
+        const uint32_t lim = g_tc_issue_wait_limit;
         for (int it = 0; it < nk; ++it) {
             const int s = it % STAGES;
             const uint32_t ph = (it / STAGES) & 1;
-            if (!mbar_wait(&sh->full[s], ph)) { atomicExch(err, 2); sh->abort_flag = 1; ok = false; break; }
+            if (!mbar_wait_n(&sh->full[s], ph, lim)) { atomicExch(err, 2); sh->abort_flag = 1; ok = false; break; }
             tc_fence_after();
             const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
             const uint64_t ah = sdesc_sw64(st), al = sdesc_sw64(st + A_TILE);
@@ -907,4 +939,11 @@ int tc_chain_splits(size_t ldk, int chain_k)
 {
     const int kt = (int)(ldk / BK), per = chain_k / BK > 0 ? chain_k / BK : 1;
     return ceil_div(kt, per);
+}
+
+// Test hook: the MMA issuer's poll limit (polls < 0: back to the default).
+cudaError_t tc_set_issue_wait_limit(long polls)
+{
+    const uint32_t v = polls < 0 ? WAIT_LIMIT : (uint32_t)std::min<long>(polls, (long)WAIT_LIMIT);
+    return cudaMemcpyToSymbol(g_tc_issue_wait_limit, &v, sizeof(v));
 }

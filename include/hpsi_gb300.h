@@ -256,13 +256,16 @@ int hpsi_velocity_matrix(hpsi_ctx* ctx, int kid, int nb, const double* psi, doub
  * (a fixed device-memory budget, a host runtime whose allocator owns all
  * device memory, or code that must not add an allocation's implicit device
  * synchronisation).  No counterpart in the reference.  Same result as
- * hpsi_apply; psi/hpsi must be device pointers (HPSI_DEVICE_PTRS).  All
- * scratch lives in one static device array of HPSI_NOALLOC_SCRATCH_BYTES that
- * every GPU loading the library holds until exit; sizes that do not fit are
- * rejected with HPSI_ERR_BAD_ARG.  The projector matrices of the precision
- * must exist (built by a first hpsi_apply/hpsi_grad_apply at that precision),
- * else HPSI_ERR_STATE.  The first call on a device looks up the array's
- * address (make it before any stream capture).  Calls share the array:
+ * hpsi_apply at HPSI_PREC_FP64 or HPSI_PREC_FP32; the tensor-core precisions
+ * are refused with HPSI_ERR_BAD_ARG.  psi/hpsi must be device pointers
+ * (HPSI_DEVICE_PTRS).  All scratch lives in one static device array of
+ * HPSI_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit; a call whose chunks do not fit is rejected with HPSI_ERR_BAD_ARG
+ * before any launch, leaving hpsi untouched.  The projector matrices of the
+ * precision must exist (built by a first hpsi_apply/hpsi_grad_apply at that
+ * precision), else HPSI_ERR_STATE.  The first call on a device looks up the
+ * array's address and keeps it (make it before any stream capture; the kept
+ * address is not valid after cudaDeviceReset).  Calls share the array:
  * calls that overlap on the GPU race. */
 #define HPSI_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int hpsi_apply_noalloc(hpsi_ctx* ctx, int kid, int nb, const double* psi, double* hpsi,
@@ -363,6 +366,29 @@ const char* hpsi_batch_last_error(const hpsi_batch* b);
  * by bit arithmetic (f_bits) and by the hardware (f_hw), and the conversion of
  * f_hw back to double both ways (d_bits, d_hw).  No reference counterpart. */
 int hpsi_selftest_convert(const double* x, long n, float* f_bits, float* f_hw, double* d_bits, double* d_hw);
+
+/* Self-test of the device line transforms (no reference counterpart): the
+ * reference's FFT3D (src/math/fft.cppm:60-85) on an n1 x n2 x n3 grid of
+ * complex<double> in host memory, transformed in place: dir = +1 G->r
+ * (unnormalised, exp(+i..)), -1 r->G (exp(-i..), 1/n per axis), lines along z,
+ * then y, then x.  HPSI_PREC_FP64: the complex128 runtime-plan stages;
+ * HPSI_PREC_FP32: complex64, with the compile-time plans and the x pass's
+ * register transform when n1 = n2 = n3 is 24, 36, 64 or 72. */
+int hpsi_selftest_fft3d(int n1, int n2, int n3, double* grid, int dir, int flags);
+
+/* Self-test of the k-point tables (no reference counterpart): copies the
+ * device Y_lm, dY_lm/dtheta, (1/sin theta) dY_lm/dphi ([3][(l_max+1)^2][npw];
+ * the derivatives only with dbeta tables) and S_a(G) ([n_atoms][npw]
+ * complex) of slot kid to host buffers (either may be NULL). */
+int hpsi_selftest_kpoint_tables(hpsi_ctx* ctx, int kid, double* ylm, double* sf);
+
+/* Test hook of the bounded pipeline waits (no reference counterpart): sets
+ * the poll limit of the tensor-core GEMMs' MMA issuer for the current device
+ * (0: its wait for a loaded stage gives up at once; polls < 0: back to the
+ * default of about a second).  With a lowered limit the GEMM takes its error
+ * path (error flag, abort, bounded drain of the copies in flight, TMEM freed)
+ * and the next synchronising call returns HPSI_ERR_TIMEOUT. */
+int hpsi_selftest_wait_limit(long polls);
 
 /* Message of the last failed call on ctx (never NULL); with ctx == NULL the
  * message of the calling thread's last failed hpsi_ctx_create. */

@@ -1,7 +1,7 @@
 """Timed CPU baseline of H|psi> on the host cores — TEST INFRASTRUCTURE.
 
-Runs the reference's own H|psi> (oracle/_ref/ref_driver, built from the
-reference sources) as one single-threaded process per core — the reference
+Runs the reference's own H|psi> (oracle/_ref/ref_bench, built from the
+reference sources at -O3) as one single-threaded process per core — the reference
 is single-threaded — over independent bands of the same k-point.  If the
 reference driver cannot be built on this machine, the oracle port
 (oracle/hpsi_oracle.c) runs instead on the same number of threads.
@@ -53,7 +53,7 @@ def run(sysm, kp, psi, bands_per_worker: int = 2, workers: int = 0):
             procs = []
             for w in range(workers):
                 b0 = (w * bands_per_worker) % nb
-                procs.append(subprocess.Popen([O.REF_DRIVER, "time", spec, os.path.join(td, f"wd{w}"), "0", str(b0),
+                procs.append(subprocess.Popen([O.REF_BENCH, "time", spec, os.path.join(td, f"wd{w}"), "0", str(b0),
                                                str(bands_per_worker)], stdout=subprocess.PIPE,
                                               stderr=subprocess.DEVNULL, text=True))
             secs = []
@@ -65,7 +65,7 @@ def run(sysm, kp, psi, bands_per_worker: int = 2, workers: int = 0):
         t = max(secs)
         return dict(value=workers * bands_per_worker / t, per_core_value=bands_per_worker / statistics.median(secs),
                     cores=workers, kind="reference", seconds=t, cpu=cpu_model(),
-                    sample=f"{workers} single-threaded reference processes x {bands_per_worker} bands "
+                    sample=f"{workers} single-threaded reference processes (g++ -O3) x {bands_per_worker} bands "
                            f"(npw={kp.npw}), H|psi> time only")
     # fallback: the oracle port, threads over bands
     O.build()

@@ -781,6 +781,294 @@ int oracle_beta_tables(int nr, const double* r, const double* rab, int uniform, 
     return HPSI_OK;
 }
 
+/* d2beta/dq2 tables as D2BetaqTables builds them (src/pseudo/ncpp_advance.cppm: */
+/* 908-1085): 4 pi S[beta r^3 j_l''(q r)] with j_l'' from SphericalBesselJ::      */
+/* secondDerivValue (src/math/sph_bessel.cppm:242-268):                          */
+/*   j_l''(x) = (l(l-1)/x^2 - 1) j_l(x) + (2/x) j_{l+1}(x),  x >= 1e-15,          */
+/*   j_0''(0) = -1/3, j_2''(0) = 2/15, else 0;                                    */
+/* a q below 1e-15 gives 0 for l other than 0 and 2 (:1019-1023).  Same grid and  */
+/* trimming as oracle_beta_tables.                                                */
+int oracle_d2beta_tables(int nr, const double* r, const double* rab, int uniform, int np, const int* l,
+                         const double* beta, double dq, double q_max, double* d2bq)
+{
+    const int nq = (int)ceil(q_max / dq) + 1 + 3;
+    double* f = (double*)malloc(sizeof(double) * (nr > 0 ? nr : 1));
+    if (!f) return HPSI_ERR_OOM;
+    const double FOUR_PI = 4.0 * 3.14159265358979323846;
+    for (int p = 0; p < np; ++p) {
+        const double* b = beta + (size_t)p * nr;
+        const int lp = l[p];
+        int n = nr;
+        while (n > 0 && b[n - 1] == 0.0) --n;
+        for (int iq = 0; iq < nq; ++iq) {
+            const double q = iq * dq;
+            double* out = d2bq + (size_t)p * nq + iq;
+            if (q < 1e-15 && lp != 0 && lp != 2) { *out = 0.0; continue; }
+            for (int i = 0; i < n; ++i) {
+                const double x = q * r[i];
+                double d;
+                if (fabs(x) < 1e-15) d = lp == 0 ? -1.0 / 3.0 : (lp == 2 ? 2.0 / 15.0 : 0.0);
+                else {
+                    const double inv_x = 1.0 / x;
+                    d = ((double)(lp * (lp - 1)) * inv_x * inv_x - 1.0) * ref_jl(lp, x) + 2.0 * inv_x * ref_jl(lp + 1, x);
+                }
+                f[i] = b[i] * r[i] * r[i] * r[i] * d;
+            }
+            *out = n ? FOUR_PI * ref_simpson(f, rab, n, uniform) : 0.0;
+        }
+    }
+    free(f);
+    return HPSI_OK;
+}
+
+/* g_n(x) = j_n(x) / x^n: power series below x = n + 2, else ref_jl(n, x)/x^n */
+static double oracle_gn(int n, double x)
+{
+    if (x < n + 2.0) {
+        const double x2h = x * x / 2.0;
+        double term = 1.0, sum = 1.0;
+        for (int k = 1; k <= 80; ++k) {
+            term *= -x2h / ((double)k * (2.0 * n + 2.0 * k + 1.0));
+            sum += term;
+            if (fabs(term) < 1e-17 * fabs(sum)) break;
+        }
+        double df = 1.0;
+        for (int i = 3; i <= 2 * n + 1; i += 2) df *= i;
+        return sum / df;
+    }
+    return ref_jl(n, x) / pow(x, n);
+}
+
+/* Radial tables of the Hessian's projector second derivatives on q_i = i dq, */
+/* i < ceil(q_max/dq) + 4, out [3][np][nq] (F0, F1, F3, raw):                  */
+/*   F0 =  4 pi S[beta r^(l+1) g_l(q r)]     = beta(q) / q^l                    */
+/*   F1 = -4 pi S[beta r^(l+3) g_(l+1)(q r)] = F0'(q) / q                       */
+/*   F3 =  4 pi S[beta r^(l+5) g_(l+2)(q r)] = (F0'' - F0'/q) / q^2             */
+/* with the reference's Simpson rule and per-projector trimming.               */
+int oracle_hess_tables(int nr, const double* r, const double* rab, int uniform, int np, const int* l,
+                       const double* beta, double dq, double q_max, double* out)
+{
+    const int nq = (int)ceil(q_max / dq) + 1 + 3;
+    double* f = (double*)malloc(sizeof(double) * (nr > 0 ? nr : 1));
+    if (!f) return HPSI_ERR_OOM;
+    const double FOUR_PI = 4.0 * 3.14159265358979323846;
+    for (int p = 0; p < np; ++p) {
+        const double* b = beta + (size_t)p * nr;
+        const int lp = l[p];
+        int n = nr;
+        while (n > 0 && b[n - 1] == 0.0) --n;
+        for (int iq = 0; iq < nq; ++iq) {
+            const double q = iq * dq;
+            for (int t = 0; t < 3; ++t) {
+                const int e = lp + 1 + 2 * t, ord = lp + t;
+                for (int i = 0; i < n; ++i) f[i] = b[i] * pow(r[i], e) * oracle_gn(ord, q * r[i]);
+                const double v = n ? FOUR_PI * ref_simpson(f, rab, n, uniform) : 0.0;
+                out[((size_t)t * np + p) * nq + iq] = t == 1 ? -v : v;
+            }
+        }
+    }
+    free(f);
+    return HPSI_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* d2H/dk_a dk_b |psi>: the operator the reference declares with its six     */
+/* outputs xx yy zz xy xz yz (src/H_psi/hamiltonian.cppm:84-91) and leaves    */
+/* empty (src/H_psi/hamiltonian_hessian.cpp:48-50).                           */
+/*   out_ab += delta_ab psi + sum_p lambda (|d_ab p><p| + |d_a p><d_b p|      */
+/*                                          + |d_b p><d_a p| + |p><d_ab p|) psi */
+/* p and d_a p exactly as oracle_grad (the reference's gradient); d_ab p of   */
+/* u = beta(q) Y_lm = F0(q) R(K) with the radial tables F0 = beta/q^l,         */
+/* F1 = F0'/q, F3 = (F0'' - F0'/q)/q^2 (ftab[species] = [3][n_proj][nq], raw;  */
+/* the reference's Lagrange stencil, times 1/sqrt(omega), range q <=          */
+/* dq (nq - 3)):                                                              */
+/*   d_ab u = F3 K_a K_b R + F1 (delta_ab R + K_a d_b R + K_b d_a R) + F0 d_ab R */
+/* where R = q^l Y_lm is the solid harmonic of the reference's Y_lm          */
+/* (oracle_ylm) and its gradient and Hessian are central differences of step  */
+/* 1 bohr^-1 — exact for these polynomials of degree l <= 2 (l > 2 refused).   */
+/* out: [6][nb][npw] interleaved complex.                                     */
+/* ------------------------------------------------------------------------ */
+int oracle_hess(const hpsi_system* sys, const hpsi_kpoint* kp, int nb, const double* psi, const double* const* ftab,
+                int nq, double dq, double* out)
+{
+    if (!sys || !kp || nb < 0 || !ftab) return HPSI_ERR_BAD_ARG;
+    const int ng = kp->npw;
+    if (nb == 0 || ng == 0) return HPSI_OK;
+    const int lmax = species_lmax(sys);
+    if (lmax > 2) return HPSI_ERR_BAD_ARG;
+    const int nlm = (lmax + 1) * (lmax + 1);
+    const double norm = 1.0 / sqrt(sys->omega);
+    const double qtop = dq * (nq - 3);
+    static const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+    const size_t nel = (size_t)nb * ng;
+    /* kinetic: delta_ab */
+    for (int k = 0; k < 3; ++k)
+        for (size_t i = 0; i < 2 * nel; ++i) out[(size_t)k * 2 * nel + i] += psi[i];
+    /* solid harmonics on the 19-point stencil of every G: K, K +- e_a, K +- e_a +- e_b */
+    enum { NS = 19 };
+    int off[NS][3];
+    {
+        int n = 0;
+        off[n][0] = off[n][1] = off[n][2] = 0; ++n;
+        for (int a = 0; a < 3; ++a)
+            for (int sg = -1; sg <= 1; sg += 2) { off[n][0] = off[n][1] = off[n][2] = 0; off[n][a] = sg; ++n; }
+        for (int a = 0; a < 3; ++a)
+            for (int b = a + 1; b < 3; ++b)
+                for (int sa = -1; sa <= 1; sa += 2)
+                    for (int sb = -1; sb <= 1; sb += 2) {
+                        off[n][0] = off[n][1] = off[n][2] = 0;
+                        off[n][a] = sa; off[n][b] = sb; ++n;
+                    }
+    }
+    const size_t npts = (size_t)NS * ng;
+    double* Kp = (double*)malloc(sizeof(double) * 3 * npts);
+    double* sq = (double*)malloc(sizeof(double) * 3 * npts);
+    double* yv = (double*)malloc(sizeof(double) * (size_t)nlm * npts);
+    double* R = (double*)malloc(sizeof(double) * (size_t)nlm * npts);
+    if (!Kp || !sq || !yv || !R) { free(Kp); free(sq); free(yv); free(R); return HPSI_ERR_OOM; }
+    for (int ig = 0; ig < ng; ++ig)
+        for (int t = 0; t < NS; ++t)
+            for (int d = 0; d < 3; ++d) Kp[3 * ((size_t)t * ng + ig) + d] = kp->kvec[3 * ig + d] + off[t][d];
+    oracle_spherical((int)npts, Kp, sq, sq + npts, sq + 2 * npts);
+    oracle_ylm(lmax, (int)npts, sq + npts, sq + 2 * npts, yv, NULL, NULL);
+    for (int l = 0; l <= lmax; ++l)
+        for (int m = -l; m <= l; ++m) {
+            const size_t lm = (size_t)(l * l + l + m) * npts;
+            for (size_t i = 0; i < npts; ++i) {
+                double ql = 1.0;
+                for (int e = 0; e < l; ++e) ql *= sq[i];
+                R[lm + i] = ql * yv[lm + i];
+            }
+        }
+    /* stencil index of K + s_a e_a (s = -1 -> 0, +1 -> 1) and of K + s_a e_a + s_b e_b */
+#define ST1(a, s) (1 + 2 * (a) + ((s) > 0))
+    int st2[3][3][2][2];
+    {
+        int n = 7;
+        for (int a = 0; a < 3; ++a)
+            for (int b = a + 1; b < 3; ++b)
+                for (int sa = 0; sa < 2; ++sa)
+                    for (int sb = 0; sb < 2; ++sb) st2[a][b][sa][sb] = n++;
+    }
+    double* beta = (double*)malloc(sizeof(double) * ng);
+    double* dbeta = (double*)malloc(sizeof(double) * ng);
+    double* F = (double*)malloc(sizeof(double) * 3 * ng);
+    double* S = (double*)malloc(sizeof(double) * 2 * ng);
+    double* pv = (double*)malloc(sizeof(double) * 20 * ng); /* p, d_x p, d_y p, d_z p, d_ab p (6): complex */
+    double* cf = (double*)malloc(sizeof(double) * 20 * nb);
+    int rc = (beta && dbeta && F && S && pv && cf) ? HPSI_OK : HPSI_ERR_OOM;
+    kprep P;
+    kprep_init(&P, sys, kp, 1);
+    for (int s = 0; s < sys->n_species && rc == HPSI_OK; ++s) {
+        const hpsi_species* sp = &sys->species[s];
+        if (!sp->dbeta_q || !ftab[s]) { rc = HPSI_ERR_STATE; break; }
+        for (int a = 0; a < sys->n_atoms && rc == HPSI_OK; ++a) {
+            if (sys->atom_species[a] != s) continue;
+            rc = oracle_structure_factor(ng, kp->g_idx, kp->k_frac, sys->atom_tau + 3 * a, sys->n1, sys->n2, sys->n3, S);
+            if (rc) break;
+            for (int ip = 0; ip < sp->n_proj && rc == HPSI_OK; ++ip) {
+                const double lam = sp->lambda[ip];
+                if (fabs(lam) < 1e-15) continue;
+                const int l = sp->proj_l[ip];
+                const double* tab = sp->beta_q + (size_t)ip * sp->nq;
+                const double* dtab = sp->dbeta_q + (size_t)ip * sp->nq;
+                double db0;
+                oracle_beta_interp(dtab, sp->nq, sp->dq, sp->q_max, norm, 0.0, &db0);
+                for (int ig = 0; ig < ng && rc == HPSI_OK; ++ig) {
+                    rc = oracle_beta_interp(tab, sp->nq, sp->dq, sp->q_max, norm, P.q[ig], &beta[ig]);
+                    if (!rc) rc = oracle_beta_interp(dtab, sp->nq, sp->dq, sp->q_max, norm, P.q[ig], &dbeta[ig]);
+                    for (int t = 0; t < 3 && !rc; ++t)
+                        rc = oracle_beta_interp(ftab[s] + ((size_t)t * sp->n_proj + ip) * nq, nq, dq, qtop, norm,
+                                                P.q[ig], &F[3 * ig + t]);
+                }
+                if (rc) break;
+                for (int m = -l; m <= l; ++m) {
+                    const size_t lmk = (size_t)(l * l + l + m) * ng, lmR = (size_t)(l * l + l + m) * npts;
+                    const double* y = P.y + lmk;
+                    const double* yt = P.yth + lmk;
+                    const double* yp = P.yph + lmk;
+                    for (int ig = 0; ig < ng; ++ig) {
+                        /* p and d_a p: oracle_grad's formulas */
+                        const double q = P.q[ig];
+                        const double boq = (q > 1e-12) ? beta[ig] / q : db0;
+                        const double gq = dbeta[ig] * y[ig], gt = boq * yt[ig], gp = boq * yp[ig];
+                        const double sth = P.st[ig], cth = P.ct[ig], sph = P.sp[ig], cph = P.cp[ig];
+                        double f[10];
+                        f[0] = beta[ig] * y[ig];
+                        f[1] = sth * cph * gq + cth * cph * gt - sph * gp;
+                        f[2] = sth * sph * gq + cth * sph * gt + cph * gp;
+                        f[3] = cth * gq - sth * gt;
+                        /* d_ab u from F0, F1, F3 and the solid harmonic's differences */
+                        const double* Rl = R + lmR;
+                        const double R0 = Rl[ig];
+                        double dR[3], HR[6];
+                        for (int d = 0; d < 3; ++d)
+                            dR[d] = (Rl[(size_t)ST1(d, 1) * ng + ig] - Rl[(size_t)ST1(d, -1) * ng + ig]) / 2.0;
+                        for (int c = 0; c < 6; ++c) {
+                            const int ca = pa[c], cb = pb[c];
+                            if (ca == cb)
+                                HR[c] = Rl[(size_t)ST1(ca, 1) * ng + ig] - 2.0 * R0 + Rl[(size_t)ST1(ca, -1) * ng + ig];
+                            else
+                                HR[c] = (Rl[(size_t)st2[ca][cb][1][1] * ng + ig] - Rl[(size_t)st2[ca][cb][1][0] * ng + ig] -
+                                         Rl[(size_t)st2[ca][cb][0][1] * ng + ig] + Rl[(size_t)st2[ca][cb][0][0] * ng + ig]) / 4.0;
+                        }
+                        const double* K = kp->kvec + 3 * ig;
+                        const double F0 = F[3 * ig], F1 = F[3 * ig + 1], F3 = F[3 * ig + 2];
+                        for (int c = 0; c < 6; ++c) {
+                            const int ca = pa[c], cb = pb[c];
+                            f[4 + c] = F3 * K[ca] * K[cb] * R0 + F1 * ((ca == cb ? R0 : 0.0) + K[ca] * dR[cb] + K[cb] * dR[ca]) +
+                                       F0 * HR[c];
+                        }
+                        const double Sr = S[2 * ig], Si = S[2 * ig + 1];
+                        for (int c = 0; c < 10; ++c) {
+                            pv[20 * ig + 2 * c] = f[c] * Sr;
+                            pv[20 * ig + 2 * c + 1] = f[c] * Si;
+                        }
+                    }
+                    /* coefficients <f_c|psi_b> */
+                    for (int b = 0; b < nb; ++b) {
+                        const double* ps = psi + 2 * (size_t)ng * b;
+                        for (int c = 0; c < 10; ++c) {
+                            double cr = 0.0, ci = 0.0;
+                            for (int ig = 0; ig < ng; ++ig) {
+                                const double pr = pv[20 * ig + 2 * c], pi_ = pv[20 * ig + 2 * c + 1];
+                                cr += pr * ps[2 * ig] + pi_ * ps[2 * ig + 1];
+                                ci += pr * ps[2 * ig + 1] - pi_ * ps[2 * ig];
+                            }
+                            cf[20 * b + 2 * c] = cr;
+                            cf[20 * b + 2 * c + 1] = ci;
+                        }
+                    }
+                    for (int k = 0; k < 6; ++k) {
+                        const int ka = pa[k], kb = pb[k];
+                        /* (ket row, coefficient row): d_ab p <p|, d_a p <d_b p|, d_b p <d_a p|, p <d_ab p| */
+                        const int ket[4] = {4 + k, 1 + ka, 1 + kb, 0}, bra[4] = {0, 1 + kb, 1 + ka, 4 + k};
+                        for (int b = 0; b < nb; ++b) {
+                            double* o = out + ((size_t)k * nb + b) * 2 * ng;
+                            for (int ig = 0; ig < ng; ++ig) {
+                                double sr = 0.0, si = 0.0;
+                                for (int t = 0; t < 4; ++t) {
+                                    const double vr = pv[20 * ig + 2 * ket[t]], vi = pv[20 * ig + 2 * ket[t] + 1];
+                                    const double cr = cf[20 * b + 2 * bra[t]], ci = cf[20 * b + 2 * bra[t] + 1];
+                                    sr += cr * vr - ci * vi;
+                                    si += cr * vi + ci * vr;
+                                }
+                                o[2 * ig] += lam * sr;
+                                o[2 * ig + 1] += lam * si;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+#undef ST1
+    kprep_free(&P);
+    free(Kp); free(sq); free(yv); free(R);
+    free(beta); free(dbeta); free(F); free(S); free(pv); free(cf);
+    return rc;
+}
+
 /* 1-D transform with the pocketfft convention (test hook for the FFT KATs). */
 int oracle_fft1d(double* c, int n, int sign, double fct)
 {

@@ -17,6 +17,8 @@ from effmass_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libhpsi_oracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+# the same reference sources at -O3 (default FP contraction): the timed CPU baseline
+REF_BENCH = os.path.join(HERE, "_ref", "ref_bench")
 
 _lib = None
 
@@ -31,7 +33,7 @@ def build_ref(quiet: bool = True) -> bool:
     r = subprocess.run(["make", "-s", "-C", HERE, "ref"],
                        stdout=subprocess.DEVNULL if quiet else None,
                        stderr=subprocess.DEVNULL if quiet else None)
-    return r.returncode == 0 and os.path.exists(REF_DRIVER)
+    return r.returncode == 0 and os.path.exists(REF_DRIVER) and os.path.exists(REF_BENCH)
 
 
 def lib():
@@ -56,6 +58,9 @@ def lib():
         L.oracle_fft1d.argtypes = [dp, C.c_int, C.c_int, C.c_double]
         L.oracle_spherical.argtypes = [C.c_int, dp, dp, dp, dp]
         L.oracle_spherical.restype = None
+        L.oracle_d2beta_tables.argtypes = [C.c_int, dp, dp, C.c_int, C.c_int, ip, dp, C.c_double, C.c_double, dp]
+        L.oracle_hess.argtypes = [sysp, kpp, C.c_int, dp, C.POINTER(dp), C.c_int, C.c_double, dp]
+        L.oracle_hess_tables.argtypes = [C.c_int, dp, dp, C.c_int, C.c_int, ip, dp, C.c_double, C.c_double, dp]
         _lib = L
     return _lib
 
@@ -114,6 +119,46 @@ def beta_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float =
                                     l.ctypes.data_as(C.POINTER(C.c_int)), abi.cptr(beta), dq, q_max,
                                     abi.cptr(bq), abi.cptr(dbq)))
     return bq, dbq
+
+
+def d2beta_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float = 20.0):
+    """d2beta/dq2 [n_proj][nq] as the reference's D2BetaqTables builds it (raw)."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    rab = np.ascontiguousarray(rab, dtype=np.float64)
+    l = np.ascontiguousarray(l, dtype=np.int32)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    nq = int(np.ceil(q_max / dq)) + 4
+    d2 = np.zeros((beta.shape[0], nq))
+    _check(lib().oracle_d2beta_tables(r.size, abi.cptr(r), abi.cptr(rab), int(uniform), beta.shape[0],
+                                      l.ctypes.data_as(C.POINTER(C.c_int)), abi.cptr(beta), dq, q_max,
+                                      abi.cptr(d2)))
+    return d2
+
+
+def hess_tables(r, rab, uniform: bool, l, beta, dq: float = 0.01, q_max: float = 20.0):
+    """[3][n_proj][nq] radial tables F0 = beta/q^l, F1 = F0'/q, F3 = (F0'' - F0'/q)/q^2 (raw)."""
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    rab = np.ascontiguousarray(rab, dtype=np.float64)
+    l = np.ascontiguousarray(l, dtype=np.int32)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    nq = int(np.ceil(q_max / dq)) + 4
+    f = np.zeros((3, beta.shape[0], nq))
+    _check(lib().oracle_hess_tables(r.size, abi.cptr(r), abi.cptr(rab), int(uniform), beta.shape[0],
+                                    l.ctypes.data_as(C.POINTER(C.c_int)), abi.cptr(beta), dq, q_max, abi.cptr(f)))
+    return f
+
+
+def hess(sysm, kp, psi: np.ndarray, ftabs, dq: float) -> np.ndarray:
+    """d2H/dk_a dk_b |psi> [6][nb][npw] (xx, yy, zz, xy, xz, yz); ftabs[s] are the
+    species' radial tables [3][n_proj][nq] (F0, F1, F3, raw) on q_i = i dq."""
+    psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(-1, kp.npw)
+    ft = [np.ascontiguousarray(f, dtype=np.float64) for f in ftabs]
+    nq = ft[0].shape[-1]
+    arr = (C.POINTER(C.c_double) * len(ft))(*[abi.cptr(f) for f in ft])
+    out = np.zeros((6,) + psi.shape, dtype=np.complex128)
+    S, K = abi.pack_system(sysm), abi.pack_kpoint(kp)
+    _check(lib().oracle_hess(S.ref(), K.ref(), psi.shape[0], abi.cptr(psi), arr, nq, dq, abi.cptr(out)))
+    return out
 
 
 def ylm(lmax: int, theta, phi):

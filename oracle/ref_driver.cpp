@@ -260,7 +260,7 @@ void setup(const Spec& s, const std::string& dir) {
     for (auto& sp : s.species) registry()[upfName(sp.z)] = &sp;
 }
 
-void load(Hamiltonian& H, const Spec& s, bool with_wg) {
+void load(Hamiltonian& H, const Spec& s, bool with_wg, bool with_d2 = false) {
     H.loadGKK("OUT.GKK");
     H.loadVR("OUT.VR");
     H.loadATOM("atom.config");
@@ -268,6 +268,7 @@ void load(Hamiltonian& H, const Spec& s, bool with_wg) {
     for (auto& sp : s.species) H.loadNCPP(upfName(sp.z));
     std::uint64_t feat = static_cast<std::uint64_t>(PSPFeature::Nonlocal) |
                          static_cast<std::uint64_t>(PSPFeature::DBetaq);
+    if (with_d2) feat |= static_cast<std::uint64_t>(PSPFeature::D2Betaq);
     H.finalize({ExtendedCheck::NCPPAtomCoverage}, feat);
 }
 
@@ -378,14 +379,16 @@ int timeit(const std::string& spec_path, const std::string& dir, int ik, int ban
 // Radial inputs of the beta(q) / dbeta(q)/dq tables as the reference builds
 // them in Hamiltonian::finalize (src/H_psi/hamiltonian.cpp:297-316: sortByL,
 // diagonalizeNonlocal, then BetaqTables / DBetaqTables from mesh r, rab and
-// the rotated beta(r)).  Output per species: "TABREF01", z, mesh type
-// (0 uniform, 1 general), nr, r[nr], rab[nr], n_proj, then per projector l,
-// len and beta[len]; then the tables: nt, nq, beta_q[nt][nq], dbeta_q[nt][nq].
+// the rotated beta(r)), and D2BetaqTables (src/pseudo/ncpp_advance.cppm:
+// 908-1085, d2 beta/dq2 for the Hessian).  Output per species: "TABREF01", z,
+// mesh type (0 uniform, 1 general), nr, r[nr], rab[nr], n_proj, then per
+// projector l, len and beta[len]; then the tables: nt, nq, beta_q[nt][nq],
+// dbeta_q[nt][nq], d2beta_q[nt][nq] (raw, without 1/sqrt(omega)).
 int tables(const std::string& spec_path, const std::string& out_path, const std::string& dir) {
     Spec s = readSpec(spec_path);
     setup(s, dir);
     Hamiltonian H(dir);
-    load(H, s, true);
+    load(H, s, true, true);
     std::FILE* f = std::fopen(out_path.c_str(), "wb");
     if (!f) throw std::runtime_error("cannot write " + out_path);
     Out O{f};
@@ -415,6 +418,8 @@ int tables(const std::string& spec_path, const std::string& out_path, const std:
         O.put(nq);
         for (int t = 0; t < nt; ++t) O.arr(bt.tables_[t].values.data(), nq);
         for (int t = 0; t < nt; ++t) O.arr(dbt.tables_[t].values.data(), nq);
+        const auto& d2t = H.d2betaqTables(sp.z);
+        for (int t = 0; t < nt; ++t) O.arr(d2t.tables_[t].values.data(), nq);
     }
     std::fclose(f);
     return 0;

@@ -19,7 +19,7 @@ reference's own arithmetic:
 * ``private:`` sections of the β(q) table classes are opened so that the
   driver can export the raw tables the GPU path consumes.
 
-Usage: python oracle/refgen.py [REFERENCE_ROOT]
+Usage: python oracle/refgen.py REFERENCE_ROOT   (or EFFMASS_REFERENCE in the environment)
 """
 import os
 import re
@@ -126,7 +126,9 @@ def transform(path, text):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EFFMASS_REFERENCE", "")
+    if not ref or not os.path.isdir(os.path.join(ref, "src")):
+        raise SystemExit("refgen: give the reference checkout's root (argument or EFFMASS_REFERENCE)")
     os.makedirs(OUT_DIR, exist_ok=True)
     parts = ['// Generated by oracle/refgen.py from the reference sources. Do not commit.\n',
              '#include "../ref_shims.hpp"\n']

@@ -1,5 +1,7 @@
 import os
+import subprocess
 import sys
+import tempfile
 
 import numpy as np
 import pytest
@@ -46,3 +48,33 @@ def oracle_lib():
     from oracle import oracle as O
     O.build()
     return O
+
+
+def reference_golden(sysm, kps, psis):
+    """The reference's own golden record (oracle/_ref/ref_driver `golden` mode)
+    for the k-points kps with bands psis[i]: H|psi>, dH/dk|psi> and everything
+    the reference used.  Needs the reference build (oracle.build_ref())."""
+    from oracle import oracle as O
+    with tempfile.TemporaryDirectory() as td:
+        spec, gold = os.path.join(td, "spec.bin"), os.path.join(td, "gold.bin")
+        S.write_spec(spec, sysm, list(kps), list(psis))
+        subprocess.run([O.REF_DRIVER, "golden", spec, gold, os.path.join(td, "wd")], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, timeout=1200)
+        return S.read_golden(gold)
+
+
+def as_used(sysm, g, ik=0):
+    """System and k-point ik as the reference used them: its own beta/dbeta
+    tables and lambda (after its per-l diagonalisation), its G-sphere views.
+    Returns (System, KPoint, golden k-point record)."""
+    sp, gk = g["species"][0], g["kpts"][ik]
+    species = S.Species(z=6, proj_l=sp["proj_l"], lam=sp["lam"], dq=float(sp["dq"]), q_max=float(sp["q_max"]),
+                        beta_q=np.ascontiguousarray(sp["beta_q"]), dbeta_q=np.ascontiguousarray(sp["dbeta_q"]))
+    used = S.System(name=sysm.name, lattice=g["lattice"], omega=float(g["omega"]), n1=sysm.n1, n2=sysm.n2,
+                    n3=sysm.n3, v_loc=np.ascontiguousarray(sysm.v_loc), species=[species],
+                    atom_species=np.ascontiguousarray(sysm.atom_species),
+                    atom_z=np.full(len(sysm.atom_tau), 6, dtype=np.int32),
+                    atom_tau=np.ascontiguousarray(sysm.atom_tau), ecut=0.0)
+    kp = S.KPoint(npw=int(gk["g_idx"].shape[0]), k_frac=gk["k_frac"], g_idx=np.ascontiguousarray(gk["g_idx"]),
+                  kvec=np.ascontiguousarray(gk["kvec"]), kinetic=np.ascontiguousarray(gk["kinetic"]))
+    return used, kp, gk

@@ -45,7 +45,8 @@ CASES = {
 
 
 def read_tables(path):
-    """The first species of a TABREF01 file: mesh, rotated beta(r) and the tables."""
+    """The first species of a TABREF01 file: mesh, rotated beta(r) and the
+    reference's beta(q), dbeta/dq and d2beta/dq2 tables."""
     raw = open(path, "rb").read()
     assert raw[:8] == b"TABREF01"
     o = 8
@@ -74,8 +75,10 @@ def read_tables(path):
     nt, nq = ints(2)
     bq = dbl(nt * nq).reshape(nt, nq)
     dbq = dbl(nt * nq).reshape(nt, nq)
+    # D2BetaqTables (files written before the driver exported them end here)
+    d2bq = dbl(nt * nq).reshape(nt, nq) if len(raw) >= o + 8 * nt * nq else None
     return dict(uniform=int(mtype == 0), r=r, rab=rab, l=np.array(ls, dtype=np.int32), beta=betas,
-                beta_q=bq, dbeta_q=dbq)
+                beta_q=bq, dbeta_q=dbq, d2beta_q=d2bq)
 
 
 def make_case(name, sysname, kf, nb, grid):

@@ -1,10 +1,14 @@
 """Hessian d2H/dk_a dk_b |psi> (hpsi_hess_apply).  The reference's operator is
-an empty stub, so it is checked against what the reference does define:
+an empty stub, so it is checked against the oracle's restatement (oracle_hess,
+itself pinned in test_oracle_hessian.py) to 1e-12 in FP64, and against what the
+reference does define:
 
 * its radial tables: the Hessian tables F0 = beta/q^l and F1 = F0'/q, built on
   the device from the radial projectors the reference integrated, give back
   the reference's beta(q) and dbeta/dq tables (beta = F0 q^l,
-  beta' = F1 q^(l+1) + l F0 q^(l-1));
+  beta' = F1 q^(l+1) + l F0 q^(l-1)) and its D2BetaqTables
+  (beta'' = F3 q^(l+2) + (2l+1) F1 q^l + l(l-1) F0 q^(l-2), against the
+  oracle's restatement that is bit-identical to the reference's);
 * its gradient (pinned in test_gpu_parity.py): central differences of
   dH/dk_a |psi> at K +- h e_b (same G set) within 1e-6 relative;
 * the kinetic part alone (all lambda = 0): out_ab = delta_ab psi exactly;
@@ -46,6 +50,41 @@ def test_hessian_tables_reproduce_reference_beta_tables(built, case):
         assert np.abs(beta - z["sp_beta_q"][p]).max() <= 1e-12 * np.abs(z["sp_beta_q"][p]).max(), (p, l)
         sel = q > 0
         assert np.abs(dbeta[sel] - z["sp_dbeta_q"][p][sel]).max() <= 1e-11 * np.abs(z["sp_dbeta_q"][p]).max(), (p, l)
+
+
+@pytest.mark.parametrize("case", ["tinyd", "sc8"])
+def test_device_hessian_tables_match_oracle_and_reference_d2beta(built, oracle_lib, case):
+    from test_oracle_hessian import beta_from_f
+    z = np.load(os.path.join(GOLDEN, f"{case}.npz"))
+    f = _tables(z)
+    fo = oracle_lib.hess_tables(z["rad_r"], z["rad_rab"], bool(z["rad_uniform"]), z["rad_l"], z["rad_beta"],
+                                float(z["sp_dq"]), float(z["sp_q_max"]))
+    d2 = oracle_lib.d2beta_tables(z["rad_r"], z["rad_rab"], bool(z["rad_uniform"]), z["rad_l"], z["rad_beta"],
+                                  float(z["sp_dq"]), float(z["sp_q_max"]))
+    q = np.arange(f.shape[-1]) * float(z["sp_dq"])
+    for p, l in enumerate(z["rad_l"]):
+        for t in range(3):
+            assert np.abs(f[t, p] - fo[t, p]).max() <= 1e-13 * np.abs(fo[t, p]).max(), (p, t)
+        b2 = beta_from_f(f[:, p], int(l), q)[2]
+        sel = q > 0 if l >= 2 else np.ones_like(q, dtype=bool)
+        assert np.abs(b2[sel] - d2[p][sel]).max() <= 1e-12 * np.abs(d2[p]).max(), (p, l)
+
+
+@pytest.mark.parametrize("case,prec,tol", [("tinyd", "fp64", 1e-12), ("sc8", "fp64", 1e-12),
+                                           ("tinyd", "fp32", 1e-5), ("sc8", "fp32", 1e-5)])
+def test_hessian_matches_oracle(built, oracle_lib, case, prec, tol):
+    from effmass_gb300.hamiltonian import Hamiltonian
+    sysm, kp, psi, _, _ = load_case(case)
+    z = np.load(os.path.join(GOLDEN, f"{case}.npz"))
+    f = _tables(z)
+    ref = oracle_lib.hess(sysm, kp, psi, [f], float(z["sp_dq"]))
+    with Hamiltonian(sysm) as H:
+        H.set_hessian_tables(0, f, float(z["sp_dq"]))
+        H.set_kpoint(0, kp)
+        out = {n: np.zeros_like(psi) for n in NAMES}
+        H.hess_apply(0, psi.shape[0], psi, out, prec)
+    errs = {n: rel_err(out[n], ref[k]) for k, n in enumerate(NAMES)}
+    assert max(errs.values()) <= tol, (case, prec, errs)
 
 
 def _shifted(kp, lattice, dK):

@@ -3,9 +3,11 @@
 Tolerances (relative, in the 2-norm over all bands and G):
   FP64 path  vs the reference's own outputs (golden fixtures):  1e-12
   FP32 path  vs the reference's own outputs:                   1e-6
-At the full 64-atom size, where the oracle is too slow for a test, the FP32
-path is checked against the FP64 GPU path (1e-6) and size-independent
-properties are checked (Hermiticity of <psi_m|H|psi_n>, linearity).
+The 64-atom cell itself is pinned to the reference in
+test_gpu_reference_c1.py (4 bands per k-point).  Here, at 64-atom sizes that
+need many bands (band chunks, 320 bands), the FP32 path is checked against
+the FP64 GPU path (1e-6) and size-independent properties are checked
+(Hermiticity of <psi_m|H|psi_n>, linearity).
 """
 import ctypes as C
 

@@ -11,7 +11,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import as_used, reference_golden, rel_err
 from effmass_gb300 import system as S
 from oracle import oracle as O
 
@@ -20,12 +20,7 @@ pytestmark = pytest.mark.skipif(not os.path.exists(O.REF_DRIVER), reason="refere
 
 def _reference(sysm, kp, psi):
     """The reference's golden record for one k-point and its bands."""
-    with tempfile.TemporaryDirectory() as td:
-        spec, gold = os.path.join(td, "spec.bin"), os.path.join(td, "gold.bin")
-        S.write_spec(spec, sysm, [kp], [psi])
-        subprocess.run([O.REF_DRIVER, "golden", spec, gold, os.path.join(td, "wd")], check=True,
-                       stderr=subprocess.DEVNULL, timeout=600)
-        return S.read_golden(gold)
+    return reference_golden(sysm, [kp], [psi])
 
 
 def _reference_density(sysm, kp, psi, occ):
@@ -43,22 +38,6 @@ def _reference_density(sysm, kp, psi, occ):
     return np.frombuffer(raw[20:], dtype=np.float64).copy()
 
 
-def _as_used(sysm, g):
-    """System and k-point as the reference used them: its own beta/dbeta tables
-    and lambda (after its per-l diagonalisation), its G-sphere views."""
-    sp, gk = g["species"][0], g["kpts"][0]
-    species = S.Species(z=6, proj_l=sp["proj_l"], lam=sp["lam"], dq=float(sp["dq"]), q_max=float(sp["q_max"]),
-                        beta_q=np.ascontiguousarray(sp["beta_q"]), dbeta_q=np.ascontiguousarray(sp["dbeta_q"]))
-    used = S.System(name=sysm.name, lattice=g["lattice"], omega=float(g["omega"]), n1=sysm.n1, n2=sysm.n2,
-                    n3=sysm.n3, v_loc=np.ascontiguousarray(sysm.v_loc), species=[species],
-                    atom_species=np.ascontiguousarray(sysm.atom_species),
-                    atom_z=np.full(len(sysm.atom_tau), 6, dtype=np.int32),
-                    atom_tau=np.ascontiguousarray(sysm.atom_tau), ecut=0.0)
-    kp = S.KPoint(npw=int(gk["g_idx"].shape[0]), k_frac=gk["k_frac"], g_idx=np.ascontiguousarray(gk["g_idx"]),
-                  kvec=np.ascontiguousarray(gk["kvec"]), kinetic=np.ascontiguousarray(gk["kinetic"]))
-    return used, kp, gk
-
-
 @pytest.mark.parametrize("name,k_frac,grid,seed", [
     ("tinyd", (0.37, -0.11, 0.05), None, 101),       # s+p+d, non-cubic 15x16x18, general k
     ("tiny", (-0.2, 0.3, 0.45), (5, 6, 7), 202),     # prime grid lengths 5 and 7
@@ -71,7 +50,7 @@ def test_oracle_matches_live_reference(name, k_frac, grid, seed):
         sysm.v_loc = S.local_potential(sysm.lattice, sysm.atom_tau, *grid)
     kp = S.g_sphere(sysm.lattice, k_frac, sysm.ecut)
     psi = S.make_bands(kp, 3, seed=seed)
-    used, kp_used, gk = _as_used(sysm, _reference(sysm, kp, psi))
+    used, kp_used, gk = as_used(sysm, _reference(sysm, kp, psi))
     assert np.array_equal(kp_used.g_idx, kp.g_idx)  # the reference read the G-sphere in the order written
     h = O.hpsi(used, kp_used, psi)
     assert rel_err(h, gk["hpsi"]) <= 1e-14
@@ -105,3 +84,14 @@ def test_oracle_beta_tables_match_live_reference(name, dr, r_max):
     bq, dbq = O.beta_tables(rad["r"], rad["rab"], bool(rad["uniform"]), rad["l"], rad["beta"], 0.01, 20.0)
     assert bq.shape == rad["beta_q"].shape
     assert np.array_equal(bq, rad["beta_q"]) and np.array_equal(dbq, rad["dbeta_q"])
+    # D2BetaqTables (src/pseudo/ncpp_advance.cppm:908-1085), which the Hessian
+    # needs: bit for bit, and rebuilt from the Hessian's F0, F1, F3 tables
+    d2 = O.d2beta_tables(rad["r"], rad["rab"], bool(rad["uniform"]), rad["l"], rad["beta"], 0.01, 20.0)
+    assert np.array_equal(d2, rad["d2beta_q"])
+    from test_oracle_hessian import beta_from_f
+    f = O.hess_tables(rad["r"], rad["rab"], bool(rad["uniform"]), rad["l"], rad["beta"], 0.01, 20.0)
+    q = np.arange(f.shape[-1]) * 0.01
+    for p, l in enumerate(rad["l"]):
+        b2 = beta_from_f(f[:, p], int(l), q)[2]
+        sel = q > 0 if l >= 2 else np.ones_like(q, dtype=bool)
+        assert np.abs(b2[sel] - d2[p][sel]).max() <= 1e-12 * np.abs(d2[p]).max(), (p, l)

@@ -7,9 +7,15 @@ Its scratch is a 32 MiB static device array instead of the context's
 workspace.  This test calls it through the C ABI, twice in a row (the array
 keeps the previous call's contents), and compares each result with the
 existing entry point hpsi_apply on the same inputs: within 1e-12 (FP64) and
-1e-6 (FP32) relative, the tolerances of the other parity tests.  It also
-checks the refusals: host pointers, projector matrices not yet built, and a
-band whose FFT planes do not fit the scratch.
+1e-6 (FP32) relative, the tolerances of the other parity tests.  One case
+(1001 bands of the 64-atom cell in FP64, on a stream of its own) needs more
+partial sums than the scratch holds, so its nonlocal term runs in chunks of
+251 bands with a last chunk of 248.  It also checks the refusals: the
+tensor-core precisions, host pointers, projector matrices not yet built, and
+a band whose FFT planes do not fit the scratch, which is refused before any
+launch with hpsi left as it was.  (A refusal on the partial sums alone would
+need more than a million projectors per band; the same up-front check covers
+it.)
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test.
@@ -26,7 +32,7 @@ pytestmark = pytest.mark.gpu
 TOL = {"fp64": 1e-12, "fp32": 1e-6}
 
 
-def _noalloc(H, kid, nb, psi_d, hpsi_d, prec, sync=True):
+def _noalloc(H, kid, nb, psi_d, hpsi_d, prec, sync=True, stream=None):
     import torch
     from effmass_gb300._lib import load
     lib = load()
@@ -34,8 +40,9 @@ def _noalloc(H, kid, nb, psi_d, hpsi_d, prec, sync=True):
     fn.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     fn.restype = C.c_int
     flags = abi.PRECISIONS[prec] | abi.HPSI_DEVICE_PTRS | (abi.HPSI_SYNC if sync else 0)
-    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    return fn(H.ctx, kid, nb, C.c_void_p(psi_d.data_ptr()), C.c_void_p(hpsi_d.data_ptr()), flags, stream)
+    st = stream if stream is not None else torch.cuda.current_stream()
+    return fn(H.ctx, kid, nb, C.c_void_p(psi_d.data_ptr()), C.c_void_p(hpsi_d.data_ptr()), flags,
+              C.c_void_p(st.cuda_stream))
 
 
 def _rel(a, b):
@@ -66,6 +73,34 @@ def test_noalloc_matches_hpsi_apply_twice(name, nb):
                 assert err <= TOL[prec], (name, prec, call, err)
 
 
+def test_noalloc_chunked_partial_sums_on_own_stream():
+    """1001 bands of the 64-atom cell (1152 projectors) in FP64: the partial
+    sums of all bands exceed the scratch, so the nonlocal term runs in chunks
+    of 251 bands and a last chunk of 248, on a non-default stream."""
+    torch = pytest.importorskip("torch")
+    from effmass_gb300 import build, system as S
+    from effmass_gb300.hamiltonian import Hamiltonian
+    build.build()
+    sysm = S.make_system("sc64")
+    kp = S.g_sphere(sysm.lattice, S.default_kpoint("sc64"), sysm.ecut)
+    nb = 1001
+    psi = torch.from_numpy(S.make_bands(kp, 8, seed=29)).cuda().repeat(126, 1)[:nb].contiguous()
+    psi *= torch.linspace(0.5, 1.5, nb, dtype=torch.float64, device="cuda")[:, None]
+    with Hamiltonian(sysm) as H:
+        H.set_kpoint(0, kp)
+        ref = torch.zeros_like(psi)
+        H.apply(0, nb, psi, ref, "fp64")
+        torch.cuda.synchronize()
+        side = torch.cuda.Stream()
+        for call in range(2):
+            out = torch.zeros_like(psi)
+            torch.cuda.synchronize()
+            st = _noalloc(H, 0, nb, psi, out, "fp64", stream=side)
+            assert st == 0, (call, st)
+            err = _rel(out, ref)
+            assert err <= TOL["fp64"], (call, err)
+
+
 def test_noalloc_refusals():
     torch = pytest.importorskip("torch")
     from effmass_gb300 import build, system as S
@@ -79,6 +114,9 @@ def test_noalloc_refusals():
         H.set_kpoint(0, kp)
         # projector matrices of fp32 not built yet on this k-point
         assert _noalloc(H, 0, 2, psi, out, "fp32") == abi.HPSI_ERR_STATE
+        # the tensor-core precisions are not offered
+        for prec in ("tc", "tc_bf16"):
+            assert _noalloc(H, 0, 2, psi, out, prec) == abi.HPSI_ERR_BAD_ARG
         # host pointers are refused
         from effmass_gb300._lib import load
         lib = load()
@@ -109,10 +147,13 @@ def test_noalloc_rejects_planes_beyond_scratch():
     kp = S.KPoint(npw=int(sel.sum()), k_frac=np.zeros(3), g_idx=np.ascontiguousarray(g[sel], dtype=np.int32),
                   kvec=np.ascontiguousarray(K[sel]), kinetic=np.ascontiguousarray(kin[sel]))
     assert len(np.unique(kp.g_idx[:, 0])) * 80 * 80 * 16 > abi.HPSI_NOALLOC_SCRATCH_BYTES
-    psi = torch.zeros((1, kp.npw), dtype=torch.complex128, device="cuda")
-    out = torch.zeros_like(psi)
+    psi = torch.ones((1, kp.npw), dtype=torch.complex128, device="cuda")
+    before = torch.arange(kp.npw, dtype=torch.float64, device="cuda").to(torch.complex128)[None, :]
+    out = before.clone()
     with Hamiltonian(sysm) as H:
         H.set_kpoint(0, kp)
         assert _noalloc(H, 0, 1, psi, out, "fp64") == abi.HPSI_ERR_BAD_ARG
         from effmass_gb300._lib import load
         assert b"scratch" in load().hpsi_last_error(H.ctx)
+        torch.cuda.synchronize()
+        assert torch.equal(out, before)  # refused before any launch
