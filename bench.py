@@ -41,10 +41,12 @@ def parse():
     ap.add_argument("--nb", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--serving-requests", type=int, default=600,
+    ap.add_argument("--serving-requests", type=int, default=10000,
                     help="requests of the served Poisson stream (0 skips serving)")
     ap.add_argument("--serving-rate", type=float, default=200.0)
-    ap.add_argument("--serving-lanes", type=int, default=4)
+    ap.add_argument("--serving-lanes", type=int, default=8)
+    ap.add_argument("--serving-sweep", type=float, nargs="*", default=[250.0, 300.0, 350.0, 400.0, 500.0],
+                    help="rates (req/s) of the capacity sweep after the main stream")
     ap.add_argument("--no-sternheimer", action="store_true",
                     help="skip the Sternheimer dpsi/dk solve (2-atom fcc cell, 4 occupied bands, x/y/z)")
     ap.add_argument("--no-kp", action="store_true",
@@ -428,48 +430,12 @@ def run_gb300(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
-def run_serving(args, H_sc64, kp_sc64):
-    """Served stream: Poisson arrivals of requests mixing the 2-, 8- and 64-atom
-    cells (6:3:1), each 1-16 k-points x 8-128 bands of H|psi> plus the velocity
-    matrix, through the library's serving loop.  Returns the summary dict."""
-    import threading
+def _serving_stream(rng, n, rate, pools):
+    """n seeded requests of the served mix: Poisson arrivals at `rate` req/s,
+    cells 6:3:1 (2-, 8-, 64-atom), 1-16 k-points drawn from the cell's pool,
+    8-128 bands."""
     import numpy as np
-    import torch
-    from effmass_gb300 import system as S
-    from effmass_gb300.hamiltonian import Hamiltonian
-    from effmass_gb300.serving import Job, Server, pinned_empty
-
-    rng = np.random.default_rng(2024)
-    pools = []
-    # the 64-atom cell (already resident: Gamma), the 8-atom cell on a 4^3 MP
-    # grid (16 of its k-points bound) and the 2-atom cell on 6^3 (16 bound)
-    made = []
-    for name, grid, nk in (("fcc2", 6, 16), ("sc8", 4, 16)):
-        sysm = S.make_system(name)
-        H = Hamiltonian(sysm)
-        kpts = S.mp_grid(grid)[:nk]
-        kps = []
-        for i, k in enumerate(kpts):
-            kp = S.g_sphere(sysm.lattice, k, sysm.ecut)
-            H.set_kpoint(i, kp)
-            kps.append(kp)
-        made.append(H)
-        pools.append((H, kps))
-    pools.append((H_sc64, [kp_sc64]))
-    hams = [p[0] for p in pools]
-    # pinned inputs (128 bands per bound k-point) and shared output buffers
-    bufs = []
-    for H, kps in pools:
-        ins, outs, vels = [], [], []
-        for kp in kps:
-            a = pinned_empty((128, kp.npw))
-            a[...] = S.make_bands(kp, 128, seed=int(rng.integers(1 << 30)))
-            ins.append(a)
-            outs.append(pinned_empty((128, kp.npw)))
-            vels.append(pinned_empty((3 * 128 * 128,)))
-        bufs.append((ins, outs, vels))
-    n = args.serving_requests
-    arrivals = np.cumsum(rng.exponential(1.0 / args.serving_rate, size=n))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
     kinds = rng.choice(3, size=n, p=[0.6, 0.3, 0.1])
     plans = []
     for i in range(n):
@@ -478,51 +444,150 @@ def run_serving(args, H_sc64, kp_sc64):
         ks = rng.integers(0, len(pools[si][1]), size=nkr)
         nb = int(rng.integers(8, 129))
         plans.append((si, [int(k) for k in ks], nb))
-    band_apps = sum(len(p[1]) * p[2] for p in plans)
-    with Server(hams, lanes=args.serving_lanes, budget_gb=48, precision=args.prec) as srv:
-        # warm-up: one request per system
+    return arrivals, kinds, plans
+
+
+def _serve(srv, bufs, pools, arrivals, plans):
+    """Submit the stream on its arrival times from a thread, wait for every
+    request; returns (per-request times, wall seconds)."""
+    import threading
+    from effmass_gb300.serving import Job
+    n = len(plans)
+    tickets = [None] * n
+    t0 = time.perf_counter()
+
+    def submitter():
+        for i, (si, ks, nb) in enumerate(plans):
+            delay = t0 + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ins, outs, vels = bufs[si]
+            jobs = []
+            for k in ks:
+                npw = pools[si][1][k].npw
+                jobs.append(Job(si, k, ins[: nb * npw].reshape(nb, npw), outs[: nb * npw].reshape(nb, npw),
+                                vels[: 3 * nb * nb].reshape(3, nb, nb)))
+            tickets[i] = srv.submit(jobs)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    times = []
+    for i in range(n):
+        while tickets[i] is None:
+            time.sleep(0.0002)
+        times.append(srv.wait(tickets[i]))
+    th.join()
+    return times, time.perf_counter() - t0
+
+
+def run_serving(args, H_sc64, kp_sc64):
+    """Served stream (the C4 workload): Poisson arrivals at --serving-rate of
+    --serving-requests requests mixing the 2-, 8- and 64-atom cells (6:3:1),
+    each 1-16 k-points x 8-128 bands of H|psi> plus the velocity matrix, over
+    the full k-point pools (the 216 k-points of the fcc cell's 6^3
+    Monkhorst-Pack grid, the 64 of the 8-atom cell's 4^3 grid, 4 k-points of
+    the 64-atom cell), through the library's serving loop.  Then a capacity
+    sweep: the same mix at higher rates; the capacity is the highest rate whose
+    completed throughput keeps up with the offered one (>= 95%) with p99 below
+    250 ms.  Returns the summary dict."""
+    import numpy as np
+    from effmass_gb300 import system as S
+    from effmass_gb300.hamiltonian import Hamiltonian
+    from effmass_gb300.serving import Job, Server, pinned_empty
+
+    rng = np.random.default_rng(2024)
+    pools = []
+    made = []
+    for name, grid in (("fcc2", 6), ("sc8", 4)):
+        sysm = S.make_system(name)
+        H = Hamiltonian(sysm)
+        kps = []
+        for i, k in enumerate(S.mp_grid(grid)):
+            kp = S.g_sphere(sysm.lattice, k, sysm.ecut)
+            H.set_kpoint(i, kp)
+            kps.append(kp)
+        made.append(H)
+        pools.append((H, kps))
+    # the 64-atom cell: Gamma (slot 0, already bound) and three more k-points
+    sc64_k = [kp_sc64]
+    sysm64 = S.make_system("sc64")
+    for i, k in enumerate([(0.01, 0.0, 0.0), (0.0, 0.01, 0.0), (0.0, 0.0, 0.01)]):
+        kp = S.g_sphere(sysm64.lattice, k, sysm64.ecut)
+        H_sc64.set_kpoint(1 + i, kp)
+        sc64_k.append(kp)
+    pools.append((H_sc64, sc64_k))
+    hams = [p[0] for p in pools]
+    # pinned host buffers per cell (128 bands of its largest sphere), shared by
+    # all requests of the cell: the stream measures time, not results
+    bufs = []
+    for H, kps in pools:
+        npw_max = max(kp.npw for kp in kps)
+        ins = pinned_empty((128 * npw_max,))
+        ins[:] = 0.0
+        ins[: 128 * kps[0].npw] = S.make_bands(kps[0], 128, seed=int(rng.integers(1 << 30))).ravel()
+        bufs.append((ins, pinned_empty((128 * npw_max,)), pinned_empty((3 * 128 * 128,))))
+    cfg = dict(lanes=args.serving_lanes, budget_gb=64, precision=args.prec, merge_max_bands=1024, bypass_ms=20.0)
+
+    def summary(times, kinds, plans, wall, rate, last_arrival_s):
+        tot = np.array([t["total_ms"] for t in times])
+        que = np.array([t["queue_ms"] for t in times])
+        band_apps = sum(len(p[1]) * p[2] for p in plans)
+        by_kind = {}
+        for name, kd in (("fcc2", 0), ("sc8", 1), ("sc64", 2)):
+            sel = tot[kinds == kd]
+            if sel.size:
+                by_kind[name] = {"requests": int(sel.size), "p50_ms": float(np.percentile(sel, 50)),
+                                 "p99_ms": float(np.percentile(sel, 99))}
+        offered = len(plans) / last_arrival_s
+        return {"requests": len(plans), "rate_req_per_s": rate, "band_apps": int(band_apps), "wall_s": wall,
+                "throughput_band_apps_per_s": band_apps / wall, "throughput_req_per_s": len(plans) / wall,
+                "offered_req_per_s": offered, "p50_ms": float(np.percentile(tot, 50)),
+                "p99_ms": float(np.percentile(tot, 99)), "max_ms": float(tot.max()),
+                "mean_queue_ms": float(que.mean()), "by_cell": by_kind}
+
+    with Server(hams, **cfg) as srv:
+        # warm-up: a few requests per system
         for si in range(3):
             ins, outs, vels = bufs[si]
-            srv.wait(srv.submit([Job(si, 0, ins[0][:8], outs[0][:8], vels[0][: 3 * 64].reshape(3, 8, 8))]))
-        tickets = [None] * n
-        t0 = time.perf_counter()
-
-        def submitter():
-            for i, (si, ks, nb) in enumerate(plans):
-                delay = t0 + arrivals[i] - time.perf_counter()
-                if delay > 0:
-                    time.sleep(delay)
-                ins, outs, vels = bufs[si]
-                jobs = [Job(si, k, ins[k][:nb], outs[k][:nb], vels[k][: 3 * nb * nb].reshape(3, nb, nb)) for k in ks]
-                tickets[i] = srv.submit(jobs)
-
-        th = threading.Thread(target=submitter)
-        th.start()
-        times = []
-        for i in range(n):
-            while tickets[i] is None:
-                time.sleep(0.0005)
-            times.append(srv.wait(tickets[i]))
-        th.join()
-        wall = time.perf_counter() - t0
+            npw = pools[si][1][0].npw
+            for _ in range(3):
+                srv.wait(srv.submit([Job(si, 0, ins[: 8 * npw].reshape(8, npw), outs[: 8 * npw].reshape(8, npw),
+                                         vels[: 3 * 64].reshape(3, 8, 8))]))
+        n = args.serving_requests
+        arrivals, kinds, plans = _serving_stream(rng, n, args.serving_rate, pools)
+        times, wall = _serve(srv, bufs, pools, arrivals, plans)
+        out = summary(times, kinds, plans, wall, args.serving_rate, float(arrivals[-1]))
         st = srv.stats()
+        out.update({"lanes": args.serving_lanes, "precision": args.prec, "merge_max_bands": cfg["merge_max_bands"],
+                    "bypass_ms": cfg["bypass_ms"], "units": st["units"], "merged_units": st["merged_units"],
+                    "merged_jobs": st["merged_jobs"], "peak_device_bytes": st["peak_bytes"],
+                    "mix": "2-, 8-, 64-atom cells 6:3:1; 1-16 k-points (pools of 216/64/4) x 8-128 bands; "
+                           "H|psi> + velocity matrix"})
+        # capacity sweep: the same mix at higher rates, fewer requests each
+        sweep = []
+        capacity = args.serving_rate if (out["throughput_req_per_s"] >= 0.95 * out["offered_req_per_s"]
+                                         and out["p99_ms"] < 250.0) else None
+        for rate in args.serving_sweep:
+            if rate <= args.serving_rate:
+                continue
+            m = max(200, min(n, int(rate * 8)))
+            a2, k2, p2 = _serving_stream(rng, m, rate, pools)
+            t2, w2 = _serve(srv, bufs, pools, a2, p2)
+            s2 = summary(t2, k2, p2, w2, rate, float(a2[-1]))
+            keeps_up = s2["throughput_req_per_s"] >= 0.95 * s2["offered_req_per_s"] and s2["p99_ms"] < 250.0
+            sweep.append({k: s2[k] for k in ("rate_req_per_s", "requests", "throughput_req_per_s",
+                                             "throughput_band_apps_per_s", "p50_ms", "p99_ms")} |
+                         {"keeps_up": keeps_up})
+            if keeps_up:
+                capacity = rate
+            else:
+                break
+        out["capacity_sweep"] = sweep
+        out["capacity_req_per_s"] = capacity
+        out["capacity_rule"] = "highest swept rate with completed >= 95% of offered req/s and p99 < 250 ms"
     for H in made:
         H.close()
-    tot = np.array([t["total_ms"] for t in times])
-    que = np.array([t["queue_ms"] for t in times])
-    by_kind = {}
-    for name, kd in (("fcc2", 0), ("sc8", 1), ("sc64", 2)):
-        sel = tot[kinds == kd]
-        if sel.size:
-            by_kind[name] = {"requests": int(sel.size), "p50_ms": float(np.percentile(sel, 50)),
-                             "p99_ms": float(np.percentile(sel, 99))}
-    return {"requests": n, "rate_req_per_s": args.serving_rate, "lanes": args.serving_lanes,
-            "precision": args.prec, "band_apps": int(band_apps), "wall_s": wall,
-            "throughput_band_apps_per_s": band_apps / wall, "throughput_req_per_s": n / wall,
-            "p50_ms": float(np.percentile(tot, 50)), "p99_ms": float(np.percentile(tot, 99)),
-            "max_ms": float(tot.max()), "mean_queue_ms": float(que.mean()), "by_cell": by_kind,
-            "peak_device_bytes": st["peak_bytes"],
-            "mix": "2-, 8-, 64-atom cells 6:3:1; 1-16 k-points (16/16/1 bound) x 8-128 bands; H|psi> + velocity"}
+    return out
 
 
 def batched_cells():

@@ -2030,13 +2030,23 @@ extern "C" int hpsi_apply_noalloc(hpsi_ctx* c, int kid, int nb, const double* ps
 // The systems (contexts) keep V_loc, the projector tables and the projector
 // matrices of their bound k-points resident in HBM.  Clients submit requests
 // (each a list of k-point jobs: psi in, hpsi accumulated, optional velocity
-// matrix) from any thread.  One scheduler thread admits requests in arrival
-// order whenever a lane (CUDA stream) is free and the request's buffers fit in
-// the device arena (the HBM budget), queues its copies and kernels on that
-// lane's stream, and retires it when the lane's completion event fires —
-// so requests that arrive while others run are admitted as soon as a slot and
-// memory free up, and the work of different requests overlaps on the device.
-// All CUDA calls are issued from the scheduler thread.
+// matrix) from any thread.  The scheduler works on jobs, not requests: every
+// job of a request enters one pending queue in arrival order, and one
+// scheduler thread admits jobs whenever a lane (CUDA stream) is free and the
+// job's buffers fit in the device arena (the HBM budget).  A request is
+// retired when its last job's lane event fires.
+//   * Arrival order, with bounded overtaking: a later job that fits may start
+//     before an older one that does not, while the oldest pending job has
+//     waited less than bypass_ms; after that only the oldest may start.
+//   * Merging: jobs of a cell with few projectors (P <= 256) — the small cells
+//     whose work is a handful of short launches — are gathered from the
+//     pending queue (up to merge_max_bands bands of one cell) into one unit:
+//     one ragged local-term launch set over all their bands (the batched
+//     plans' item tables) and one ragged projection / expansion pair, instead
+//     of a launch sequence per job.
+// So requests that arrive while others run are admitted as lanes and memory
+// free up, and the work of different requests overlaps on the device.  All
+// CUDA calls are issued from the scheduler thread.
 // ===========================================================================
 #include <atomic>
 #include <chrono>
@@ -2093,12 +2103,32 @@ struct Arena {
 struct SrvReq {
     long long ticket = 0;
     std::vector<hpsi_job> jobs;
-    size_t bytes = 0, off = 0;
-    int lane = -1;
+    int remaining = 0;  // jobs not yet retired
     int status = HPSI_OK;
-    double t_submit = 0, t_admit = 0, t_done = 0;
+    double t_submit = 0, t_admit = -1, t_done = 0;
     bool done = false;
     std::string err;
+};
+
+// one k-point job of a request
+struct SrvTask {
+    SrvReq* req = nullptr;
+    int job = 0;
+    size_t bytes = 0;  // arena bytes when it runs on its own
+};
+
+// what one lane runs: one job, or several merged jobs of one cell
+struct SrvUnit {
+    std::vector<SrvTask> tasks;
+    bool merged = false;
+    size_t bytes = 0, off = 0;
+};
+
+// Ragged work of a merged unit: offsets in its arena block and launch choices
+struct MergePlan {
+    size_t o_psi = 0, o_hpsi = 0, o_m = 0, o_T = 0, o_part = 0, o_W = 0, o_li = 0, o_bi = 0, o_xb = 0, o_gi = 0,
+           o_ws = 0, bytes = 0;
+    int nbands = 0, nb_max = 0, npw_max = 0, max_nxs = 0, nsplit = 1, P = 0, nxblk = 0;
 };
 
 }  // namespace
@@ -2107,20 +2137,22 @@ struct hpsi_server {
     std::vector<hpsi_ctx*> sys;
     int prec = HPSI_PREC_TC;
     int dev = 0;
+    int merge_max_bands = 0;
+    double bypass_ms = 0.0;
     unsigned char* arena_mem = nullptr;
     Arena arena;
     std::vector<cudaStream_t> lanes;
     std::vector<cudaEvent_t> lane_ev;
-    std::vector<SrvReq*> lane_req;
+    std::vector<SrvUnit*> lane_unit;
     std::mutex mu;
     std::condition_variable cv_done, cv_work;
-    std::deque<SrvReq*> queue;
+    std::deque<SrvTask> pending;
     std::map<long long, SrvReq*> reqs;
     long long next_ticket = 1;
     bool stop = false;
     std::thread th;
     size_t peak_in_use = 0;
-    long long completed = 0;
+    long long completed = 0, units = 0, merged_units = 0, merged_jobs = 0;
     std::string err;
 };
 
@@ -2131,75 +2163,291 @@ static int srv_fail(hpsi_server* s, int code, const std::string& m)
     return code;
 }
 
-// device bytes a request holds while it runs
-static int srv_request_bytes(hpsi_server* S, const std::vector<hpsi_job>& jobs, size_t* bytes, std::string* why)
+static constexpr int kMergeMaxP = 256;  // cells with at most this many projectors merge
+
+static bool srv_mergeable(const hpsi_server* S, const hpsi_job& j)
 {
-    size_t psi_max = 0, m_max = 0, ws_max = 0;
-    for (const hpsi_job& j : jobs) {
-        if (j.system < 0 || j.system >= (int)S->sys.size()) { *why = "job system index out of range"; return HPSI_ERR_BAD_ARG; }
-        hpsi_ctx* c = S->sys[j.system];
-        auto it = c->slots.find(j.kid);
-        if (it == c->slots.end() || !it->second.valid) { *why = "job k-point slot not bound"; return HPSI_ERR_STATE; }
-        if (j.nb < 0 || (j.nb > 0 && (!j.psi || !j.hpsi))) { *why = "job psi/hpsi NULL or nb < 0"; return HPSI_ERR_BAD_ARG; }
-        const KSlot& s = it->second;
-        const size_t nel = (size_t)j.nb * s.npw;
-        psi_max = std::max(psi_max, nel * sizeof(double2));
-        ws_max = std::max(ws_max, apply_ws_bytes(c, s, j.nb, S->prec));
-        if (j.vel) {
-            m_max = std::max(m_max, (size_t)3 * j.nb * j.nb * sizeof(double2));
-            ws_max = std::max(ws_max, vel_ws_bytes(s, j.nb, S->prec));
-        }
+    if (S->merge_max_bands <= 0) return false;
+    const hpsi_ctx* c = S->sys[j.system];
+    auto it = c->slots.find(j.kid);
+    return it != c->slots.end() && it->second.P <= kMergeMaxP && it->second.npw > 0 && j.nb > 0 &&
+           j.nb <= S->merge_max_bands;
+}
+
+// device bytes of one job run on its own
+static int srv_job_bytes(hpsi_server* S, const hpsi_job& j, size_t* bytes, std::string* why)
+{
+    if (j.system < 0 || j.system >= (int)S->sys.size()) { *why = "job system index out of range"; return HPSI_ERR_BAD_ARG; }
+    hpsi_ctx* c = S->sys[j.system];
+    auto it = c->slots.find(j.kid);
+    if (it == c->slots.end() || !it->second.valid) { *why = "job k-point slot not bound"; return HPSI_ERR_STATE; }
+    if (j.nb < 0 || (j.nb > 0 && (!j.psi || !j.hpsi))) { *why = "job psi/hpsi NULL or nb < 0"; return HPSI_ERR_BAD_ARG; }
+    const KSlot& s = it->second;
+    const size_t nel = (size_t)j.nb * s.npw;
+    size_t ws = apply_ws_bytes(c, s, j.nb, S->prec), m = 0;
+    if (j.vel) {
+        m = (size_t)3 * j.nb * j.nb * sizeof(double2);
+        ws = std::max(ws, vel_ws_bytes(s, j.nb, S->prec));
     }
     Carver cv;
-    cv.take<unsigned char>(psi_max);
-    cv.take<unsigned char>(psi_max);
-    cv.take<unsigned char>(m_max);
-    cv.take<unsigned char>(ws_max);
+    cv.take<double2>(nel);
+    cv.take<double2>(nel);
+    cv.take<unsigned char>(m);
+    cv.take<unsigned char>(ws);
     *bytes = cv.off;
     return HPSI_OK;
 }
 
-// queue a request's work on its lane (scheduler thread)
-static int srv_issue(hpsi_server* S, SrvReq* r)
+static size_t srv_csize(const hpsi_server* S) { return S->prec == HPSI_PREC_FP64 ? sizeof(double2) : sizeof(float2); }
+
+// layout of a merged unit of jobs of one cell
+static MergePlan srv_merge_plan(const hpsi_server* S, const std::vector<SrvTask>& tasks)
 {
-    cudaStream_t st = S->lanes[r->lane];
-    size_t psi_max = 0, m_max = 0;
-    for (const hpsi_job& j : r->jobs) {
-        const KSlot& s = S->sys[j.system]->slots[j.kid];
-        psi_max = std::max(psi_max, (size_t)j.nb * s.npw * sizeof(double2));
-        if (j.vel) m_max = std::max(m_max, (size_t)3 * j.nb * j.nb * sizeof(double2));
+    MergePlan m;
+    const hpsi_ctx* c = S->sys[tasks[0].req->jobs[tasks[0].job].system];
+    const size_t cs = srv_csize(S);
+    size_t nel = 0, t_el = 0, vel_m = 0, vel_ws = 0;
+    for (const SrvTask& t : tasks) {
+        const hpsi_job& j = t.req->jobs[t.job];
+        const KSlot& s = c->slots.at(j.kid);
+        nel += (size_t)j.nb * s.npw;
+        t_el += (size_t)j.nb * s.nxs * c->n2 * c->n3;
+        m.nbands += j.nb;
+        m.nb_max = std::max(m.nb_max, j.nb);
+        m.npw_max = std::max(m.npw_max, s.npw);
+        m.max_nxs = std::max(m.max_nxs, s.nxs);
+        m.P = s.P;
+        if (j.vel) {
+            vel_m = std::max(vel_m, (size_t)3 * j.nb * j.nb * sizeof(double2));
+            vel_ws = std::max(vel_ws, vel_ws_bytes(s, j.nb, S->prec));
+        }
     }
+    // split count of the ragged projection: enough blocks for the SMs, K >= 128 per split
+    const long blocks = (long)tasks.size() * ceil_div(std::max(m.P, 1), 32) * ceil_div(std::max(m.nb_max, 1), 64);
+    while (m.nsplit < 32 && blocks * m.nsplit < 2 * 152 && m.npw_max / (2 * m.nsplit) >= 64) m.nsplit *= 2;
+    m.nxblk = m.nbands;  // upper bound: one x-pass band block per band
     Carver cv;
-    unsigned char* base = S->arena_mem + r->off;
-    double2* psi = reinterpret_cast<double2*>(base + cv.take<unsigned char>(psi_max));
-    double2* hpsi = reinterpret_cast<double2*>(base + cv.take<unsigned char>(psi_max));
-    double2* m = reinterpret_cast<double2*>(base + cv.take<unsigned char>(m_max));
-    unsigned char* ws = base + cv.take<unsigned char>(0);
-    for (const hpsi_job& j : r->jobs) {
-        if (j.nb == 0) continue;
-        hpsi_ctx* c = S->sys[j.system];
-        KSlot& s = c->slots[j.kid];
-        const size_t nel = (size_t)j.nb * s.npw;
-        if (s.npw == 0) continue;
-        cudaError_t e;
-        if ((e = cudaMemcpyAsync(psi, j.psi, nel * sizeof(double2), cudaMemcpyHostToDevice, st)) ||
-            (e = cudaMemcpyAsync(hpsi, j.hpsi, nel * sizeof(double2), cudaMemcpyHostToDevice, st))) {
-            r->err = cudaGetErrorString(e);
-            return HPSI_ERR_CUDA;
-        }
-        int rc = apply_dev(c, s, j.nb, psi, hpsi, S->prec, ws, st, nullptr, nullptr, false);
-        if (!rc && j.vel) rc = velocity_dev(c, s, j.nb, psi, m, S->prec, ws, st);
-        if (rc) { r->err = c->err; return rc; }
-        if ((e = cudaMemcpyAsync(j.hpsi, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st))) {
-            r->err = cudaGetErrorString(e);
-            return HPSI_ERR_CUDA;
-        }
-        if (j.vel && (e = cudaMemcpyAsync(j.vel, m, (size_t)3 * j.nb * j.nb * sizeof(double2), cudaMemcpyDeviceToHost, st))) {
-            r->err = cudaGetErrorString(e);
-            return HPSI_ERR_CUDA;
-        }
+    m.o_psi = cv.take<double2>(nel);
+    m.o_hpsi = cv.take<double2>(nel);
+    m.o_m = cv.take<unsigned char>(vel_m);
+    m.o_T = cv.take<unsigned char>(t_el * cs);
+    m.o_part = cv.take<unsigned char>((size_t)m.nsplit * m.P * m.nbands * cs);
+    m.o_W = cv.take<unsigned char>((size_t)m.P * m.nbands * cs);
+    m.o_li = cv.take<LocalItem>(tasks.size());
+    m.o_bi = cv.take<int>((size_t)m.nbands);
+    m.o_xb = cv.take<int2>((size_t)m.nbands);
+    m.o_gi = cv.take<BGemmItem>(tasks.size());
+    m.o_ws = cv.take<unsigned char>(vel_ws);
+    m.bytes = cv.off;
+    return m;
+}
+
+// copy a job's outputs back to the host (hpsi, and the velocity matrix)
+static int srv_copy_back(SrvReq* r, const hpsi_job& j, size_t nel, const double2* hpsi, const double2* m,
+                         cudaStream_t st)
+{
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(j.hpsi, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st))) {
+        r->err = cudaGetErrorString(e);
+        return HPSI_ERR_CUDA;
+    }
+    if (j.vel && (e = cudaMemcpyAsync(j.vel, m, (size_t)3 * j.nb * j.nb * sizeof(double2), cudaMemcpyDeviceToHost, st))) {
+        r->err = cudaGetErrorString(e);
+        return HPSI_ERR_CUDA;
     }
     return HPSI_OK;
+}
+
+// one job on its lane (scheduler thread)
+static int srv_issue_one(hpsi_server* S, SrvUnit* u, cudaStream_t st)
+{
+    SrvReq* r = u->tasks[0].req;
+    const hpsi_job& j = r->jobs[u->tasks[0].job];
+    if (j.nb == 0) return HPSI_OK;
+    hpsi_ctx* c = S->sys[j.system];
+    KSlot& s = c->slots[j.kid];
+    const size_t nel = (size_t)j.nb * s.npw;
+    if (s.npw == 0) return HPSI_OK;
+    Carver cv;
+    unsigned char* base = S->arena_mem + u->off;
+    double2* psi = reinterpret_cast<double2*>(base + cv.take<double2>(nel));
+    double2* hpsi = reinterpret_cast<double2*>(base + cv.take<double2>(nel));
+    double2* m = reinterpret_cast<double2*>(base + cv.take<unsigned char>(j.vel ? (size_t)3 * j.nb * j.nb * sizeof(double2) : 0));
+    unsigned char* ws = base + cv.take<unsigned char>(0);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(psi, j.psi, nel * sizeof(double2), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(hpsi, j.hpsi, nel * sizeof(double2), cudaMemcpyHostToDevice, st))) {
+        r->err = cudaGetErrorString(e);
+        return HPSI_ERR_CUDA;
+    }
+    int rc = apply_dev(c, s, j.nb, psi, hpsi, S->prec, ws, st, nullptr, nullptr, false);
+    if (!rc && j.vel) rc = velocity_dev(c, s, j.nb, psi, m, S->prec, ws, st);
+    if (rc) { r->err = c->err; return rc; }
+    return srv_copy_back(r, j, nel, hpsi, m, st);
+}
+
+template <typename C, typename V>
+static cudaError_t srv_merged_launches(hpsi_ctx* c, const LocalArgs& la, const MergePlan& m, unsigned char* base,
+                                       const BGemmItem* d_gi, int n_items, const V* vloc, const C* tw, cudaStream_t st)
+{
+    cudaError_t e = launch_local_batch<C, V>(la, m.nbands, m.max_nxs, m.nxblk, reinterpret_cast<C*>(base + m.o_T), vloc,
+                                             tw, tw + c->n1, tw + c->n1 + c->n2, st);
+    if (e || m.P == 0) return e;
+    if ((e = launch_bproj<C, C>(m.P, d_gi, n_items, m.nb_max, m.nsplit, m.P <= 16 ? 0 : 3,
+                                reinterpret_cast<C*>(base + m.o_part), st)))
+        return e;
+    return launch_bexp<C, C>(m.P, d_gi, n_items, m.nb_max, m.npw_max, m.nsplit, 3,
+                             reinterpret_cast<const C*>(base + m.o_part), reinterpret_cast<C*>(base + m.o_W), st);
+}
+
+// several jobs of one cell on a lane: one ragged launch set over all their bands
+static int srv_issue_merged(hpsi_server* S, SrvUnit* u, cudaStream_t st)
+{
+    const hpsi_job& j0 = u->tasks[0].req->jobs[u->tasks[0].job];
+    hpsi_ctx* c = S->sys[j0.system];
+    const bool f64 = S->prec == HPSI_PREC_FP64;
+    const MergePlan m = srv_merge_plan(S, u->tasks);
+    unsigned char* base = S->arena_mem + u->off;
+    double2* psi = reinterpret_cast<double2*>(base + m.o_psi);
+    double2* hpsi = reinterpret_cast<double2*>(base + m.o_hpsi);
+    std::vector<LocalItem> li;
+    std::vector<BGemmItem> gi;
+    std::vector<int> band_item;
+    std::vector<size_t> off;
+    size_t el = 0, t_off = 0;
+    int band0 = 0;
+    cudaError_t e;
+    for (const SrvTask& t : u->tasks) {
+        const hpsi_job& j = t.req->jobs[t.job];
+        KSlot& s = c->slots[j.kid];
+        const size_t nel = (size_t)j.nb * s.npw;
+        off.push_back(el);
+        if ((e = cudaMemcpyAsync(psi + el, j.psi, nel * sizeof(double2), cudaMemcpyHostToDevice, st)) ||
+            (e = cudaMemcpyAsync(hpsi + el, j.hpsi, nel * sizeof(double2), cudaMemcpyHostToDevice, st))) {
+            t.req->err = cudaGetErrorString(e);
+            return HPSI_ERR_CUDA;
+        }
+        const int* pl = s.d_plane;
+        LocalItem L{};
+        L.plane_x = pl;
+        L.plane_off = pl + s.nxs;
+        L.ent_ig = pl + 2 * s.nxs + 1;
+        L.ent_jk = pl + 2 * s.nxs + 1 + s.npw;
+        L.plane_jr = pl + 2 * s.nxs + 1 + 2 * s.npw;
+        L.kinetic = s.d_kin;
+        L.psi = psi + el;
+        L.hpsi = hpsi + el;
+        L.t_off = t_off;
+        L.npw = s.npw;
+        L.nxs = s.nxs;
+        L.nb = j.nb;
+        L.band0 = band0;
+        for (int k = 0; k < j.nb; ++k) band_item.push_back((int)li.size());
+        li.push_back(L);
+        BGemmItem G{};
+        G.pr = f64 ? (const void*)s.pr64 : (const void*)s.pr32;
+        G.psi = L.psi;
+        G.hpsi = L.hpsi;
+        G.lam = s.d_lam;
+        G.part_off = (size_t)m.nsplit * m.P * band0;
+        G.w_off = (size_t)m.P * band0;
+        G.nb = j.nb;
+        G.npw = s.npw;
+        gi.push_back(G);
+        el += nel;
+        t_off += (size_t)j.nb * s.nxs * c->n2 * c->n3;
+        band0 += j.nb;
+    }
+    LocalArgs la{};
+    la.n1 = c->n1; la.n2 = c->n2; la.n3 = c->n3;
+    la.inv_n = 1.0 / ((double)c->n1 * c->n2 * c->n3);
+    la.Lx = c->L[0]; la.Ly = c->L[1]; la.Lz = c->L[2];
+    local_xpass_shape(&la, srv_csize(S));
+    std::vector<int2> xb;
+    for (size_t i = 0; i < li.size(); ++i)
+        for (int b0 = 0; b0 < li[i].nb; b0 += la.bb) xb.push_back(make_int2((int)i, b0));
+    MergePlan mp = m;
+    mp.nxblk = (int)xb.size();
+    la.items = reinterpret_cast<const LocalItem*>(base + m.o_li);
+    la.band_item = reinterpret_cast<const int*>(base + m.o_bi);
+    la.xblk = reinterpret_cast<const int2*>(base + m.o_xb);
+    // item tables: pageable host vectors, staged by the copy call itself
+    SrvReq* r0 = u->tasks[0].req;
+    if ((e = cudaMemcpyAsync(base + m.o_li, li.data(), li.size() * sizeof(LocalItem), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(base + m.o_bi, band_item.data(), band_item.size() * sizeof(int), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(base + m.o_xb, xb.data(), xb.size() * sizeof(int2), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(base + m.o_gi, gi.data(), gi.size() * sizeof(BGemmItem), cudaMemcpyHostToDevice, st))) {
+        r0->err = cudaGetErrorString(e);
+        return HPSI_ERR_CUDA;
+    }
+    const BGemmItem* d_gi = reinterpret_cast<const BGemmItem*>(base + m.o_gi);
+    e = f64 ? srv_merged_launches<double2, double>(c, la, mp, base, d_gi, (int)gi.size(), c->d_v64, c->d_tw64, st)
+            : srv_merged_launches<float2, float>(c, la, mp, base, d_gi, (int)gi.size(), c->d_v32, c->d_tw32, st);
+    if (e) { r0->err = cudaGetErrorString(e); return HPSI_ERR_CUDA; }
+    double2* mv = reinterpret_cast<double2*>(base + m.o_m);
+    for (size_t i = 0; i < u->tasks.size(); ++i) {
+        const SrvTask& t = u->tasks[i];
+        const hpsi_job& j = t.req->jobs[t.job];
+        KSlot& s = c->slots[j.kid];
+        if (j.vel) {
+            const int rc = velocity_dev(c, s, j.nb, psi + off[i], mv, S->prec, base + m.o_ws, st);
+            if (rc) { t.req->err = c->err; return rc; }
+        }
+        const int rc = srv_copy_back(t.req, j, (size_t)j.nb * s.npw, hpsi + off[i], mv, st);
+        if (rc) return rc;
+    }
+    return HPSI_OK;
+}
+
+// Take the next unit from the pending queue that fits the arena (lock held):
+// the oldest job, or — while the oldest has waited less than bypass_ms — the
+// first later one that fits; with merging, further pending jobs of the same
+// cell join it up to merge_max_bands bands while the unit still fits.
+static SrvUnit* srv_take_unit(hpsi_server* S, double now)
+{
+    if (S->pending.empty()) return nullptr;
+    const bool may_bypass = now - S->pending.front().req->t_submit < S->bypass_ms;
+    const size_t scan = may_bypass ? std::min<size_t>(S->pending.size(), 256) : 1;
+    for (size_t i = 0; i < scan; ++i) {
+        const SrvTask& t = S->pending[i];
+        const hpsi_job& j = t.req->jobs[t.job];
+        SrvUnit* u = new SrvUnit();
+        u->tasks.push_back(t);
+        u->bytes = t.bytes;
+        std::vector<size_t> taken{i};
+        if (srv_mergeable(S, j)) {
+            int bands = j.nb;
+            for (size_t k = i + 1; k < S->pending.size() && k < i + 512; ++k) {
+                const SrvTask& t2 = S->pending[k];
+                const hpsi_job& j2 = t2.req->jobs[t2.job];
+                if (j2.system != j.system || !srv_mergeable(S, j2) || bands + j2.nb > S->merge_max_bands) continue;
+                u->tasks.push_back(t2);
+                const MergePlan mp = srv_merge_plan(S, u->tasks);
+                if (mp.bytes > S->arena.size) { u->tasks.pop_back(); continue; }
+                taken.push_back(k);
+                bands += j2.nb;
+            }
+            if (u->tasks.size() > 1) {
+                u->merged = true;
+                u->bytes = srv_merge_plan(S, u->tasks).bytes;
+            }
+        }
+        size_t off = 0;
+        bool ok = S->arena.alloc(u->bytes, &off);
+        while (!ok && u->tasks.size() > 1) {
+            // does not fit now: fewer merged jobs, else the next candidate
+            u->tasks.pop_back();
+            taken.pop_back();
+            u->merged = u->tasks.size() > 1;
+            u->bytes = u->merged ? srv_merge_plan(S, u->tasks).bytes : u->tasks[0].bytes;
+            ok = S->arena.alloc(u->bytes, &off);
+        }
+        if (!ok) { delete u; continue; }
+        u->off = off;
+        for (size_t k = taken.size(); k-- > 0;) S->pending.erase(S->pending.begin() + (long)taken[k]);
+        return u;
+    }
+    return nullptr;
 }
 
 static void srv_loop(hpsi_server* S)
@@ -2208,39 +2456,49 @@ static void srv_loop(hpsi_server* S)
     std::unique_lock<std::mutex> lk(S->mu);
     while (!S->stop) {
         bool progress = false;
-        // admit in arrival order while a lane is free and memory fits
-        while (!S->queue.empty()) {
+        // admit jobs while a lane is free and a unit fits
+        for (;;) {
             int lane = -1;
             for (int i = 0; i < (int)S->lanes.size(); ++i)
-                if (!S->lane_req[i]) { lane = i; break; }
+                if (!S->lane_unit[i]) { lane = i; break; }
             if (lane < 0) break;
-            SrvReq* r = S->queue.front();
-            size_t off = 0;
-            if (!S->arena.alloc(r->bytes, &off)) break;  // head waits for memory
-            S->queue.pop_front();
-            r->off = off;
-            r->lane = lane;
-            r->t_admit = now_ms();
-            S->lane_req[lane] = r;
+            const double t = now_ms();
+            SrvUnit* u = srv_take_unit(S, t);
+            if (!u) break;
+            for (const SrvTask& tk : u->tasks)
+                if (tk.req->t_admit < 0) tk.req->t_admit = t;
+            S->lane_unit[lane] = u;
+            S->units++;
+            if (u->merged) { S->merged_units++; S->merged_jobs += (long long)u->tasks.size(); }
             S->peak_in_use = std::max(S->peak_in_use, S->arena.in_use());
             lk.unlock();
-            r->status = srv_issue(S, r);
+            const int rc = u->merged ? srv_issue_merged(S, u, S->lanes[lane]) : srv_issue_one(S, u, S->lanes[lane]);
             cudaEventRecord(S->lane_ev[lane], S->lanes[lane]);
             lk.lock();
+            if (rc)
+                for (const SrvTask& tk : u->tasks)
+                    if (tk.req->status == HPSI_OK) tk.req->status = rc;
             progress = true;
         }
         // retire finished lanes
         for (int i = 0; i < (int)S->lanes.size(); ++i) {
-            SrvReq* r = S->lane_req[i];
-            if (!r) continue;
+            SrvUnit* u = S->lane_unit[i];
+            if (!u) continue;
             cudaError_t q = cudaEventQuery(S->lane_ev[i]);
             if (q == cudaErrorNotReady) continue;
-            if (q != cudaSuccess && r->status == HPSI_OK) { r->status = HPSI_ERR_CUDA; r->err = cudaGetErrorString(q); }
-            r->t_done = now_ms();
-            r->done = true;
-            S->arena.release(r->off, r->bytes);
-            S->lane_req[i] = nullptr;
-            S->completed++;
+            const double t = now_ms();
+            for (const SrvTask& tk : u->tasks) {
+                SrvReq* r = tk.req;
+                if (q != cudaSuccess && r->status == HPSI_OK) { r->status = HPSI_ERR_CUDA; r->err = cudaGetErrorString(q); }
+                if (--r->remaining == 0) {
+                    r->t_done = t;
+                    r->done = true;
+                    S->completed++;
+                }
+            }
+            S->arena.release(u->off, u->bytes);
+            S->lane_unit[i] = nullptr;
+            delete u;
             progress = true;
         }
         if (progress) S->cv_done.notify_all();
@@ -2258,9 +2516,13 @@ extern "C" int hpsi_server_create(hpsi_ctx* const* systems, int n_systems, const
     if (prec < HPSI_PREC_FP64 || prec > HPSI_PREC_TC_BF16) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: precision");
     if (cfg->lanes < 1 || cfg->lanes > 64) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: lanes must be 1..64");
     if (!(cfg->device_budget_bytes > 0)) return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: device budget");
+    if (cfg->merge_max_bands < 0 || cfg->merge_max_bands > 65535 || !(cfg->bypass_ms >= 0.0))
+        return srv_fail(nullptr, HPSI_ERR_BAD_ARG, "server: merge_max_bands must be 0..65535 and bypass_ms >= 0");
     hpsi_server* S = new hpsi_server();
     S->prec = prec;
     S->dev = systems[0]->dev;
+    S->merge_max_bands = cfg->merge_max_bands;
+    S->bypass_ms = cfg->bypass_ms;
     for (int i = 0; i < n_systems; ++i) {
         if (!systems[i] || systems[i]->dev != S->dev) {
             delete S;
@@ -2275,6 +2537,9 @@ extern "C" int hpsi_server_create(hpsi_ctx* const* systems, int n_systems, const
         for (auto& kv : c->slots) {
             if (!kv.second.valid) continue;
             int rc = prepare_slot(c, kv.second, prec, c->have_dbeta, 0);
+            // merged units run the small cells' nonlocal term on the SIMT matrices
+            if (!rc && S->merge_max_bands > 0 && kv.second.P <= kMergeMaxP && prec != HPSI_PREC_FP64)
+                rc = ensure_proj<float2>(c, kv.second, false, 0);
             if (rc) {
                 std::string m = "server: preparing k-point slot: " + c->err;
                 delete S;
@@ -2294,7 +2559,7 @@ extern "C" int hpsi_server_create(hpsi_ctx* const* systems, int n_systems, const
         cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
         S->lanes.push_back(st);
         S->lane_ev.push_back(ev);
-        S->lane_req.push_back(nullptr);
+        S->lane_unit.push_back(nullptr);
     }
     S->th = std::thread(srv_loop, S);
     *out = S;
@@ -2307,18 +2572,33 @@ extern "C" int hpsi_server_submit(hpsi_server* S, const hpsi_job* jobs, int n_jo
     SrvReq* r = new SrvReq();
     r->jobs.assign(jobs, jobs + n_jobs);
     std::lock_guard<std::mutex> lk(S->mu);
-    std::string why;
-    int rc = srv_request_bytes(S, r->jobs, &r->bytes, &why);
-    if (rc) { delete r; return srv_fail(S, rc, "server submit: " + why); }
-    if (r->bytes > S->arena.size) {
-        delete r;
-        return srv_fail(S, HPSI_ERR_OOM, "server submit: request needs more than the whole device budget");
+    std::vector<SrvTask> tasks;
+    for (int i = 0; i < n_jobs; ++i) {
+        std::string why;
+        SrvTask t;
+        t.req = r;
+        t.job = i;
+        const int rc = srv_job_bytes(S, r->jobs[i], &t.bytes, &why);
+        if (rc) { delete r; return srv_fail(S, rc, "server submit: " + why); }
+        if (t.bytes > S->arena.size) {
+            delete r;
+            return srv_fail(S, HPSI_ERR_OOM, "server submit: a job needs more than the whole device budget");
+        }
+        tasks.push_back(t);
     }
     r->ticket = S->next_ticket++;
     r->t_submit = now_ms();
-    S->queue.push_back(r);
+    r->remaining = n_jobs;
     S->reqs[r->ticket] = r;
     *ticket = r->ticket;
+    if (n_jobs == 0) {
+        r->t_admit = r->t_done = r->t_submit;
+        r->done = true;
+        S->completed++;
+        S->cv_done.notify_all();
+        return HPSI_OK;
+    }
+    for (const SrvTask& t : tasks) S->pending.push_back(t);
     S->cv_work.notify_one();
     return HPSI_OK;
 }
@@ -2352,12 +2632,15 @@ extern "C" int hpsi_server_stats(hpsi_server* S, hpsi_server_statistics* out)
     if (!S || !out) return HPSI_ERR_BAD_ARG;
     std::lock_guard<std::mutex> lk(S->mu);
     out->completed = S->completed;
-    out->queued = (long long)S->queue.size();
+    out->queued = (long long)S->pending.size();
     long long run = 0;
-    for (auto* r : S->lane_req) run += r ? 1 : 0;
+    for (auto* u : S->lane_unit) run += u ? (long long)u->tasks.size() : 0;
     out->running = run;
     out->budget_bytes = (double)S->arena.size;
     out->peak_bytes = (double)S->peak_in_use;
+    out->units = S->units;
+    out->merged_units = S->merged_units;
+    out->merged_jobs = S->merged_jobs;
     return HPSI_OK;
 }
 
@@ -2380,6 +2663,7 @@ extern "C" int hpsi_server_destroy(hpsi_server* S)
     for (auto st : S->lanes) cudaStreamSynchronize(st);
     for (auto st : S->lanes) cudaStreamDestroy(st);
     for (auto ev : S->lane_ev) cudaEventDestroy(ev);
+    for (auto* u : S->lane_unit) delete u;
     for (auto& kv : S->reqs) delete kv.second;
     if (S->arena_mem) cudaFree(S->arena_mem);
     delete S;

@@ -380,10 +380,11 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
 // registers; a 168-register bound, three blocks, spilled and measured slower,
 // 0.142 vs 0.129 ms on the 64-atom cell), three for 36, four for 24.
 //
-// ENERGY: after the G->r transform each thread also sums, in compensated FP32
-// over its line's N points, V|psi(r)|^2 (+ dV |psi(r)|^2, the FP64 part of V
-// the FP32 table misses) and |psi(r)|^2; the block adds its lines' sums in
-// FP64 in a fixed order and writes one slot per (band, block):
+// ENERGY: after the G->r transform each thread also sums over its line's N
+// points V|psi(r)|^2 (+ dV |psi(r)|^2, the FP64 part of V the FP32 table
+// misses) and |psi(r)|^2, in four interleaved FP32 partial sums combined in
+// FP64; the block adds its lines' sums in FP64 in a fixed order and writes
+// one slot per (band, block):
 // epart[((e_band0 + band) * gridDim.x + blockIdx.x) * 2 + {0, 1}].
 constexpr int XREG_THREADS = 128;
 constexpr int xreg_minb(int n) { return n >= 64 ? 2 : (n >= 36 ? 3 : 4); }
@@ -427,25 +428,30 @@ __global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n)) x_pass_reg(Loc
         }
     }
     fftreg::fft_nat_to_split<+1, N1, N2>(v);
-    Sum2f s1, s0;
+    float a1[4] = {0.f, 0.f, 0.f, 0.f}, a0[4] = {0.f, 0.f, 0.f, 0.f}, ac = 0.f;
     {
         const float* vp = vloc + jk;
+        const float* dvp = (ENERGY && a.dv32) ? a.dv32 + jk : nullptr;
 #pragma unroll
         for (int x = 0; x < N; ++x) {
             const float w = valid ? __ldg(vp + (size_t)x * N23) : 0.f;
             float2& e = v[fftreg::split_pos<N1, N2>(x)];
             if constexpr (ENERGY) {
+                // four interleaved FP32 partial sums per line (N/4 terms each);
+                // the FP64 part of V the FP32 table misses (dV) in one more
                 const float mm = e.x * e.x + e.y * e.y;
-                const float dv = (valid && a.dv32) ? __ldg(a.dv32 + jk + (size_t)x * N23) : 0.f;
-                s1.add(w * mm);
-                s1.add(dv * mm);
-                s0.add(mm);
+                a1[x & 3] += w * mm;
+                a0[x & 3] += mm;
+                if (dvp && valid) ac += __ldg(dvp + (size_t)x * N23) * mm;
             }
-            e = make_float2(e.x * w, e.y * w);
+            // rounded product (never fused into the next stage's adds), so that
+            // both variants of the kernel give bit-identical hpsi
+            e = make_float2(__fmul_rn(e.x, w), __fmul_rn(e.y, w));
         }
     }
     if constexpr (ENERGY) {
-        double t1 = f2d_bits(s1.s) + f2d_bits(s1.c), t0 = f2d_bits(s0.s) + f2d_bits(s0.c);
+        double t1 = (f2d_bits(a1[0]) + f2d_bits(a1[1])) + (f2d_bits(a1[2]) + f2d_bits(a1[3])) + f2d_bits(ac);
+        double t0 = (f2d_bits(a0[0]) + f2d_bits(a0[1])) + (f2d_bits(a0[2]) + f2d_bits(a0[3]));
         for (int o = 16; o > 0; o >>= 1) {
             t1 += __shfl_xor_sync(0xffffffffu, t1, o);
             t0 += __shfl_xor_sync(0xffffffffu, t0, o);

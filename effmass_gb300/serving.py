@@ -4,9 +4,11 @@
     t = srv.submit([Job(system=0, kid=3, psi=psi, hpsi=out, vel=v), ...])
     times = srv.wait(t)          # {'queue_ms', 'run_ms', 'total_ms'}
 
-Requests run on the GPU concurrently (one CUDA stream per lane); a request is
-admitted, in arrival order, as soon as a lane is free and its buffers fit in
-the device budget.  Arrays are host numpy complex128 (pinned memory, e.g. from
+Jobs run on the GPU concurrently (one CUDA stream per lane); a job is admitted,
+in arrival order (later jobs that fit may overtake for up to ``bypass_ms``), as
+soon as a lane is free and its buffers fit in the device budget; with
+``merge_max_bands`` > 0 jobs of small cells are merged into one ragged launch
+set.  A request completes when its last job does.  Arrays are host numpy complex128 (pinned memory, e.g. from
 ``pinned_empty``, gives asynchronous copies) and must stay alive until wait().
 """
 from __future__ import annotations
@@ -27,7 +29,8 @@ class HpsiJob(C.Structure):
 
 
 class HpsiServerConfig(C.Structure):
-    _fields_ = [("lanes", C.c_int), ("device_budget_bytes", C.c_double), ("precision", C.c_int)]
+    _fields_ = [("lanes", C.c_int), ("device_budget_bytes", C.c_double), ("precision", C.c_int),
+                ("merge_max_bands", C.c_int), ("bypass_ms", C.c_double)]
 
 
 class HpsiRequestTimes(C.Structure):
@@ -36,7 +39,8 @@ class HpsiRequestTimes(C.Structure):
 
 class HpsiServerStatistics(C.Structure):
     _fields_ = [("completed", C.c_longlong), ("queued", C.c_longlong), ("running", C.c_longlong),
-                ("budget_bytes", C.c_double), ("peak_bytes", C.c_double)]
+                ("budget_bytes", C.c_double), ("peak_bytes", C.c_double), ("units", C.c_longlong),
+                ("merged_units", C.c_longlong), ("merged_jobs", C.c_longlong)]
 
 
 def _bind(L):
@@ -84,12 +88,13 @@ class Job:
 
 
 class Server:
-    def __init__(self, hamiltonians: List, lanes: int = 4, budget_gb: float = 16.0, precision: str = "tc"):
+    def __init__(self, hamiltonians: List, lanes: int = 4, budget_gb: float = 16.0, precision: str = "tc",
+                 merge_max_bands: int = 0, bypass_ms: float = 0.0):
         self._lib = load()
         _bind(self._lib)
         self._hams = list(hamiltonians)
         arr = (C.c_void_p * len(self._hams))(*[h.ctx.value for h in self._hams])
-        cfg = HpsiServerConfig(lanes, budget_gb * (1 << 30), abi.PRECISIONS[precision])
+        cfg = HpsiServerConfig(lanes, budget_gb * (1 << 30), abi.PRECISIONS[precision], merge_max_bands, bypass_ms)
         h = C.c_void_p()
         st = self._lib.hpsi_server_create(arr, len(self._hams), C.byref(cfg), C.byref(h))
         if st:
@@ -125,7 +130,8 @@ class Server:
         s = HpsiServerStatistics()
         self._check(self._lib.hpsi_server_stats(self._srv, C.byref(s)))
         return {"completed": s.completed, "queued": s.queued, "running": s.running,
-                "budget_bytes": s.budget_bytes, "peak_bytes": s.peak_bytes}
+                "budget_bytes": s.budget_bytes, "peak_bytes": s.peak_bytes, "units": s.units,
+                "merged_units": s.merged_units, "merged_jobs": s.merged_jobs}
 
     def close(self):
         if getattr(self, "_srv", None):

@@ -286,9 +286,14 @@ int hpsi_profile_read(hpsi_ctx* ctx, double* ms, long long* launches);
 /* ---- Serving: a device-resident request loop with continuous batching ------
  * Systems (contexts with their bound k-points) stay resident in HBM; requests
  * are lists of k-point jobs submitted from any host thread.  One scheduler
- * thread admits requests in arrival order when a lane (CUDA stream) is free and
- * the request's buffers fit in the device budget, runs them concurrently on the
- * lanes and retires them as their lanes finish.  psi/hpsi/vel of a job are host
+ * thread admits jobs in arrival order when a lane (CUDA stream) is free and
+ * the job's buffers fit in the device budget (a later job that fits may
+ * overtake an older one while the oldest has waited less than bypass_ms), runs
+ * them concurrently on the lanes, and retires a request when its last job
+ * finishes.  With merge_max_bands > 0, pending jobs of a cell with at most 256
+ * projectors are merged (up to that many bands) into one ragged launch set
+ * whose nonlocal term runs on the FP32 (FP64 for HPSI_PREC_FP64) SIMT GEMMs.
+ * psi/hpsi/vel of a job are host
  * memory (pinned memory gives asynchronous copies) and must stay valid until
  * hpsi_server_wait returns; hpsi accumulates (+=) as in hpsi_apply, vel (if not
  * NULL) receives the [3][nb][nb] velocity matrix.  While a server runs, its
@@ -303,16 +308,21 @@ typedef struct hpsi_job {
     double* vel;              /* [3][nb][nb] complex or NULL */
 } hpsi_job;
 typedef struct hpsi_server_config {
-    int lanes;                /* concurrent requests (CUDA streams), 1..64 */
+    int lanes;                /* concurrent work units (CUDA streams), 1..64 */
     double device_budget_bytes; /* arena for in-flight request buffers and workspaces */
     int precision;            /* HPSI_PREC_* for every request */
+    int merge_max_bands;      /* 0: no merging; else bands of one cell per merged unit (<= 65535) */
+    double bypass_ms;         /* 0: strict arrival order; else how long the oldest pending
+                               * job may be overtaken by later jobs that fit */
 } hpsi_server_config;
 typedef struct hpsi_request_times {
     double queue_ms, run_ms, total_ms;  /* submit->admit, admit->done, submit->done */
 } hpsi_request_times;
 typedef struct hpsi_server_statistics {
-    long long completed, queued, running;
+    long long completed;      /* requests retired */
+    long long queued, running; /* jobs pending, jobs on the lanes */
     double budget_bytes, peak_bytes;
+    long long units, merged_units, merged_jobs; /* units admitted; merged ones and their jobs */
 } hpsi_server_statistics;
 int hpsi_server_create(hpsi_ctx* const* systems, int n_systems, const hpsi_server_config* cfg, hpsi_server** out);
 int hpsi_server_submit(hpsi_server* srv, const hpsi_job* jobs, int n_jobs, long long* ticket);

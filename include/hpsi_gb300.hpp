@@ -43,6 +43,11 @@ struct GradHPsi {
     std::span<std::complex<double>> z;
 };
 
+class Hamiltonian;
+// plane-wave count of a bound k-point slot (Callable::dim); std::runtime_error
+// for an unbound slot (hpsi_dim records no message, so it is written here)
+inline int slot_dim(const Hamiltonian* H, int ikpt);
+
 class Hamiltonian {
 public:
     explicit Hamiltonian(const hpsi_system& sys, int precision = HPSI_PREC_FP64)
@@ -81,18 +86,14 @@ public:
                   parent_->ctx_);
         }
 
-        int dim() const
-        {
-            int n = hpsi_dim(parent_->ctx_, ikpt_);
-            if (n < 0) check(n, parent_->ctx_);
-            return n;
-        }
+        int dim() const { return slot_dim(parent_, ikpt_); }
 
-        // Rebind to another (already set) k-point slot.
+        // Rebind to another (already set) k-point slot; on an unbound slot
+        // this throws std::runtime_error and the Callable keeps its slot.
         void set_ikpt(int ikpt)
         {
+            (void)slot_dim(parent_, ikpt);
             ikpt_ = ikpt;
-            (void)dim();
         }
 
         // Device-resident spans, queued on `stream` (cudaStream_t).
@@ -135,12 +136,7 @@ public:
                                       ptr(out.x), ptr(out.y), ptr(out.z), parent_->precision_, nullptr),
                       parent_->ctx_);
             }
-            int dim() const
-            {
-                int n = hpsi_dim(parent_->ctx_, ikpt_);
-                if (n < 0) check(n, parent_->ctx_);
-                return n;
-            }
+            int dim() const { return slot_dim(parent_, ikpt_); }
 
         private:
             friend class Gradient;
@@ -161,5 +157,13 @@ private:
     hpsi_ctx* ctx_ = nullptr;
     int precision_ = HPSI_PREC_FP64;
 };
+
+inline int slot_dim(const Hamiltonian* H, int ikpt)
+{
+    const int n = hpsi_dim(H->ctx(), ikpt);
+    if (n == HPSI_ERR_STATE) throw std::runtime_error("k-point slot " + std::to_string(ikpt) + " is not bound");
+    if (n < 0) check(n, H->ctx());
+    return n;
+}
 
 }  // namespace hpsi

@@ -56,7 +56,8 @@ def test_struct_layout_matches_c():
       printf("%zu %zu %zu %zu\n", sizeof(hpsi_kpoint), offsetof(hpsi_kpoint,k_frac), offsetof(hpsi_kpoint,g_idx), offsetof(hpsi_kpoint,kinetic));
       printf("%zu %zu %zu\n", sizeof(hpsi_batch_item), offsetof(hpsi_batch_item,kid), offsetof(hpsi_batch_item,nb));
       printf("%zu %zu %zu\n", sizeof(hpsi_job), offsetof(hpsi_job,psi), offsetof(hpsi_job,vel));
-      printf("%zu %zu %zu\n", sizeof(hpsi_server_config), offsetof(hpsi_server_config,device_budget_bytes), offsetof(hpsi_server_config,precision));
+      printf("%zu %zu %zu %zu %zu\n", sizeof(hpsi_server_config), offsetof(hpsi_server_config,device_budget_bytes), offsetof(hpsi_server_config,precision), offsetof(hpsi_server_config,merge_max_bands), offsetof(hpsi_server_config,bypass_ms));
+      printf("%zu %zu %zu\n", sizeof(hpsi_server_statistics), offsetof(hpsi_server_statistics,peak_bytes), offsetof(hpsi_server_statistics,merged_jobs));
       return 0; }
     """
     with tempfile.TemporaryDirectory() as td:
@@ -69,12 +70,15 @@ def test_struct_layout_matches_c():
     assert got[0] == [C.sizeof(S), S.dq.offset, S.beta_q.offset, S.dbeta_q.offset]
     assert got[1] == [C.sizeof(Y), Y.lattice.offset, Y.omega.offset, Y.species.offset, Y.atom_tau.offset]
     assert got[2] == [C.sizeof(K), K.k_frac.offset, K.g_idx.offset, K.kinetic.offset]
-    from effmass_gb300.serving import HpsiJob, HpsiServerConfig
+    from effmass_gb300.serving import HpsiJob, HpsiServerConfig, HpsiServerStatistics
     B = abi.HpsiBatchItem
     assert got[3] == [C.sizeof(B), B.kid.offset, B.nb.offset]
     assert got[4] == [C.sizeof(HpsiJob), HpsiJob.psi.offset, HpsiJob.vel.offset]
     assert got[5] == [C.sizeof(HpsiServerConfig), HpsiServerConfig.device_budget_bytes.offset,
-                      HpsiServerConfig.precision.offset]
+                      HpsiServerConfig.precision.offset, HpsiServerConfig.merge_max_bands.offset,
+                      HpsiServerConfig.bypass_ms.offset]
+    T = HpsiServerStatistics
+    assert got[6] == [C.sizeof(T), T.peak_bytes.offset, T.merged_jobs.offset]
 
 
 def test_cpp_wrapper_header_compiles():

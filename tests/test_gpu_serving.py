@@ -1,7 +1,8 @@
 """The serving loop (hpsi_server_*): results of a request are the same alone and
-in a mixed, concurrently running stream (within the tensor-core tolerance,
-1e-6 relative), agree with direct hpsi_apply / hpsi_velocity_matrix calls, and
-admission respects the device budget."""
+in a mixed, concurrently running stream — where jobs overtake one another and
+small cells' jobs are merged into one ragged launch set — within the
+tensor-core tolerance (1e-6 relative), agree with direct hpsi_apply /
+hpsi_velocity_matrix calls, and admission respects the device budget."""
 import numpy as np
 import pytest
 
@@ -76,7 +77,8 @@ def test_same_alone_and_in_the_mix(systems):
     reqs = _requests(systems)
     hams = [h for h, _ in systems]
     alone, _ = _run(lambda: Server(hams, lanes=1, budget_gb=2, precision="tc"), reqs, concurrent=False)
-    mixed, stats = _run(lambda: Server(hams, lanes=4, budget_gb=2, precision="tc"), reqs, concurrent=True)
+    mixed, stats = _run(lambda: Server(hams, lanes=4, budget_gb=2, precision="tc", merge_max_bands=256,
+                                       bypass_ms=5.0), reqs, concurrent=True)
     assert stats["completed"] == len(reqs)
     for a_jobs, m_jobs, jobs in zip(alone, mixed, reqs):
         for a, m, j in zip(a_jobs, m_jobs, jobs):
@@ -91,6 +93,46 @@ def test_same_alone_and_in_the_mix(systems):
             if a.vel is not None:
                 vref = H.velocity_matrix(j["kid"], j["psi"].shape[0], j["psi"], precision="fp64")
                 assert rel_err(m.vel, vref) <= 1e-6
+
+
+def test_merged_units_match_direct_calls(systems):
+    """One lane kept busy by a first job while many small requests queue: the
+    scheduler merges the queued jobs of each small cell into ragged units."""
+    from effmass_gb300 import system as S
+    from effmass_gb300.serving import Job, Server
+    hams = [h for h, _ in systems]
+    rng = np.random.default_rng(5)
+    reqs = []
+    for r in range(40):
+        si = int(rng.integers(0, len(systems)))
+        H, kps = systems[si]
+        ki = int(rng.integers(0, len(kps)))
+        nb = int(rng.integers(1, 24))
+        psi = S.make_bands(kps[ki], nb, seed=int(rng.integers(0, 10 ** 6)))
+        vel = bool(rng.integers(0, 2))
+        reqs.append((si, ki, psi, vel))
+    with Server(hams, lanes=1, budget_gb=2, precision="tc", merge_max_bands=512, bypass_ms=50.0) as srv:
+        H, kps = systems[2]
+        big = S.make_bands(kps[0], 96, seed=3)
+        t0 = srv.submit([Job(2, 0, big, np.zeros_like(big))])
+        jobs = [Job(si, ki, psi, np.zeros_like(psi),
+                    np.zeros((3, psi.shape[0], psi.shape[0]), dtype=np.complex128) if vel else None)
+                for si, ki, psi, vel in reqs]
+        ts = [srv.submit([j]) for j in jobs]
+        srv.wait(t0)
+        for t in ts:
+            srv.wait(t)
+        st = srv.stats()
+    assert st["completed"] == len(reqs) + 1
+    assert st["merged_units"] >= 1 and st["merged_jobs"] >= 2, st
+    for (si, ki, psi, vel), j in zip(reqs, jobs):
+        H, kps = systems[si]
+        ref = np.zeros_like(psi)
+        H.apply(ki, psi.shape[0], psi, ref, "fp64")
+        assert rel_err(j.hpsi, ref) <= 1e-6
+        if vel:
+            vref = H.velocity_matrix(ki, psi.shape[0], psi, precision="fp64")
+            assert rel_err(j.vel, vref) <= 1e-6
 
 
 def test_budget_admission_and_refusals(systems):
