@@ -249,4 +249,58 @@ HPSI_HD constexpr int split_pos(int x)
     return N2 * (x % N1) + x / N1;
 }
 
+// ---- a line of N = 2 H on a lane pair ------------------------------------
+// Lanes l and l ^ 16 of a warp share one line (the "even" lane is the one in
+// the lower half-warp), so that each half-warp touches 16 consecutive lines
+// or elements: coalesced global accesses and conflict-free shared-memory rows
+// and columns.  Half the registers of a one-thread line; every lane of the
+// warp must make the calls (the exchange is a full-warp shuffle).
+//
+// fft_pair (decimation in time): the even lane holds x[2n], the odd lane
+// x[2n+1] (n < H = N1 N2, natural order in v).  Each lane transforms its half
+// in registers, the odd lane multiplies by W_N^{S m}, and one exchange gives
+//   even lane:  X[m]     = E[m] + W_N^{S m} O[m]
+//   odd lane:   X[m + H] = E[m] - W_N^{S m} O[m],   m < H,
+// with X[m (+ H)] left at v[split_pos<N1, N2>(m)].
+
+template <int S, int N1, int N2, int I>
+HPSI_D void pair_twiddle(float2 (&v)[N1 * N2])  // v[split_pos(m)] *= W_{2H}^{S m}, m = I..H-1
+{
+    constexpr int H = N1 * N2;
+    if constexpr (I < H) {
+        constexpr int r = split_pos<N1, N2>(I);
+        v[r] = twiddle<2 * H, I, S>(v[r]);
+        pair_twiddle<S, N1, N2, I + 1>(v);
+    }
+}
+
+// even lane: v + partner's v; odd lane: partner's v - v
+template <int H>
+HPSI_D void pair_exchange(float2 (&v)[H], bool odd)
+{
+    const float sgn = odd ? -1.f : 1.f;
+#pragma unroll
+    for (int r = 0; r < H; ++r) {
+        const float ox = __shfl_xor_sync(0xffffffffu, v[r].x, 16);
+        const float oy = __shfl_xor_sync(0xffffffffu, v[r].y, 16);
+        v[r] = make_float2(fmaf(sgn, v[r].x, ox), fmaf(sgn, v[r].y, oy));
+    }
+}
+
+// half-length plans H = h1 h2 of the lane-pair transforms of the common lines
+template <int N> struct PairPlan;
+template <> struct PairPlan<72> { static constexpr int h1 = 9, h2 = 4; };
+template <> struct PairPlan<36> { static constexpr int h1 = 9, h2 = 2; };
+template <> struct PairPlan<24> { static constexpr int h1 = 4, h2 = 3; };
+template <> struct PairPlan<64> { static constexpr int h1 = 8, h2 = 4; };
+
+template <int S, int N1, int N2>
+HPSI_D void fft_pair(float2 (&v)[N1 * N2], bool odd)
+{
+    fft_nat_to_split<S, N1, N2>(v);
+    if (odd) pair_twiddle<S, N1, N2, 0>(v);
+    pair_exchange<N1 * N2>(v, odd);
+}
+
 }  // namespace fftreg
+

@@ -181,6 +181,239 @@ __global__ void __launch_bounds__(Cfg<C>::g2r_threads, WIDE ? 1 : Cfg<C>::plane_
     }
 }
 
+// ---- lane-pair plane passes (complex64, compile-time plans) ----------------
+// One (plane, band) per block and ONE shared-memory plane of n x (n+1)
+// complex64 values (odd row stride: rows and columns conflict-free),
+// transformed in place: each z-row and each y-column is owned by one lane
+// pair (fftreg::fft_pair: even/odd samples, a half-length register transform
+// per lane, one shuffle exchange; the pair is lanes l and l ^ 16, so a
+// half-warp reads one run of 16 rows or columns: no bank conflicts, and the
+// y-transforms' T accesses are 128-byte runs), so a plane costs three block barriers
+// instead of one per Stockham stage.  Blocks are 2n threads rounded up to
+// whole warps (160 for n = 72), small enough (one plane, ~100 registers) that
+// four or more planes share an SM.
+using fftreg::PairPlan;
+template <int N> constexpr int pair_threads() { return (2 * N + 31) / 32 * 32; }
+template <int N> constexpr int pair_minb() { return N >= 64 ? 4 : (N >= 36 ? 8 : 12); }
+
+// The rows of a plane that hold sphere points, |G_y| <= jr: rows 0..jr and
+// n-jr..n-1, or every row when 2 jr + 1 >= n.  row(L) is the L-th of them.
+struct PlaneRows {
+    int jr, n;
+    bool all;
+    HPSI_D PlaneRows(int jr_, int n_) : jr(jr_), n(n_), all(2 * jr_ + 1 >= n_) {}
+    HPSI_D int count() const { return all ? n : 2 * jr + 1; }
+    HPSI_D int row(int L) const { return (all || L <= jr) ? L : L + n - (2 * jr + 1); }
+    HPSI_D bool holds(int j) const { return all || j <= jr || j >= n - jr; }
+};
+
+template <typename PL>
+__global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
+    g2r_planes_pair(LocalArgs a, const double2* __restrict__ psi, float2* __restrict__ T)
+{
+    constexpr int N = PL::n, NP = N + 1, N23 = N * N, H1 = PairPlan<N>::h1, H2 = PairPlan<N>::h2, H = N / 2;
+    constexpr int NT = pair_threads<N>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* pl = reinterpret_cast<float2*>(smem_raw);
+    const int p = blockIdx.x;
+    int b = blockIdx.y;
+    int npw = a.npw, nxs = a.nxs;
+    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk, *plane_jr = a.plane_jr;
+    if (a.items) {  // batched: the band's item (uniform per block, before any barrier)
+        const LocalItem I = a.items[a.band_item[b]];
+        if (p >= I.nxs) return;
+        b -= I.band0;
+        npw = I.npw; nxs = I.nxs;
+        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk; plane_jr = I.plane_jr;
+        psi = I.psi;
+        T += I.t_off;
+    }
+    const PlaneRows rows(plane_jr ? plane_jr[p] : N, N);
+    const int nrows = rows.count();
+    // zero the rows in use (the others are never read)
+    for (int t = threadIdx.x; t < nrows * NP; t += NT) {
+        const int L = t / NP, k = t - L * NP;
+        pl[rows.row(L) * NP + k] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const double2* ps = psi + (size_t)b * npw;
+    const int e0 = plane_off[p], e1 = plane_off[p + 1];
+    uint32_t mx = 0u;  // float bits of the largest |re|, |im| this thread scattered
+    // in batches of SB entries per thread: all index loads, then all psi loads,
+    // then the stores, so the two dependent global round trips are paid once
+    // per batch, not once per entry
+    constexpr int SB = 8;
+    const bool want_max = a.rowmax && !a.items;
+    for (int eb = e0 + threadIdx.x; eb < e1; eb += SB * NT) {
+        int ig[SB], jk[SB];
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+            const int e = eb + u * NT;
+            ig[u] = e < e1 ? ent_ig[e] : -1;
+            jk[u] = e < e1 ? ent_jk[e] : -1;
+        }
+        double2 c[SB];
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+            // a G that shares its grid point with a later one (ig < 0) is not
+            // scattered, but its coefficient is still a row element of the band operand
+            const bool need = jk[u] >= 0 && (ig[u] >= 0 || want_max);
+            c[u] = need ? ps[ig[u] & 0x7fffffff] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < SB; ++u) {
+            if (jk[u] < 0) continue;
+            const float2 v = to_c64(c[u]);
+            if (ig[u] >= 0) {
+                const int j = jk[u] / N, k = jk[u] - (jk[u] / N) * N;
+                pl[j * NP + k] = v;
+            }
+            mx = max(mx, max(__float_as_uint(v.x) & 0x7fffffffu, __float_as_uint(v.y) & 0x7fffffffu));
+        }
+    }
+    if (a.rowmax && !a.items) {
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if ((threadIdx.x & 31) == 0 && mx) atomicMax(a.rowmax + b, mx);
+    }
+    __syncthreads();
+    // lane pair (l, l ^ 16) of warp w: pair index 16 w + (l & 15)
+    const int pr = (threadIdx.x >> 5) * 16 + (threadIdx.x & 15);
+    const bool odd = (threadIdx.x >> 4) & 1;
+    float2 v[H];
+    // z (rows in use), G->r, in place
+    {
+        const bool on = pr < nrows;
+        float2* row = pl + (on ? rows.row(pr) : 0) * NP;
+#pragma unroll
+        for (int n = 0; n < H; ++n) v[n] = on ? row[2 * n + odd] : make_float2(0.f, 0.f);
+        fftreg::fft_pair<+1, H1, H2>(v, odd);
+        if (on) {
+#pragma unroll
+            for (int m = 0; m < H; ++m) row[m + (odd ? H : 0)] = v[fftreg::split_pos<H1, H2>(m)];
+        }
+    }
+    __syncthreads();
+    // y (columns), G->r, straight to T: the even lane holds rows 2n, the odd 2n+1
+    {
+        const bool on = pr < N;
+        const int k = on ? pr : 0;
+#pragma unroll
+        for (int n = 0; n < H; ++n) {
+            const int j = 2 * n + (odd ? 1 : 0);
+            v[n] = (on && rows.holds(j)) ? pl[j * NP + k] : make_float2(0.f, 0.f);
+        }
+        fftreg::fft_pair<+1, H1, H2>(v, odd);
+        if (on) {
+            float2* Tp = T + ((size_t)b * nxs + p) * N23 + k + (odd ? H * N : 0);
+#pragma unroll
+            for (int m = 0; m < H; ++m) Tp[(size_t)m * N] = v[fftreg::split_pos<H1, H2>(m)];
+        }
+    }
+}
+
+template <typename PL>
+__global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
+    r2g_planes_pair(LocalArgs a, const float2* __restrict__ T, const double2* __restrict__ psi,
+                    double2* __restrict__ hpsi, const double* __restrict__ kinetic)
+{
+    constexpr int N = PL::n, NP = N + 1, N23 = N * N, H1 = PairPlan<N>::h1, H2 = PairPlan<N>::h2, H = N / 2;
+    constexpr int NT = pair_threads<N>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* pl = reinterpret_cast<float2*>(smem_raw);
+    const int p = blockIdx.x;
+    int b = blockIdx.y;
+    int npw = a.npw, nxs = a.nxs;
+    const int *plane_off = a.plane_off, *ent_ig = a.ent_ig, *ent_jk = a.ent_jk, *plane_jr = a.plane_jr;
+    if (a.items) {  // batched: the band's item (uniform per block, before any barrier)
+        const LocalItem I = a.items[a.band_item[b]];
+        if (p >= I.nxs) return;
+        b -= I.band0;
+        npw = I.npw; nxs = I.nxs;
+        plane_off = I.plane_off; ent_ig = I.ent_ig; ent_jk = I.ent_jk; plane_jr = I.plane_jr;
+        psi = I.psi; hpsi = I.hpsi; kinetic = I.kinetic;
+        T += I.t_off;
+    }
+    const PlaneRows rows(plane_jr ? plane_jr[p] : N, N);
+    const int nrows = rows.count();
+    // lane pair (l, l ^ 16) of warp w: pair index 16 w + (l & 15)
+    const int pr = (threadIdx.x >> 5) * 16 + (threadIdx.x & 15);
+    const bool odd = (threadIdx.x >> 4) & 1;
+    float2 v[H];
+    // y (columns), r->G, from T; only the rows in use are kept
+    {
+        const bool on = pr < N;
+        const int k = on ? pr : 0;
+        const float2* Tp = T + ((size_t)b * nxs + p) * N23 + k + (odd ? N : 0);
+#pragma unroll
+        for (int n = 0; n < H; ++n) v[n] = on ? Tp[(size_t)(2 * n) * N] : make_float2(0.f, 0.f);
+        fftreg::fft_pair<-1, H1, H2>(v, odd);
+        if (on) {
+#pragma unroll
+            for (int m = 0; m < H; ++m) {
+                const int j = m + (odd ? H : 0);
+                if (rows.holds(j)) pl[j * NP + k] = v[fftreg::split_pos<H1, H2>(m)];
+            }
+        }
+    }
+    __syncthreads();
+    // z (rows in use), r->G, in place
+    {
+        const bool on = pr < nrows;
+        float2* row = pl + (on ? rows.row(pr) : 0) * NP;
+#pragma unroll
+        for (int n = 0; n < H; ++n) v[n] = on ? row[2 * n + odd] : make_float2(0.f, 0.f);
+        fftreg::fft_pair<-1, H1, H2>(v, odd);
+        if (on) {
+#pragma unroll
+            for (int m = 0; m < H; ++m) row[m + (odd ? H : 0)] = v[fftreg::split_pos<H1, H2>(m)];
+        }
+    }
+    __syncthreads();
+    // gather: kinetic*psi + grid/N in FP32, one FP64 add per component into
+    // hpsi, or stored to out32 (the tensor-core expansion adds it)
+    const double2* ps = psi + (size_t)b * npw;
+    double2* hp = hpsi + (size_t)b * npw;
+    const int e0 = plane_off[p], e1 = plane_off[p + 1];
+    const float inv_n = (float)a.inv_n;
+    float2* o32 = (a.out32 && !a.items) ? a.out32 + (size_t)b * npw : nullptr;
+    // in batches of GB entries per thread: index loads, then psi / kinetic
+    // (and hpsi) loads, then the stores
+    constexpr int GB = 4;
+    for (int eb = e0 + threadIdx.x; eb < e1; eb += GB * NT) {
+        int ig[GB], jk[GB];
+#pragma unroll
+        for (int u = 0; u < GB; ++u) {
+            const int e = eb + u * NT;
+            ig[u] = e < e1 ? (ent_ig[e] & 0x7fffffff) : -1;
+            jk[u] = e < e1 ? ent_jk[e] : 0;
+        }
+        double2 c[GB], h[GB];
+        double kd[GB];
+#pragma unroll
+        for (int u = 0; u < GB; ++u) {
+            c[u] = ig[u] >= 0 ? ps[ig[u]] : make_double2(0.0, 0.0);
+            kd[u] = ig[u] >= 0 ? kinetic[ig[u]] : 0.0;
+            h[u] = (ig[u] >= 0 && !o32) ? hp[ig[u]] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < GB; ++u) {
+            if (ig[u] < 0) continue;
+            const int j = jk[u] / N, k = jk[u] - (jk[u] / N) * N;
+            const float2 g = pl[j * NP + k];
+            const float2 s = to_c64(c[u]);
+            const float kin = d2f_bits(kd[u]);
+            const float2 t = make_float2(fmaf(kin, s.x, g.x * inv_n), fmaf(kin, s.y, g.y * inv_n));
+            if (o32) {
+                o32[ig[u]] = t;
+            } else {
+                h[u].x += f2d_bits(t.x);
+                h[u].y += f2d_bits(t.y);
+                hp[ig[u]] = h[u];
+            }
+        }
+    }
+}
+
 // x pass: a block owns the x-lines of (j, k0..k0+KT) for BB consecutive bands
 // (NL = KT*BB lines, line L = bb*KT + kk, element x at [x*NL + L]); the V tile
 // is loaded once per block.  The G->r transform reads the sphere planes of T
@@ -694,11 +927,26 @@ void local_xpass_shape(LocalArgs* a, size_t csize)
         else x_pass_reg<PL, false><<<G, XREG_THREADS, 0, st>>>(a, T, vloc);                  \
     } while (0)
 
-// the register x pass serves the complex64 compile-time plans
+// the register x pass and the lane-pair plane passes serve the complex64
+// compile-time plans
 template <typename C, typename PL>
 constexpr bool xreg_plan()
 {
     return std::is_same<C, float2>::value && !std::is_same<PL, NoPlan>::value;
+}
+
+// launch of a lane-pair plane kernel: one n x (n+1) complex64 plane per block
+template <typename PL>
+constexpr size_t pair_smem()
+{
+    if constexpr (std::is_same<PL, NoPlan>::value) return 0;
+    else return sizeof(float2) * (size_t)PL::n * (PL::n + 1);
+}
+template <typename PL>
+constexpr int pair_block()
+{
+    if constexpr (std::is_same<PL, NoPlan>::value) return 0;
+    else return pair_threads<PL::n>();
 }
 
 template <typename C, typename V, bool WIDE, typename PL, int KTC>
@@ -719,7 +967,11 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     const int ptg = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::g2r_threads;
     int h = prof->open(PH_G2R, st);
-    g2r<<<gp, ptg, sp, st>>>(a, psi, T, twy, twz);
+    if constexpr (xreg_plan<C, PL>()) {
+        g2r_planes_pair<PL><<<gp, pair_block<PL>(), pair_smem<PL>(), st>>>(a, psi, T);
+    } else {
+        g2r<<<gp, ptg, sp, st>>>(a, psi, T, twy, twz);
+    }
     prof->close(h, st);
     if (a.after_g2r && (e = cudaEventRecord(a.after_g2r, st))) return e;
     h = prof->open(PH_XPASS, st);
@@ -731,7 +983,11 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     }
     prof->close(h, st);
     h = prof->open(PH_R2G, st);
-    r2g<<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
+    if constexpr (xreg_plan<C, PL>()) {
+        r2g_planes_pair<PL><<<gp, pair_block<PL>(), pair_smem<PL>(), st>>>(a, T, psi, hpsi, kinetic);
+    } else {
+        r2g<<<gp, pt, sp, st>>>(a, T, psi, hpsi, kinetic, twy, twz);
+    }
     prof->close(h, st);
     return cudaGetLastError();
 }
@@ -751,14 +1007,17 @@ static cudaError_t launch_local_batch_t(const LocalArgs& a, int nbands, int max_
     if (max_nxs == 0 || nbands == 0 || nxblk == 0) return cudaSuccess;
     const int pt = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::plane_threads;
     dim3 gp(max_nxs, nbands);
-    g2r<<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
+    if constexpr (xreg_plan<C, PL>()) g2r_planes_pair<PL><<<gp, pair_block<PL>(), pair_smem<PL>(), st>>>(a, nullptr, T);
+    else g2r<<<gp, pt, sp, st>>>(a, nullptr, T, twy, twz);
     if constexpr (xreg_plan<C, PL>()) {
         XREG_LAUNCH(PL, dim3(ceil_div(PL::n * PL::n, XREG_THREADS), nbands));
     } else {
         dim3 gx(ceil_div(a.n3, a.kt), a.n2, nxblk);
         xp<<<gx, 256, sx, st>>>(a, 0, T, vloc, twx);
     }
-    r2g<<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
+    if constexpr (xreg_plan<C, PL>())
+        r2g_planes_pair<PL><<<gp, pair_block<PL>(), pair_smem<PL>(), st>>>(a, T, nullptr, nullptr, nullptr);
+    else r2g<<<gp, pt, sp, st>>>(a, T, nullptr, nullptr, nullptr, twy, twz);
     return cudaGetLastError();
 }
 
@@ -827,7 +1086,9 @@ static cudaError_t launch_density_t(const LocalArgs& a, int nb, const double2* p
     if ((e = cudaFuncSetAttribute(xd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
     const int ptg = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::g2r_threads;
-    g2r<<<dim3(a.nxs, nb), ptg, sp, st>>>(a, psi, T, twy, twz);
+    if constexpr (xreg_plan<C, PL>())
+        g2r_planes_pair<PL><<<dim3(a.nxs, nb), pair_block<PL>(), pair_smem<PL>(), st>>>(a, psi, T);
+    else g2r<<<dim3(a.nxs, nb), ptg, sp, st>>>(a, psi, T, twy, twz);
     xd<<<dim3(ceil_div(a.n3, a.kt), a.n2), 256, sx, st>>>(a, nb, T, occ, rho, twx);
     return cudaGetLastError();
 }

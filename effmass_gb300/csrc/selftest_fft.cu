@@ -9,9 +9,8 @@
 //     Stockham stages of fft.cuh (fft_lines_io), one line per block in shared
 //     memory;
 //   * complex64 with a compile-time plan (n1 = n2 = n3 in {24, 36, 64, 72}):
-//     the compile-time two-stage plans (fft_lines_cc) of the plane kernels
-//     along z and y, and the register transform of the x pass (fft_reg.cuh)
-//     along x.
+//     the lane-pair transform of the plane kernels (fftreg::fft_pair) along z
+//     and y, and the one-thread register transform of the x pass along x.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -49,24 +48,29 @@ __global__ void line_fft_kernel(C* g, int n, int es, int lines_inner, int stride
     for (int t = threadIdx.x; t < n; t += blockDim.x) g[base + (size_t)t * es] = cscale(a[t], (R)scale);
 }
 
-// compile-time plan, one line per block (the plane kernels' z / y transforms)
-template <typename PL>
-__global__ void line_fft_ct_kernel(float2* g, int es, int lines_inner, int stride_inner, int stride_outer,
-                                   const float2* __restrict__ tw_g, int sign, float scale)
+// lane-pair transform (the plane kernels' z / y transforms): lanes l and
+// l ^ 16 share a line, the even lane holding the even samples; natural order
+// out (each lane writes its half of the outputs)
+template <typename PL, int S>
+__global__ void line_fft_pair_kernel(float2* g, int es, int lines_inner, int stride_inner, int stride_outer,
+                                     int nlines, float scale)
 {
-    constexpr int N = PL::n;
-    __shared__ float2 a[N], b[N], tw[N];
-    const int line = blockIdx.x;
-    const size_t base = (size_t)(line % lines_inner) * stride_inner + (size_t)(line / lines_inner) * stride_outer;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) {
-        a[t] = g[base + (size_t)t * es];
-        tw[t] = tw_g[t];
+    constexpr int N = PL::n, H = N / 2, H1 = fftreg::PairPlan<N>::h1, H2 = fftreg::PairPlan<N>::h2;
+    const int line = blockIdx.x * (blockDim.x / 2) + (threadIdx.x >> 5) * 16 + (threadIdx.x & 15);
+    const bool odd = (threadIdx.x >> 4) & 1;
+    const bool on = line < nlines;  // every lane runs the transform (full-warp exchange)
+    float2* p = g + (on ? (size_t)(line % lines_inner) * stride_inner + (size_t)(line / lines_inner) * stride_outer : 0);
+    float2 v[H];
+#pragma unroll
+    for (int n = 0; n < H; ++n) v[n] = on ? p[(size_t)(2 * n + (odd ? 1 : 0)) * es] : make_float2(0.f, 0.f);
+    fftreg::fft_pair<S, H1, H2>(v, odd);
+    if (on) {
+#pragma unroll
+        for (int m = 0; m < H; ++m) {
+            const float2 e = v[fftreg::split_pos<H1, H2>(m)];
+            p[(size_t)(m + (odd ? H : 0)) * es] = make_float2(e.x * scale, e.y * scale);
+        }
     }
-    __syncthreads();
-    fft_lines_cc<float2, PL, 1>(SmemLinesC<float2, N, 1>{a}, SmemLinesC<float2, N, 1>{a},
-                                SmemLinesC<float2, N, 1>{b}, tw, sign);
-    __syncthreads();
-    for (int t = threadIdx.x; t < N; t += blockDim.x) g[base + (size_t)t * es] = cscale(a[t], scale);
 }
 
 // register transform, one thread per line (the x pass's transform); natural
@@ -143,24 +147,19 @@ template <typename PL>
 cudaError_t run_plan_axes(float2* d, int sign, cudaStream_t st)
 {
     constexpr int N = PL::n;
-    std::vector<float2> tw = twiddles<float2>(N);
-    float2* dtw = nullptr;
-    cudaError_t e = cudaMalloc(&dtw, tw.size() * sizeof(float2));
-    if (e) return e;
-    cudaMemcpy(dtw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
     const float scale = sign < 0 ? 1.0f / N : 1.0f;
     const int nlines = N * N;
     int es, li, si, so;
-    for (int ax : {2, 1}) {  // z then y: compile-time two-stage plans
+    for (int ax : {2, 1}) {  // z then y: lane-pair transforms, 64 lines per 128-thread block
         axis_walk(ax, N, N, N, &es, &li, &si, &so);
-        line_fft_ct_kernel<PL><<<nlines, 128, 0, st>>>(d, es, li, si, so, dtw, sign, scale);
+        if (sign > 0) line_fft_pair_kernel<PL, +1><<<(nlines + 63) / 64, 128, 0, st>>>(d, es, li, si, so, nlines, scale);
+        else line_fft_pair_kernel<PL, -1><<<(nlines + 63) / 64, 128, 0, st>>>(d, es, li, si, so, nlines, scale);
     }
-    axis_walk(0, N, N, N, &es, &li, &si, &so);  // x: register transform
+    axis_walk(0, N, N, N, &es, &li, &si, &so);  // x: one-thread register transform
     if (sign > 0) line_fft_reg_kernel<PL, +1><<<(nlines + 127) / 128, 128, 0, st>>>(d, es, li, si, so, nlines, scale);
     else line_fft_reg_kernel<PL, -1><<<(nlines + 127) / 128, 128, 0, st>>>(d, es, li, si, so, nlines, scale);
-    e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
     cudaStreamSynchronize(st);
-    cudaFree(dtw);
     return e;
 }
 
