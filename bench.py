@@ -365,9 +365,10 @@ def run_gb300(args, rank, world, local):
         roof = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "peak_source": src + " dense bf16 tensor peak"}
     # DRAM bytes (read + write) of one launch of this workload (128 bands per
-    # launch, 64-atom cell, tensor-core path) from an ncu --set full capture of
-    # this bench command: x pass 219.2 MB read + 162.3 MB written
-    ncu_traffic = {"x_pass": 381.45e6}
+    # launch, 64-atom cell, tensor-core path) from ncu --set full captures of
+    # this bench command: x pass 219.2 + 157.9 MB, G->r planes 76.3 + 159.4 MB,
+    # r->G planes 294.2 + 29.1 MB
+    ncu_traffic = {"x_pass": 377.15e6, "g2r_planes": 235.76e6, "r2g_planes": 323.30e6}
     roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec != "fp64") else None
     if roof["traffic"] is not None and bound == "hbm":
         roof["algorithmic_bytes_per_launch"] = alg[dom][1] / prof[dom][1]
