@@ -357,7 +357,8 @@ static int build_group(hpsi_batch* b, Group& g)
     for (int idx : g.items) {
         const BItem& it = b->items[idx];
         KSlot& s = c->slots[it.kid];
-        int rc = prepare_slot(c, s, b->prec, false, 0);
+        // the batched nonlocal term reads the complex64 (or complex128) projector matrix
+        int rc = prepare_slot(c, s, fp64(b) ? HPSI_PREC_FP64 : HPSI_PREC_FP32, false, 0);
         if (rc) return bfail(b, rc, "item %d: %s", idx, c->err.c_str());
         if (g.litems.empty()) g.P = s.P;
         if (s.P != g.P) return bfail(b, HPSI_ERR_STATE, "item %d: projector count differs within a cell", idx);

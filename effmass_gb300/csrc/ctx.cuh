@@ -29,15 +29,19 @@ struct KSlot {
     bool aliased = false;          // two G-vectors map to one grid point (the scatter keeps the last)
     int* d_plane = nullptr;    // plane_x[nxs], plane_off[nxs+1], ent_ig[npw], ent_jk[npw]
     int P = 0;
+    std::vector<ProjRow> rows;     // host copy of d_rows
     ProjRow* d_rows = nullptr;
     double* d_lam = nullptr;
     double2* pr64 = nullptr;
     bool pr64_grad = false;
     float2* pr32 = nullptr;
     bool pr32_grad = false;
-    // tensor-core operands (built from pr32 on first use of a TC precision)
+    // tensor-core H|psi>: generator tables of the projector operands (built
+    // from the FP64 tables on first use of a TC precision); tc_proj and
+    // tc_expand carry only their K depth and row factors
     int tc_fmt = -1;               // -1 none, 0 FP16 split, 1 BF16 split
     unsigned char* tc_mem = nullptr;
+    TcGen tcgen;
     TcOperand tc_proj, tc_expand;
     int tcg_fmt = -1;              // gradient operands (4P-row projection, per-direction expansion)
     unsigned char* tcg_mem = nullptr;

@@ -354,6 +354,7 @@ extern "C" int hpsi_set_kpoint(hpsi_ctx* c, int kid, const hpsi_kpoint* kp)
             CUDA_TRY(c, dalloc(&s.d_rows, (size_t)s.P));
             CUDA_TRY(c, dalloc(&s.d_lam, (size_t)s.P));
             CUDA_TRY(c, cudaMemcpy(s.d_rows, rows.data(), s.P * sizeof(ProjRow), cudaMemcpyHostToDevice));
+            s.rows.assign(rows.begin(), rows.begin() + s.P);
             CUDA_TRY(c, cudaMemcpy(s.d_lam, lam.data(), s.P * sizeof(double), cudaMemcpyHostToDevice));
         }
         CUDA_TRY(c, cudaDeviceSynchronize());
@@ -532,27 +533,29 @@ static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
 {
     if (s.P == 0 || s.npw == 0) return HPSI_OK;
     if (s.tc_fmt == fmt && s.tc_mem) return HPSI_OK;
-    int rc;
-    if ((rc = ensure_proj<float2>(c, s, false, st))) return rc;
     dfree(s.tc_mem);
     s.tc_fmt = -1;
-    const size_t k1 = tc_round_k(2 * (size_t)s.npw), k2 = tc_round_k(2 * (size_t)s.P);
-    Carver cv;
-    const size_t rp = tc_rows_pad(s.P), rg = tc_rows_pad(s.npw);
-    const size_t o1h = cv.take<uint16_t>(rp * k1), o1l = cv.take<uint16_t>(rp * k1);
-    const size_t o1s = cv.take<float>((size_t)s.P);
-    const size_t o2h = cv.take<uint16_t>(rg * k2), o2l = cv.take<uint16_t>(rg * k2);
-    const size_t o2s = cv.take<float>((size_t)s.npw);
-    const size_t ocm = cv.take<float>((size_t)s.npw);
-    CUDA_TRY(c, dalloc(&s.tc_mem, cv.off));
-    // padding rows and the K padding of Pr^T must read as zero
-    CUDA_TRY(c, cudaMemsetAsync(s.tc_mem, 0, cv.off, st));
-    s.tc_proj = TcOperand{s.tc_mem + o1h, s.tc_mem + o1l, reinterpret_cast<float*>(s.tc_mem + o1s), k1};
-    s.tc_expand = TcOperand{s.tc_mem + o2h, s.tc_mem + o2l, reinterpret_cast<float*>(s.tc_mem + o2s), k2};
+    // by rows: the distinct (radial function, lm) pairs of the projectors
+    std::vector<int2> prow((size_t)s.P), byinfo;
+    std::map<std::pair<int, int>, int> at;
+    for (int p = 0; p < s.P; ++p) {
+        const ProjRow& r = s.rows[(size_t)p];
+        const std::pair<int, int> key(r.rad, r.l * r.l + r.l + r.m);
+        auto it = at.find(key);
+        if (it == at.end()) {
+            it = at.emplace(key, (int)byinfo.size()).first;
+            byinfo.push_back(make_int2(key.first, key.second));
+        }
+        prow[(size_t)p] = make_int2(r.atom, it->second);
+    }
+    const int nby = (int)byinfo.size();
+    CUDA_TRY(c, dalloc(&s.tc_mem, tc_gen_bytes(s.P, s.npw, nby, c->natom)));
     int h = c->prof.open(PH_BUILD, st);
-    CUDA_TRY(c, tc_build_proj_operands(s.pr32, s.P, s.npw, fmt == 0, &s.tc_proj, &s.tc_expand,
-                                       reinterpret_cast<float*>(s.tc_mem + ocm), st));
-    c->prof.close(h, st);
+    CUDA_TRY(c, tc_build_gen(s.tc_mem, s.P, s.npw, prow.data(), byinfo.data(), nby, c->natom, s.d_beta, s.d_ylm,
+                             s.d_sf, fmt == 0, &s.tcgen, st));
+    c->prof.close(h, st, 4);
+    s.tc_proj = TcOperand{nullptr, nullptr, const_cast<float*>(s.tcgen.p_inv), tc_round_k(2 * (size_t)s.npw)};
+    s.tc_expand = TcOperand{nullptr, nullptr, const_cast<float*>(s.tcgen.g_inv), tc_round_k(2 * (size_t)s.P)};
     s.tc_fmt = fmt;
     return HPSI_OK;
 }
@@ -641,7 +644,7 @@ static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi
     CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &t.B1, t.rowmax, st, have_max));
     c->prof.close(h, st, (have_max ? 1 : 2) + zero_rows);
     CUDA_TRY(c, tc_projection(s.tc_proj, s.P, t.B1, nb, t.ns, fp16, t.part, s.d_lam, s.P, t.W, c->d_err, st,
-                              &c->prof, t.eterm, e_nl));
+                              &c->prof, t.eterm, e_nl, &s.tcgen));
     h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_w_operand(t.W, s.P, nb, fp16, &t.B2, t.rowmax, st));
     c->prof.close(h, st, 2 + zero_rows);
@@ -653,7 +656,8 @@ static int tc_nonlocal_expand(hpsi_ctx* c, KSlot& s, int nb, double2* hpsi, unsi
                               bool energy, const float2* add32)
 {
     TcNl t = tc_layout(s, nb, ws, energy);
-    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, t.B2, nb, s.tc_fmt == 0, hpsi, c->d_err, st, &c->prof, add32));
+    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, t.B2, nb, s.tc_fmt == 0, hpsi, c->d_err, st, &c->prof, add32,
+                             &s.tcgen));
     return HPSI_OK;
 }
 

@@ -280,8 +280,9 @@ __global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
     const int pr = (threadIdx.x >> 5) * 16 + (threadIdx.x & 15);
     const bool odd = (threadIdx.x >> 4) & 1;
     float2 v[H];
-    // z (rows in use), G->r, in place
-    {
+    // z (rows in use), G->r, in place; a warp with no row in use skips it
+    // (warp-uniform: both lanes of every pair are in the same warp)
+    if (__any_sync(0xffffffffu, pr < nrows)) {
         const bool on = pr < nrows;
         float2* row = pl + (on ? rows.row(pr) : 0) * NP;
 #pragma unroll
@@ -356,8 +357,8 @@ __global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
         }
     }
     __syncthreads();
-    // z (rows in use), r->G, in place
-    {
+    // z (rows in use), r->G, in place; a warp with no row in use skips it
+    if (__any_sync(0xffffffffu, pr < nrows)) {
         const bool on = pr < nrows;
         float2* row = pl + (on ? rows.row(pr) : 0) * NP;
 #pragma unroll

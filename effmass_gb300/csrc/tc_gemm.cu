@@ -180,21 +180,249 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
 }
 
 struct TcSmem {
-    uint64_t full[STAGES];
+    uint64_t full[STAGES];   // the stage's bulk copies have landed
+    uint64_t gfull[STAGES];  // generated A: the generator threads have written the stage's A pieces
     uint64_t empty[STAGES];
     uint64_t done;
     uint32_t tmem_base;
     uint32_t abort_flag;
 };
 
+// ---- generated projector tiles (GEN) ---------------------------------------
+// The A operand of the projection (Pr [P][2 npw]) or of the expansion
+// (Pr^T [npw][2 P]) is written into each stage's shared memory by the eight
+// epilogue warps, which are otherwise idle during the main loop: Pr[p][G] =
+// by[j(p)][G] * sf[a(p)][G] (TcGen), times the row's power-of-two split
+// scale, split into hi + lo in the swizzled K-major layout of the copied
+// tiles (16 complex values of a row per 32-deep stage).  The table loads of
+// two stages ahead are in flight while a stage is split and stored.
+constexpr int GEN_THREADS = 256;
+constexpr int TC_THREADS = 64 + GEN_THREADS;  // producer warp, MMA warp, 8 epilogue / generator warps
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// make this thread's generic-proxy shared-memory writes visible to the tensor cores
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// hi + lo pieces of two consecutive K elements (a at the lower address)
+template <typename T>
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t& hi, uint32_t& lo);
+template <>
+__device__ __forceinline__ void split_pair<__half>(float a, float b, uint32_t& hi, uint32_t& lo)
+{
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+template <>
+__device__ __forceinline__ void split_pair<__nv_bfloat16>(float a, float b, uint32_t& hi, uint32_t& lo)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+// Wait until stage s may be overwritten (phase ph of its empty barrier).  The
+// decision to go on is taken by the whole warp (shuffles follow).
+__device__ __forceinline__ bool gen_wait_empty(TcSmem* sh, int s, uint32_t ph, int* err)
+{
+    bool ok = mbar_wait_abort(&sh->empty[s], ph ^ 1, &sh->abort_flag);
+    if (!ok && !*(volatile uint32_t*)&sh->abort_flag) { atomicExch(err, 4); sh->abort_flag = 1; }
+    ok = ok && !*(volatile uint32_t*)&sh->abort_flag;
+    return __all_sync(0xffffffffu, ok);
+}
+
+// every lane fences its own stores for the tensor cores; after the warp
+// barrier (which orders the lanes' stores before lane 0) one arrival per warp
+__device__ __forceinline__ void gen_publish(TcSmem* sh, int s)
+{
+    fence_proxy_async_smem();
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&sh->gfull[s]);
+}
+
+// Projection operand (rows = projectors, K pairs = G).  Lane l of generator
+// warp w (0..7) writes the 16-byte chunk c = l & 3 (G 4c .. 4c+3 of the
+// stage) of tile rows 8 w + (l >> 2) and 64 + 8 w + (l >> 2): float4 table
+// loads of 64- and 128-byte row pieces, and stores of which each group of 8
+// lanes fills two whole 64-byte rows (all 32 banks).
+template <typename T>
+struct GenRows {
+    int bo[2], fo[2], so[2];
+    float sc[2];
+    float4 b[3][2], f[3][4];
+    __device__ __forceinline__ void load(const TcGen& gen, int buf, int g)
+    {
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            b[buf][i] = __ldg(reinterpret_cast<const float4*>(gen.by + bo[i] + g));
+            const float4* f4 = reinterpret_cast<const float4*>(gen.sf + fo[i] + g);
+            f[buf][2 * i] = __ldg(f4);
+            f[buf][2 * i + 1] = __ldg(f4 + 1);
+        }
+    }
+    __device__ __forceinline__ bool emit(TcSmem* sh, unsigned char* tiles, int it, int buf, int* err)
+    {
+        uint4 hi[2], lo[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const float4 bv = b[buf][i];
+            const float4 f0 = f[buf][2 * i], f1 = f[buf][2 * i + 1];
+            const float s = sc[i];  // a power of two (or 0 past the last row): exact
+            const float b0 = bv.x * s, b1 = bv.y * s, b2 = bv.z * s, b3 = bv.w * s;
+            split_pair<T>(b0 * f0.x, b0 * f0.y, hi[i].x, lo[i].x);
+            split_pair<T>(b1 * f0.z, b1 * f0.w, hi[i].y, lo[i].y);
+            split_pair<T>(b2 * f1.x, b2 * f1.y, hi[i].z, lo[i].z);
+            split_pair<T>(b3 * f1.z, b3 * f1.w, hi[i].w, lo[i].w);
+        }
+        const int s = it % STAGES;
+        if (!gen_wait_empty(sh, s, (it / STAGES) & 1, err)) return false;
+        unsigned char* st = tiles + s * STAGE_BYTES;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            *reinterpret_cast<uint4*>(st + so[i]) = hi[i];
+            *reinterpret_cast<uint4*>(st + A_TILE + so[i]) = lo[i];
+        }
+        gen_publish(sh, s);
+        return true;
+    }
+};
+
+template <typename T>
+__device__ void gen_loop_rows(const TcGen& gen, TcSmem* sh, unsigned char* tiles, int m0, int kt0, int nk, int t,
+                              int* err)
+{
+    const int lane = t & 31, w = t >> 5, c = lane & 3;
+    GenRows<T> R;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int r = 64 * i + 8 * w + (lane >> 2);
+        const int p = m0 + r;
+        const int2 o = p < gen.P ? __ldg(gen.rows + p) : make_int2(0, gen.zero_off);
+        R.fo[i] = o.x;
+        R.bo[i] = o.y;
+        R.sc[i] = p < gen.P ? __ldg(gen.p_scale + p) : 0.f;
+        R.so[i] = 64 * r + 16 * (c ^ ((r >> 1) & 3));
+    }
+    const int g0 = 16 * kt0 + 4 * c;
+    if (nk > 0) R.load(gen, 0, g0);
+    if (nk > 1) R.load(gen, 1, g0 + 16);
+    for (int it = 0; it < nk; it += 3) {
+        if (it + 2 < nk) R.load(gen, 2, g0 + 16 * (it + 2));
+        if (!R.emit(sh, tiles, it, 0, err) || it + 1 >= nk) break;
+        if (it + 3 < nk) R.load(gen, 0, g0 + 16 * (it + 3));
+        if (!R.emit(sh, tiles, it + 1, 1, err) || it + 2 >= nk) break;
+        if (it + 4 < nk) R.load(gen, 1, g0 + 16 * (it + 4));
+        if (!R.emit(sh, tiles, it + 2, 2, err)) break;
+    }
+}
+
+// Expansion operand (rows = G, K pairs = projectors).  Thread t writes rows
+// G = m0 + 2 (t & 63) and the next, projectors 4 (t >> 6) .. +3 of each stage
+// (the 16-byte chunk t >> 6 of both rows): float2 / float4 table loads of
+// two consecutive G, coalesced over the warp, and warp-uniform 32-byte loads
+// of the projectors' table offsets.  Lanes store their two rows in an order
+// chosen so that each group of 8 lanes writes 8 distinct bank quads.
+template <typename T>
+struct GenCols {
+    int4 o[3][2];    // offsets (sf, by) of the 4 projectors, two per int4
+    float2 b[3][4];  // by of each projector at the two rows
+    float4 f[3][4];  // sf of each projector at the two rows
+    __device__ __forceinline__ void load_offsets(const TcGen& gen, int buf, int p0)
+    {
+        const int4* src = reinterpret_cast<const int4*>(gen.rows + p0);
+        o[buf][0] = __ldg(src);
+        o[buf][1] = __ldg(src + 1);
+    }
+    __device__ __forceinline__ void load(const TcGen& gen, int buf, int obuf, int g)
+    {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int4 v = o[obuf][q];
+            b[buf][2 * q] = __ldg(reinterpret_cast<const float2*>(gen.by + v.y + g));
+            f[buf][2 * q] = __ldg(reinterpret_cast<const float4*>(gen.sf + v.x + g));
+            b[buf][2 * q + 1] = __ldg(reinterpret_cast<const float2*>(gen.by + v.w + g));
+            f[buf][2 * q + 1] = __ldg(reinterpret_cast<const float4*>(gen.sf + v.z + g));
+        }
+    }
+    __device__ __forceinline__ bool emit(TcSmem* sh, unsigned char* tiles, int it, int buf, float sc0, float sc1,
+                                         int r0, int c, int first, int* err)
+    {
+        uint4 h0, l0, h1, l1;  // rows r0, r0 + 1
+        uint32_t* hp0 = reinterpret_cast<uint32_t*>(&h0);
+        uint32_t* lp0 = reinterpret_cast<uint32_t*>(&l0);
+        uint32_t* hp1 = reinterpret_cast<uint32_t*>(&h1);
+        uint32_t* lp1 = reinterpret_cast<uint32_t*>(&l1);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float2 bv = b[buf][i];
+            const float4 fv = f[buf][i];
+            const float b0 = bv.x * sc0, b1 = bv.y * sc1;  // power-of-two scales: exact
+            split_pair<T>(b0 * fv.x, b0 * fv.y, hp0[i], lp0[i]);
+            split_pair<T>(b1 * fv.z, b1 * fv.w, hp1[i], lp1[i]);
+        }
+        const int s = it % STAGES;
+        if (!gen_wait_empty(sh, s, (it / STAGES) & 1, err)) return false;
+        unsigned char* st = tiles + s * STAGE_BYTES;
+        const int ra = r0 + first, rb = r0 + 1 - first;
+        const int oa = 64 * ra + 16 * (c ^ ((ra >> 1) & 3)), ob = 64 * rb + 16 * (c ^ ((rb >> 1) & 3));
+        *reinterpret_cast<uint4*>(st + oa) = first ? h1 : h0;
+        *reinterpret_cast<uint4*>(st + A_TILE + oa) = first ? l1 : l0;
+        *reinterpret_cast<uint4*>(st + ob) = first ? h0 : h1;
+        *reinterpret_cast<uint4*>(st + A_TILE + ob) = first ? l0 : l1;
+        gen_publish(sh, s);
+        return true;
+    }
+};
+
+template <typename T>
+__device__ void gen_loop_cols(const TcGen& gen, TcSmem* sh, unsigned char* tiles, int m0, int kt0, int nk, int t,
+                              int* err)
+{
+    const int rp = t & 63, c = t >> 6;
+    const int r0 = 2 * rp;
+    const int g = m0 + r0;  // g + 1 < ldg (a multiple of 128)
+    // 1 past npw, where the tables are zero
+    const float sc0 = __ldg(gen.g_scale + g), sc1 = __ldg(gen.g_scale + g + 1);
+    const int first = (rp >> 2) & 1;
+    const int p0 = 16 * kt0 + 4 * c;
+    GenCols<T> C;
+    // offsets run one stage ahead of the values, the values two ahead of the stores
+    if (nk > 0) C.load_offsets(gen, 0, p0);
+    if (nk > 1) C.load_offsets(gen, 1, p0 + 16);
+    if (nk > 0) C.load(gen, 0, 0, g);
+    if (nk > 2) C.load_offsets(gen, 2, p0 + 32);
+    if (nk > 1) C.load(gen, 1, 1, g);
+    for (int it = 0; it < nk; it += 3) {
+        if (it + 3 < nk) C.load_offsets(gen, 0, p0 + 16 * (it + 3));
+        if (it + 2 < nk) C.load(gen, 2, 2, g);
+        if (!C.emit(sh, tiles, it, 0, sc0, sc1, r0, c, first, err) || it + 1 >= nk) break;
+        if (it + 4 < nk) C.load_offsets(gen, 1, p0 + 16 * (it + 4));
+        if (it + 3 < nk) C.load(gen, 0, 0, g);
+        if (!C.emit(sh, tiles, it + 1, 1, sc0, sc1, r0, c, first, err) || it + 2 >= nk) break;
+        if (it + 5 < nk) C.load_offsets(gen, 2, p0 + 16 * (it + 5));
+        if (it + 4 < nk) C.load(gen, 1, 1, g);
+        if (!C.emit(sh, tiles, it + 2, 2, sc0, sc1, r0, c, first, err)) break;
+    }
+}
+
 // Epilogue modes
-//   0: projection partials  part[z][m][n] = C * 2^-(sa[m] + sb[n])   (row-major, ldp = N)
-//   1: expansion            hpsi[b][g] += (C[g][re] + i C[g][im]) * 2^-(sa[g] + sb[b])
-template <int MODE>
-__global__ void __launch_bounds__(192, 1)
+//   0: projection partials  part[z][n][m] = C[m][n] * sa[m] * sb[n]   (column-major per split)
+//   1: expansion            hpsi[b][g] += (C[g][re] + i C[g][im]) * sa[g] * sb[b]
+// GEN: the A operand is generated in shared memory from gen (GEN_FP16 selects
+// the FP16 split, else BF16) instead of bulk-copied from Ah / Al.
+template <int MODE, bool GEN = false, bool GEN_FP16 = true>
+__global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const unsigned char* __restrict__ Ah, const unsigned char* __restrict__ Al,
                    const unsigned char* __restrict__ Bh, const unsigned char* __restrict__ Bl, TcEpilogue ep, int M,
-                   int N, int ktiles_total, int ktiles_per_split, uint32_t idesc, int* err)
+                   int N, int ktiles_total, int ktiles_per_split, uint32_t idesc, int* err, TcGen gen = TcGen{})
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned tile area
@@ -211,6 +439,7 @@ __global__ void __launch_bounds__(192, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->gfull[s], GEN ? GEN_THREADS / 32 : 1);
             mbar_init(&sh->empty[s], 1);
         }
         mbar_init(&sh->done, 1);
@@ -230,8 +459,8 @@ __global__ void __launch_bounds__(192, 1)
     if (warp == 0 && lane == 0) {
         // ---- bulk-copy producer: tiles (row block, k block) of the tiled operands
         const size_t KT = (size_t)ktiles_total;
-        const unsigned char* ah = Ah + (size_t)blockIdx.x * KT * A_TILE;
-        const unsigned char* al = Al + (size_t)blockIdx.x * KT * A_TILE;
+        const unsigned char* ah = GEN ? nullptr : Ah + (size_t)blockIdx.x * KT * A_TILE;
+        const unsigned char* al = GEN ? nullptr : Al + (size_t)blockIdx.x * KT * A_TILE;
         const unsigned char* bh = Bh + (size_t)(2 * blockIdx.y) * KT * A_TILE;  // 128-row blocks n0/128, +1
         const unsigned char* bl = Bl + (size_t)(2 * blockIdx.y) * KT * A_TILE;
         int issued = 0;
@@ -244,10 +473,12 @@ __global__ void __launch_bounds__(192, 1)
             }
             if (*(volatile uint32_t*)&sh->abort_flag) break;
             unsigned char* st = tiles + s * STAGE_BYTES;
-            mbar_arrive_expect_tx(&sh->full[s], STAGE_BYTES);
+            mbar_arrive_expect_tx(&sh->full[s], GEN ? 2 * B_TILE : STAGE_BYTES);
             const size_t kt = (size_t)(kt0 + it);
-            bulk_load(st, ah + kt * A_TILE, A_TILE, &sh->full[s]);
-            bulk_load(st + A_TILE, al + kt * A_TILE, A_TILE, &sh->full[s]);
+            if (!GEN) {
+                bulk_load(st, ah + kt * A_TILE, A_TILE, &sh->full[s]);
+                bulk_load(st + A_TILE, al + kt * A_TILE, A_TILE, &sh->full[s]);
+            }
             bulk_load(st + 2 * A_TILE, bh + kt * A_TILE, A_TILE, &sh->full[s]);
             bulk_load(st + 3 * A_TILE, bh + (KT + kt) * A_TILE, A_TILE, &sh->full[s]);
             bulk_load(st + 2 * A_TILE + B_TILE, bl + kt * A_TILE, A_TILE, &sh->full[s]);
@@ -264,7 +495,12 @@ __global__ void __launch_bounds__(192, 1)
         for (int it = 0; it < nk; ++it) {
             const int s = it % STAGES;
             const uint32_t ph = (it / STAGES) & 1;
-            if (!mbar_wait_n(&sh->full[s], ph, lim)) { atomicExch(err, 2); sh->abort_flag = 1; ok = false; break; }
+            if (!mbar_wait_n(&sh->full[s], ph, lim) || (GEN && !mbar_wait_n(&sh->gfull[s], ph, lim))) {
+                atomicExch(err, 2);
+                sh->abort_flag = 1;
+                ok = false;
+                break;
+            }
             tc_fence_after();
             const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
             const uint64_t ah = sdesc_sw64(st), al = sdesc_sw64(st + A_TILE);
@@ -285,8 +521,16 @@ __global__ void __launch_bounds__(192, 1)
         (void)ok;
         tc_commit(&sh->done);  // accumulator final (arrives after all prior MMAs)
     } else if (warp >= 2) {
-        // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
+        // ---- generated A (GEN): these warps write each stage's A pieces first
+        using GT = typename std::conditional<GEN_FP16, __half, __nv_bfloat16>::type;
+        if constexpr (GEN) {
+            if (MODE == 0) gen_loop_rows<GT>(gen, sh, tiles, m0, kt0, nk, threadIdx.x - 64, err);
+            else gen_loop_cols<GT>(gen, sh, tiles, m0, kt0, nk, threadIdx.x - 64, err);
+        }
+        // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31; warps 2-5
+        // take the first half of the columns, warps 6-9 the second
         const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int row = m0 + q * 32 + lane;
         bool ok = mbar_wait(&sh->done, 0);
         tc_fence_after();
@@ -298,9 +542,11 @@ __global__ void __launch_bounds__(192, 1)
             const float sa = (row < M) ? ep.sa_scale[row] : 0.f;
             const bool two = nk > 1;  // the odd accumulator holds data only with two or more k-tiles
             if (MODE == 0) {
-                float* out = ep.part + ((size_t)blockIdx.z * M + row) * (size_t)N + n0;
+                // partials column-major within a split ([z][N][M]): the 32 lanes
+                // (consecutive rows) of a warp store one 128-byte line per column
+                float* out = ep.part + ((size_t)blockIdx.z * N + n0) * (size_t)M + row;
 #pragma unroll 1
-                for (int c0 = 0; c0 < BN; c0 += 32) {
+                for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
                     float v[32], w[32];
                     tmem_ld32(tbase + c0, v);
                     if (two) {
@@ -315,14 +561,14 @@ __global__ void __launch_bounds__(192, 1)
                         for (int i = 0; i < 32; ++i) sb[i] = (n0 + c0 + i < N) ? ep.sb_scale[n0 + c0 + i] : 0.f;
 #pragma unroll
                         for (int i = 0; i < 32; ++i)
-                            if (n0 + c0 + i < N) out[c0 + i] = v[i] * sa * sb[i];
+                            if (n0 + c0 + i < N) out[(size_t)(c0 + i) * M] = v[i] * sa * sb[i];
                     }
                 }
             } else {
                 // columns [0,128): real parts of bands 128*blockIdx.y + j, [128,256): imaginary
                 const bool add = ep.add32 != nullptr;
 #pragma unroll 1
-                for (int c0 = 0; c0 < 128; c0 += 32) {
+                for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
                     float re[32], im[32], w[32];
                     tmem_ld32(tbase + c0, re);
                     tmem_ld32(tbase + 128 + c0, im);
@@ -335,18 +581,18 @@ __global__ void __launch_bounds__(192, 1)
                         for (int i = 0; i < 32; ++i) im[i] += w[i];
                     }
                     if (row < M) {
-                        // read-modify-write of hpsi in groups of 16 bands: all loads
+                        // read-modify-write of hpsi in groups of 8 bands: all loads
                         // of a group are issued before its stores, so the HBM round
                         // trips overlap instead of following one another band by band
                         const int b0 = blockIdx.y * 128 + c0;
 #pragma unroll
-                        for (int h0 = 0; h0 < 32; h0 += 16) {
-                            double2 o[16];
-                            float2 ad[16];
-                            float f[16];
+                        for (int h0 = 0; h0 < 32; h0 += 8) {
+                            double2 o[8];
+                            float2 ad[8];
+                            float f[8];
                             // loads only (predicated, no use), so that they all overlap
 #pragma unroll
-                            for (int i = 0; i < 16; ++i) {
+                            for (int i = 0; i < 8; ++i) {
                                 const int b = b0 + h0 + i;
                                 const size_t at = (size_t)b * ep.ldh + row;
                                 f[i] = sa * ep.sb_scale[n0 + c0 + h0 + i];
@@ -354,7 +600,7 @@ __global__ void __launch_bounds__(192, 1)
                                 ad[i] = (add && b < ep.nb) ? ep.add32[at] : make_float2(0.f, 0.f);
                             }
 #pragma unroll
-                            for (int i = 0; i < 16; ++i) {
+                            for (int i = 0; i < 8; ++i) {
                                 const int b = b0 + h0 + i;
                                 if (b < ep.nb) {
                                     o[i].x += f2d_bits(fmaf(re[h0 + i], f[i], ad[i].x));
@@ -651,17 +897,22 @@ template <typename CW>
 __global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float* __restrict__ part,
                                    const double* __restrict__ lam, int period, CW* W, double* eterm = nullptr)
 {
-    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (size_t)P * nb) return;
-    const int p = (int)(idx / nb), b = (int)(idx % nb);
+    // consecutive threads take consecutive projectors: coalesced reads of the
+    // column-major partials part[z][n][p]
+    const size_t t_idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t_idx >= (size_t)P * nb) return;
+    const int p = (int)(t_idx % P), b = (int)(t_idx / P);
+    const size_t idx = (size_t)p * nb + b;  // W[p][b]
     const int t = b / 128, j = b % 128;
     const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
+    const size_t zs = (size_t)N * P;
+    const float* pre = part + cre * P + p;
+    const float* pim = part + cim * P + p;
     if constexpr (std::is_same<CW, float2>::value) {
         Sum2f re, im;  // complex64 W: compensated FP32 sums, no FP64 pipe
         for (int z = 0; z < nsplit; ++z) {
-            const float* row = part + ((size_t)z * P + p) * N;
-            re.add(row[cre]);
-            im.add(row[cim]);
+            re.add(pre[z * zs]);
+            im.add(pim[z * zs]);
         }
         const float f = lam ? d2f_bits(lam[p % period]) : 1.f;
         W[idx] = make_float2(f * re.value(), f * im.value());
@@ -674,9 +925,8 @@ __global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float
     }
     double sr = 0.0, si = 0.0;
     for (int z = 0; z < nsplit; ++z) {
-        const float* row = part + ((size_t)z * P + p) * N;
-        sr += row[cre];
-        si += row[cim];
+        sr += pre[z * zs];
+        si += pim[z * zs];
     }
     const double f = lam ? lam[p % period] : 1.0;
     W[idx] = from_c128<CW>(make_double2(f * sr, f * si));
@@ -839,9 +1089,24 @@ int tc_proj_splits(int P, int nb, size_t ldk)
     return best;
 }
 
-// A: rows M, B: rows N (= tc_band_rows(nb)); one launch
+template <int MODE, bool GEN, bool GEN_FP16>
+static cudaError_t launch_tc_t(dim3 grid, size_t smem, cudaStream_t st, const unsigned char* ah,
+                               const unsigned char* al, const unsigned char* bh, const unsigned char* bl,
+                               const TcEpilogue& ep, int M, int N, int ktiles, int per, uint32_t idesc, int* err,
+                               const TcGen& gen)
+{
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<MODE, GEN, GEN_FP16>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    tc_gemm_kernel<MODE, GEN, GEN_FP16><<<grid, TC_THREADS, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err,
+                                                                  gen);
+    return cudaGetLastError();
+}
+
+// A: rows M, B: rows N (= tc_band_rows(nb)); one launch.  With gen the A
+// operand is generated from those tables (A.hi / A.lo unused).
 static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperand& B, int N, int nsplit, bool fp16,
-                             const TcEpilogue& ep, int* err, cudaStream_t st)
+                             const TcEpilogue& ep, int* err, cudaStream_t st, const TcGen* gen = nullptr)
 {
     if (A.ldk != B.ldk || A.ldk % BK) return cudaErrorInvalidValue;
     const int ktiles = (int)(A.ldk / BK);
@@ -852,22 +1117,24 @@ static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperan
     const uint32_t idesc = idesc_f16(BM, BN, fp16 ? 0u : 1u);
     const unsigned char *ah = (const unsigned char*)A.hi, *al = (const unsigned char*)A.lo;
     const unsigned char *bh = (const unsigned char*)B.hi, *bl = (const unsigned char*)B.lo;
-    cudaError_t e;
-    if (mode == 0) {
-        if ((e = cudaFuncSetAttribute(tc_gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
-        tc_gemm_kernel<0><<<grid, 192, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err);
-    } else {
-        if ((e = cudaFuncSetAttribute(tc_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
-        tc_gemm_kernel<1><<<grid, 192, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err);
+    if (!gen) {
+        const TcGen none{};
+        return mode == 0 ? launch_tc_t<0, false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc,
+                                                       err, none)
+                         : launch_tc_t<1, false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc,
+                                                       err, none);
     }
-    return cudaGetLastError();
+    if (mode == 0)
+        return fp16 ? launch_tc_t<0, true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, *gen)
+                    : launch_tc_t<0, true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err,
+                                                  *gen);
+    return fp16 ? launch_tc_t<1, true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, *gen)
+                : launch_tc_t<1, true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, *gen);
 }
 
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                           const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof,
-                          double* eterm, double* e_nl)
+                          double* eterm, double* e_nl, const TcGen* gen)
 {
     const int N = tc_band_rows(nb);
     TcEpilogue ep{};
@@ -875,7 +1142,7 @@ cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb,
     ep.sa_scale = A.inv_scale;
     ep.sb_scale = B.inv_scale;
     int h = prof->open(PH_PROJ, st);
-    cudaError_t e = launch_tc(0, A, P, B, N, nsplit, fp16, ep, err, st);
+    cudaError_t e = launch_tc(0, A, P, B, N, nsplit, fp16, ep, err, st, gen);
     prof->close(h, st);
     if (e) return e;
     const int ktiles = (int)(A.ldk / BK);
@@ -919,7 +1186,7 @@ cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, 
 }
 
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi,
-                         int* err, cudaStream_t st, Prof* prof, const float2* add32)
+                         int* err, cudaStream_t st, Prof* prof, const float2* add32, const TcGen* gen)
 {
     const int N = tc_band_rows(nb);
     TcEpilogue ep{};
@@ -930,9 +1197,143 @@ cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb
     ep.sa_scale = A.inv_scale;
     ep.sb_scale = B.inv_scale;
     int h = prof->open(PH_EXPAND, st);
-    cudaError_t e = launch_tc(1, A, npw, B, N, 1, fp16, ep, err, st);
+    cudaError_t e = launch_tc(1, A, npw, B, N, 1, fp16, ep, err, st, gen);
     prof->close(h, st);
     return e;
+}
+
+// ---------------------------------------------------------------- generator tables
+// by[j][g] = beta_rad(j)[g] * Y_lm(j)[g] rounded to FP32 (zero past npw)
+__global__ void gen_by_kernel(const int2* __restrict__ byinfo, const double* __restrict__ beta,
+                              const double* __restrict__ ylm, int npw, int ldg, float* __restrict__ by)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (g >= ldg) return;
+    const int2 bi = byinfo[j];
+    by[(size_t)j * ldg + g] = g < npw ? (float)(beta[(size_t)bi.x * npw + g] * ylm[(size_t)bi.y * npw + g]) : 0.f;
+}
+
+__global__ void gen_sf_kernel(const double2* __restrict__ sf, int npw, int ldg, float2* __restrict__ out)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.y;
+    if (g >= ldg) return;
+    float2 v = make_float2(0.f, 0.f);
+    if (g < npw) {
+        const double2 x = sf[(size_t)a * npw + g];
+        v = make_float2((float)x.x, (float)x.y);
+    }
+    out[(size_t)a * ldg + g] = v;
+}
+
+// rmax[j] = max_g |by[j][g]|: bounds |Re|, |Im| of every projector row on by row j (|S| = 1)
+__global__ void gen_rowmax_kernel(const float* __restrict__ by, int ldg, float* __restrict__ rmax)
+{
+    __shared__ float red[32];
+    const float* row = by + (size_t)blockIdx.x * ldg;
+    float mx = 0.f;
+    for (int g = threadIdx.x; g < ldg; g += blockDim.x) mx = fmaxf(mx, fabsf(row[g]));
+    mx = block_max(mx, red);
+    if (threadIdx.x == 0) rmax[blockIdx.x] = mx;
+}
+
+// split scales: per G row of the transposed operand (max over by rows) and per projector row
+__global__ void gen_scales_kernel(const float* __restrict__ by, int nby, int ldg, const int2* __restrict__ rows,
+                                  int P, const float* __restrict__ rmax, bool fp16, float* g_scale, float* g_inv,
+                                  float* p_scale, float* p_inv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ldg) {
+        float mx = 0.f;
+        for (int j = 0; j < nby; ++j) mx = fmaxf(mx, fabsf(by[(size_t)j * ldg + i]));
+        const float sc = row_scale(mx, fp16);
+        g_scale[i] = sc;
+        g_inv[i] = 1.f / sc;
+    }
+    if (i < P) {
+        const float sc = row_scale(rmax[rows[i].y / ldg], fp16);
+        p_scale[i] = sc;
+        p_inv[i] = 1.f / sc;
+    }
+}
+
+// leading dimension of the tables: whole 128-row tiles of the expansion operand
+static int gen_ldg(int npw) { return (int)tc_rows_pad((size_t)npw); }
+// entries of the offset table: the projection's K pairs (P rounded up to 16)
+static int gen_ppad(int P) { return (int)(tc_round_k(2 * (size_t)P) / 2); }
+
+struct GenLayout {
+    size_t by, sf, rows, ps, pi, gs, gi, rmax, byinfo, bytes;
+};
+
+static GenLayout gen_layout(int P, int npw, int nby, int natom)
+{
+    const size_t ldg = (size_t)gen_ldg(npw);
+    GenLayout o;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    o.by = take((size_t)(nby + 1) * ldg * sizeof(float));  // + a zero row
+    o.sf = take((size_t)natom * ldg * sizeof(float2));
+    o.rows = take((size_t)gen_ppad(P) * sizeof(int2));
+    o.ps = take((size_t)P * sizeof(float));
+    o.pi = take((size_t)P * sizeof(float));
+    o.gs = take(ldg * sizeof(float));
+    o.gi = take(ldg * sizeof(float));
+    o.rmax = take((size_t)nby * sizeof(float));
+    o.byinfo = take((size_t)nby * sizeof(int2));
+    o.bytes = off;
+    return o;
+}
+
+size_t tc_gen_bytes(int P, int npw, int nby, int natom) { return gen_layout(P, npw, nby, natom).bytes; }
+
+cudaError_t tc_build_gen(unsigned char* mem, int P, int npw, const int2* h_rows, const int2* h_byinfo, int nby,
+                         int natom, const double* beta, const double* ylm, const double2* sf, bool fp16, TcGen* out,
+                         cudaStream_t st)
+{
+    if (P <= 0 || npw <= 0 || nby <= 0 || natom <= 0) return cudaErrorInvalidValue;
+    const GenLayout o = gen_layout(P, npw, nby, natom);
+    const int ldg = gen_ldg(npw);
+    // element offsets of table rows are 32-bit
+    if ((double)(std::max(nby + 1, natom)) * ldg >= 2147483647.0) return cudaErrorInvalidValue;
+    const int ppad = gen_ppad(P);
+    // (sf offset, by offset) per projector; past P the zero by row
+    std::vector<int2> off((size_t)ppad, make_int2(0, nby * ldg));
+    for (int p = 0; p < P; ++p) off[(size_t)p] = make_int2(h_rows[p].x * ldg, h_rows[p].y * ldg);
+    TcGen g;
+    g.by = reinterpret_cast<const float*>(mem + o.by);
+    g.sf = reinterpret_cast<const float2*>(mem + o.sf);
+    g.rows = reinterpret_cast<const int2*>(mem + o.rows);
+    g.p_scale = reinterpret_cast<const float*>(mem + o.ps);
+    g.p_inv = reinterpret_cast<const float*>(mem + o.pi);
+    g.g_scale = reinterpret_cast<const float*>(mem + o.gs);
+    g.g_inv = reinterpret_cast<const float*>(mem + o.gi);
+    g.P = P;
+    g.npw = npw;
+    g.ldg = ldg;
+    g.zero_off = nby * ldg;
+    cudaError_t e;
+    int2* rows = reinterpret_cast<int2*>(mem + o.rows);
+    int2* byinfo = reinterpret_cast<int2*>(mem + o.byinfo);
+    if ((e = cudaMemcpyAsync(rows, off.data(), (size_t)ppad * sizeof(int2), cudaMemcpyHostToDevice, st))) return e;
+    if ((e = cudaMemcpyAsync(byinfo, h_byinfo, (size_t)nby * sizeof(int2), cudaMemcpyHostToDevice, st))) return e;
+    float* by = reinterpret_cast<float*>(mem + o.by);
+    float* rmax = reinterpret_cast<float*>(mem + o.rmax);
+    if ((e = cudaMemsetAsync(by + (size_t)nby * ldg, 0, (size_t)ldg * sizeof(float), st))) return e;
+    gen_by_kernel<<<dim3(ceil_div(ldg, 256), nby), 256, 0, st>>>(byinfo, beta, ylm, npw, ldg, by);
+    gen_sf_kernel<<<dim3(ceil_div(ldg, 256), natom), 256, 0, st>>>(sf, npw, ldg, reinterpret_cast<float2*>(mem + o.sf));
+    gen_rowmax_kernel<<<nby, 256, 0, st>>>(by, ldg, rmax);
+    gen_scales_kernel<<<ceil_div(std::max(ldg, P), 256), 256, 0, st>>>(
+        by, nby, ldg, rows, P, rmax, fp16, reinterpret_cast<float*>(mem + o.gs), reinterpret_cast<float*>(mem + o.gi),
+        reinterpret_cast<float*>(mem + o.ps), reinterpret_cast<float*>(mem + o.pi));
+    if ((e = cudaGetLastError())) return e;
+    *out = g;
+    return cudaSuccess;
 }
 
 int tc_chain_splits(size_t ldk, int chain_k)

@@ -14,7 +14,7 @@ struct TcOperand {
 };
 
 struct TcEpilogue {
-    float* part;               // mode 0: [splits][M][N] partial sums
+    float* part;               // mode 0: [splits][N][M] partial sums
     double2* hpsi;             // mode 1: output, [nb][ldh]
     int ldh;
     int nb;
@@ -22,6 +22,34 @@ struct TcEpilogue {
     const float* sb_scale;     // per B row
     const float2* add32;       // mode 1: optional [nb][ldh] term added with the product
 };
+
+// Tables from which the generated-operand variant of the projector GEMMs
+// writes its A tiles in shared memory: Pr[p][G] = by[j(p)][G] * sf[a(p)][G],
+// scaled by a power of two per row and split like a copied operand.  About
+// 22 MB for the 64-atom cell instead of 2 x 342 MB of pre-split matrices.
+struct TcGen {
+    const float* by = nullptr;       // [nby + 1][ldg] beta_rad(|k+G|) Y_lm(k+G) in FP32, zero for G >= npw
+                                     // and in the last row
+    const float2* sf = nullptr;      // [natom][ldg] structure factors in complex64, zero for G >= npw
+    const int2* rows = nullptr;      // [P rounded up to 16] element offsets (a(p) ldg, j(p) ldg) of
+                                     // projector p's sf and by rows; past P (0, zero_off)
+    const float* p_scale = nullptr;  // [P] split scale of projector row p (projection operand)
+    const float* p_inv = nullptr;    // [P] its inverse
+    const float* g_scale = nullptr;  // [ldg] split scale of row G of the transposed operand (expansion)
+    const float* g_inv = nullptr;    // [ldg] its inverse
+    int P = 0, npw = 0, ldg = 0;     // ldg = npw rounded up to whole 128-row tiles
+    int zero_off = 0;                // element offset of the zero by row
+};
+
+// Device bytes of the generator tables (P projectors over nby distinct
+// (radial function, lm) rows and natom atoms)
+size_t tc_gen_bytes(int P, int npw, int nby, int natom);
+// Build them in mem (tc_gen_bytes): h_rows[p] = (atom, by row), h_byinfo[j] =
+// (radial function, lm index) on the host; beta [nrad][npw], ylm [nlm][npw] and
+// sf [natom][npw] the slot's FP64 tables.
+cudaError_t tc_build_gen(unsigned char* mem, int P, int npw, const int2* h_rows, const int2* h_byinfo, int nby,
+                         int natom, const double* beta, const double* ylm, const double2* sf, bool fp16, TcGen* out,
+                         cudaStream_t st);
 
 size_t tc_round_k(size_t k);   // K padded to the K depth of a pipeline stage
 int tc_chain_splits(size_t ldk, int chain_k);  // splits that keep every split's K depth <= chain_k
@@ -51,14 +79,17 @@ cudaError_t tc_band_operand(const double2* psi, int nb, int npw, bool fp16, TcOp
 cudaError_t tc_w_operand(const float2* W, int P, int nb, bool fp16, TcOperand* B, unsigned* rowmax, cudaStream_t st);
 // W[p][b] = lambda_p * sum_G conj(Pr[p][G]) psi[b][G]  (lam may be null); with e_nl also
 // e_nl[b] = sum_p lambda_p |<p|psi_b>|^2 in FP64 (eterm: P*nb doubles of scratch)
+// With gen the projector operand is generated from those tables (A then only
+// supplies ldk and inv_scale = gen->p_inv).
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                           const double* lam, int period, float2* W, int* err, cudaStream_t st, Prof* prof,
-                          double* eterm = nullptr, double* e_nl = nullptr);
+                          double* eterm = nullptr, double* e_nl = nullptr, const TcGen* gen = nullptr);
 // Row operand [rows][2npw] of a complex128 matrix (psi), for conj(A) B^T GEMMs
 cudaError_t tc_rows_operand(const double2* x, int rows, int npw, bool fp16, TcOperand* A, cudaStream_t st);
 // out[m][n] = sum_G conj(A[m][G]) B[n][G] in complex128 (B a band operand of nb rows)
 cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                          double2* out, int* err, cudaStream_t st);
 // hpsi[b][G] += sum_p W[p][b] Pr[p][G] (+ add32[b][G] when given, summed in FP32 first)
+// (gen as in tc_projection; A.inv_scale = gen->g_inv)
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
-                         cudaStream_t st, Prof* prof, const float2* add32 = nullptr);
+                         cudaStream_t st, Prof* prof, const float2* add32 = nullptr, const TcGen* gen = nullptr);
