@@ -179,11 +179,28 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 struct TcSmem {
     uint64_t full[STAGES];   // the stage's bulk copies have landed
     uint64_t gfull[STAGES];  // generated A: the generator threads have written the stage's A pieces
     uint64_t empty[STAGES];
     uint64_t done;
+    uint64_t tfull[2];       // persistent expansion: accumulator a final
+    uint64_t tempty[2];      // persistent expansion: accumulator a read out by the epilogue warps
+    uint64_t tlast;          // persistent expansion: the CTA's last tile final (one phase)
     uint32_t tmem_base;
     uint32_t abort_flag;
 };
@@ -333,8 +350,8 @@ __device__ void gen_loop_rows(const TcGen& gen, TcSmem* sh, unsigned char* tiles
 template <typename T>
 struct GenCols {
     int4 o[3][2];    // offsets (sf, by) of the 4 projectors, two per int4
-    float2 b[3][4];  // by of each projector at the two rows
-    float4 f[3][4];  // sf of each projector at the two rows
+    float2 b[2][4];  // by of each projector at the two rows
+    float4 f[2][4];  // sf of each projector at the two rows
     __device__ __forceinline__ void load_offsets(const TcGen& gen, int buf, int p0)
     {
         const int4* src = reinterpret_cast<const int4*>(gen.rows + p0);
@@ -382,9 +399,11 @@ struct GenCols {
     }
 };
 
+// it0: the stage counter of the ring at this tile's first k-tile (tiles of a
+// persistent CTA share the ring); false when the kernel aborted
 template <typename T>
-__device__ void gen_loop_cols(const TcGen& gen, TcSmem* sh, unsigned char* tiles, int m0, int kt0, int nk, int t,
-                              int* err)
+__device__ bool gen_loop_cols(const TcGen& gen, TcSmem* sh, unsigned char* tiles, int m0, int kt0, int nk, int t,
+                              int* err, int it0 = 0)
 {
     const int rp = t & 63, c = t >> 6;
     const int r0 = 2 * rp;
@@ -394,31 +413,29 @@ __device__ void gen_loop_cols(const TcGen& gen, TcSmem* sh, unsigned char* tiles
     const int first = (rp >> 2) & 1;
     const int p0 = 16 * kt0 + 4 * c;
     GenCols<T> C;
-    // offsets run one stage ahead of the values, the values two ahead of the stores
+    // offsets run two stages ahead of the stores, the values one
     if (nk > 0) C.load_offsets(gen, 0, p0);
     if (nk > 1) C.load_offsets(gen, 1, p0 + 16);
     if (nk > 0) C.load(gen, 0, 0, g);
-    if (nk > 2) C.load_offsets(gen, 2, p0 + 32);
-    if (nk > 1) C.load(gen, 1, 1, g);
-    for (int it = 0; it < nk; it += 3) {
-        if (it + 3 < nk) C.load_offsets(gen, 0, p0 + 16 * (it + 3));
-        if (it + 2 < nk) C.load(gen, 2, 2, g);
-        if (!C.emit(sh, tiles, it, 0, sc0, sc1, r0, c, first, err) || it + 1 >= nk) break;
-        if (it + 4 < nk) C.load_offsets(gen, 1, p0 + 16 * (it + 4));
-        if (it + 3 < nk) C.load(gen, 0, 0, g);
-        if (!C.emit(sh, tiles, it + 1, 1, sc0, sc1, r0, c, first, err) || it + 2 >= nk) break;
-        if (it + 5 < nk) C.load_offsets(gen, 2, p0 + 16 * (it + 5));
-        if (it + 4 < nk) C.load(gen, 1, 1, g);
-        if (!C.emit(sh, tiles, it + 2, 2, sc0, sc1, r0, c, first, err)) break;
+    for (int it = 0; it < nk; it += 6) {
+#pragma unroll
+        for (int u = 0; u < 6; ++u) {
+            // stage it + u: values in buffer u & 1, offsets of it + u in buffer u % 3
+            if (it + u >= nk) return true;
+            if (it + u + 2 < nk) C.load_offsets(gen, (u + 2) % 3, p0 + 16 * (it + u + 2));
+            if (it + u + 1 < nk) C.load(gen, (u + 1) & 1, (u + 1) % 3, g);
+            if (!C.emit(sh, tiles, it0 + it + u, u & 1, sc0, sc1, r0, c, first, err)) return false;
+        }
     }
+    return true;
 }
 
-// Epilogue modes
-//   0: projection partials  part[z][n][m] = C[m][n] * sa[m] * sb[n]   (column-major per split)
-//   1: expansion            hpsi[b][g] += (C[g][re] + i C[g][im]) * sa[g] * sb[b]
-// GEN: the A operand is generated in shared memory from gen (GEN_FP16 selects
-// the FP16 split, else BF16) instead of bulk-copied from Ah / Al.
-template <int MODE, bool GEN = false, bool GEN_FP16 = true>
+// Split-K GEMM with partials (the projection and the complex128 GEMMs):
+//   part[z][n][m] = C[m][n] * sa[m] * sb[n]   (column-major per split)
+// over K range z of A [M][K] and B [N][K].  GEN: the A operand is generated in
+// shared memory from gen (GEN_FP16 selects the FP16 split, else BF16)
+// instead of bulk-copied from Ah / Al.
+template <bool GEN = false, bool GEN_FP16 = true>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const unsigned char* __restrict__ Ah, const unsigned char* __restrict__ Al,
                    const unsigned char* __restrict__ Bh, const unsigned char* __restrict__ Bl, TcEpilogue ep, int M,
@@ -523,10 +540,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     } else if (warp >= 2) {
         // ---- generated A (GEN): these warps write each stage's A pieces first
         using GT = typename std::conditional<GEN_FP16, __half, __nv_bfloat16>::type;
-        if constexpr (GEN) {
-            if (MODE == 0) gen_loop_rows<GT>(gen, sh, tiles, m0, kt0, nk, threadIdx.x - 64, err);
-            else gen_loop_cols<GT>(gen, sh, tiles, m0, kt0, nk, threadIdx.x - 64, err);
-        }
+        if constexpr (GEN) gen_loop_rows<GT>(gen, sh, tiles, m0, kt0, nk, threadIdx.x - 64, err);
         // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31; warps 2-5
         // take the first half of the columns, warps 6-9 the second
         const int q = warp & 3;
@@ -541,7 +555,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (go) {
             const float sa = (row < M) ? ep.sa_scale[row] : 0.f;
             const bool two = nk > 1;  // the odd accumulator holds data only with two or more k-tiles
-            if (MODE == 0) {
+            {
                 // partials column-major within a split ([z][N][M]): the 32 lanes
                 // (consecutive rows) of a warp store one 128-byte line per column
                 float* out = ep.part + ((size_t)blockIdx.z * N + n0) * (size_t)M + row;
@@ -564,53 +578,231 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                             if (n0 + c0 + i < N) out[(size_t)(c0 + i) * M] = v[i] * sa * sb[i];
                     }
                 }
-            } else {
-                // columns [0,128): real parts of bands 128*blockIdx.y + j, [128,256): imaginary
-                const bool add = ep.add32 != nullptr;
-#pragma unroll 1
-                for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 32) {
-                    float re[32], im[32], w[32];
-                    tmem_ld32(tbase + c0, re);
-                    tmem_ld32(tbase + 128 + c0, im);
-                    if (two) {
-                        tmem_ld32(tbase + BN + c0, w);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// hpsi[b][row] += (re + i im) * sa * sb[col] + add32[b][row] for the 16 bands of
+// one accumulator chunk (band b0 + i at scale column sb0 + i): read-modify-write
+// in groups of 8 bands, all loads of a group issued before its stores, so that
+// the HBM round trips overlap instead of following one another band by band.
+__device__ __forceinline__ void expand_rmw(const TcEpilogue& ep, int row, float sa, int b0, int sb0,
+                                           const float (&re)[16], const float (&im)[16])
+{
+    const bool add = ep.add32 != nullptr;
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) re[i] += w[i];
-                        tmem_ld32(tbase + BN + 128 + c0, w);
+    for (int h0 = 0; h0 < 16; h0 += 8) {
+        double2 o[8];
+        float2 ad[8];
+        float f[8];
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) im[i] += w[i];
-                    }
-                    if (row < M) {
-                        // read-modify-write of hpsi in groups of 8 bands: all loads
-                        // of a group are issued before its stores, so the HBM round
-                        // trips overlap instead of following one another band by band
-                        const int b0 = blockIdx.y * 128 + c0;
+        for (int i = 0; i < 8; ++i) {
+            const int b = b0 + h0 + i;
+            const size_t at = (size_t)b * ep.ldh + row;
+            f[i] = sa * ep.sb_scale[sb0 + h0 + i];
+            o[i] = b < ep.nb ? ep.hpsi[at] : make_double2(0.0, 0.0);
+            ad[i] = (add && b < ep.nb) ? ep.add32[at] : make_float2(0.f, 0.f);
+        }
 #pragma unroll
-                        for (int h0 = 0; h0 < 32; h0 += 8) {
-                            double2 o[8];
-                            float2 ad[8];
-                            float f[8];
-                            // loads only (predicated, no use), so that they all overlap
-#pragma unroll
-                            for (int i = 0; i < 8; ++i) {
-                                const int b = b0 + h0 + i;
-                                const size_t at = (size_t)b * ep.ldh + row;
-                                f[i] = sa * ep.sb_scale[n0 + c0 + h0 + i];
-                                o[i] = b < ep.nb ? ep.hpsi[at] : make_double2(0.0, 0.0);
-                                ad[i] = (add && b < ep.nb) ? ep.add32[at] : make_float2(0.f, 0.f);
-                            }
-#pragma unroll
-                            for (int i = 0; i < 8; ++i) {
-                                const int b = b0 + h0 + i;
-                                if (b < ep.nb) {
-                                    o[i].x += f2d_bits(fmaf(re[h0 + i], f[i], ad[i].x));
-                                    o[i].y += f2d_bits(fmaf(im[h0 + i], f[i], ad[i].y));
-                                    ep.hpsi[(size_t)b * ep.ldh + row] = o[i];
-                                }
-                            }
-                        }
-                    }
+        for (int i = 0; i < 8; ++i) {
+            const int b = b0 + h0 + i;
+            if (b < ep.nb) {
+                o[i].x += f2d_bits(fmaf(re[h0 + i], f[i], ad[i].x));
+                o[i].y += f2d_bits(fmaf(im[h0 + i], f[i], ad[i].y));
+                ep.hpsi[(size_t)b * ep.ldh + row] = o[i];
+            }
+        }
+    }
+}
+
+constexpr int TCP_THREADS = TC_THREADS + 128;  // + 4 epilogue warps (10..13)
+
+// The expansion, hpsi[b][g] += (C[g][re b] + i C[g][im b]) * sa[g] * sb[b]
+// (+ add32), as a persistent kernel: one CTA per SM walks the 128 x 256
+// output tiles (tile, tile + gridDim.x, ...).  The stage ring runs on across
+// tiles; the two 256-column TMEM accumulators alternate by tile, so that the
+// four epilogue warps drain tile i (the hpsi read-modify-write, HBM-bound)
+// while the tensor cores accumulate tile i + 1.  Warp 0 copies B (and A
+// without GEN), warp 1 issues the MMAs, warps 2-9 generate A (GEN).
+template <bool GEN, bool GEN_FP16>
+__global__ void __launch_bounds__(TCP_THREADS, 1)
+    tc_expand_kernel(const unsigned char* __restrict__ Ah, const unsigned char* __restrict__ Al,
+                     const unsigned char* __restrict__ Bh, const unsigned char* __restrict__ Bl, TcEpilogue ep, int M,
+                     int N, int ktiles, uint32_t idesc, int* err, TcGen gen)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    TcSmem* sh = reinterpret_cast<TcSmem*>(tiles + STAGES * STAGE_BYTES);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = (M + BM - 1) / BM, ntile = mt * (N / BN);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->gfull[s], GEN ? GEN_THREADS / 32 : 1);
+            mbar_init(&sh->empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&sh->tfull[a], 1);
+            mbar_init(&sh->tempty[a], 4);
+        }
+        mbar_init(&sh->tlast, 1);
+        mbar_init(&sh->done, 1);
+        sh->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+    volatile uint32_t* abort = &sh->abort_flag;
+
+    if (warp == 0 && lane == 0) {
+        // ---- bulk-copy producer
+        const size_t KT = (size_t)ktiles;
+        int git = 0;  // stage uses issued
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < ntile && !stop; tile += gridDim.x) {
+            const int mb = tile % mt, nbk = tile / mt;
+            const unsigned char* ah = GEN ? nullptr : Ah + (size_t)mb * KT * A_TILE;
+            const unsigned char* al = GEN ? nullptr : Al + (size_t)mb * KT * A_TILE;
+            const unsigned char* bh = Bh + (size_t)(2 * nbk) * KT * A_TILE;
+            const unsigned char* bl = Bl + (size_t)(2 * nbk) * KT * A_TILE;
+            for (int kt = 0; kt < ktiles; ++kt) {
+                const int s = git % STAGES;
+                const uint32_t ph = (git / STAGES) & 1;
+                if (!mbar_wait_abort(&sh->empty[s], ph ^ 1, &sh->abort_flag)) {
+                    if (!*abort) { atomicExch(err, 1); *abort = 1; }
+                    stop = true;
+                    break;
                 }
+                if (*abort) { stop = true; break; }
+                unsigned char* st = tiles + s * STAGE_BYTES;
+                mbar_arrive_expect_tx(&sh->full[s], GEN ? 2 * B_TILE : STAGE_BYTES);
+                if (!GEN) {
+                    bulk_load(st, ah + kt * A_TILE, A_TILE, &sh->full[s]);
+                    bulk_load(st + A_TILE, al + kt * A_TILE, A_TILE, &sh->full[s]);
+                }
+                bulk_load(st + 2 * A_TILE, bh + kt * A_TILE, A_TILE, &sh->full[s]);
+                bulk_load(st + 3 * A_TILE, bh + (KT + kt) * A_TILE, A_TILE, &sh->full[s]);
+                bulk_load(st + 2 * A_TILE + B_TILE, bl + kt * A_TILE, A_TILE, &sh->full[s]);
+                bulk_load(st + 3 * A_TILE + B_TILE, bl + (KT + kt) * A_TILE, A_TILE, &sh->full[s]);
+                ++git;
+            }
+        }
+        // drain: copies in flight must land before the CTA exits (bounded)
+        for (int i = max(0, git - STAGES); i < git; ++i) mbar_wait(&sh->full[i % STAGES], (i / STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        const uint32_t lim = g_tc_issue_wait_limit;
+        int git = 0, lt = 0;
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < ntile && !stop; tile += gridDim.x, ++lt) {
+            const int a = lt & 1;
+            // accumulator a free: its previous tile read out by the epilogue warps
+            if (!mbar_wait_abort(&sh->tempty[a], ((lt >> 1) & 1) ^ 1, &sh->abort_flag)) {
+                if (!*abort) { atomicExch(err, 5); *abort = 1; }
+                break;
+            }
+            tc_fence_after();
+            const uint32_t acc = tmem + (uint32_t)(a * BN);
+            for (int kt = 0; kt < ktiles; ++kt) {
+                const int s = git % STAGES;
+                const uint32_t ph = (git / STAGES) & 1;
+                if (!mbar_wait_n(&sh->full[s], ph, lim) || (GEN && !mbar_wait_n(&sh->gfull[s], ph, lim))) {
+                    atomicExch(err, 2);
+                    *abort = 1;
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
+                const uint64_t adh = sdesc_sw64(st), adl = sdesc_sw64(st + A_TILE);
+                const uint64_t bdh = sdesc_sw64(st + 2 * A_TILE), bdl = sdesc_sw64(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint64_t adv = (uint64_t)((kk * 32) >> 4);  // 16 elements = 32 bytes along K
+                    const uint32_t first = (kt == 0 && kk == 0) ? 0u : 1u;
+                    tc_mma(acc, adh + adv, bdh + adv, idesc, first);
+                    tc_mma(acc, adh + adv, bdl + adv, idesc, 1u);
+                    tc_mma(acc, adl + adv, bdh + adv, idesc, 1u);
+                }
+                tc_commit(&sh->empty[s]);
+                ++git;
+            }
+            if (!stop) {
+                tc_commit(&sh->tfull[a]);
+                if (tile + (int)gridDim.x >= ntile) tc_commit(&sh->tlast);
+            }
+        }
+        // every MMA issued has completed before the accumulators are freed (bounded)
+        tc_commit(&sh->done);
+        mbar_wait(&sh->done, 0);
+    } else if (warp >= 2) {
+        // The CTA's last tile: its epilogue is exposed (no next tile to overlap),
+        // so warps 2-13 share it, three per TMEM lane quadrant (the epilogue
+        // warp, then generator warps w < 6 and w >= 6 take the 16-band chunks
+        // c with c % 3 = 0, 1, 2).  Earlier tiles: the epilogue warps alone.
+        const int last_lt = (ntile - 1 - (int)blockIdx.x) / (int)gridDim.x;
+        const int role = warp >= 10 ? 0 : (warp < 6 ? 1 : 2);
+        const int q = warp & 3;
+        int lt = 0;
+        if (warp < 10) {
+            // ---- generated A
+            if constexpr (GEN) {
+                using GT = typename std::conditional<GEN_FP16, __half, __nv_bfloat16>::type;
+                int git = 0;
+                for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+                    if (!gen_loop_cols<GT>(gen, sh, tiles, (tile % mt) * BM, 0, ktiles, threadIdx.x - 64, err, git))
+                        break;
+                    git += ktiles;
+                }
+            }
+            lt = last_lt;
+        }
+        // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31
+        for (int tile = blockIdx.x + lt * gridDim.x; tile < ntile; tile += gridDim.x, ++lt) {
+            const int a = lt & 1, mb = tile % mt, nbk = tile / mt;
+            const bool last = lt == last_lt;
+            // warps 2-9 join at the last tile only, at any point of the
+            // accumulators' phases: they wait on the single-phase barrier
+            bool ok = warp < 10 ? mbar_wait_abort(&sh->tlast, 0, &sh->abort_flag)
+                                : mbar_wait_abort(&sh->tfull[a], (lt >> 1) & 1, &sh->abort_flag);
+            if (!ok && !*abort) { atomicExch(err, 3); *abort = 1; }
+            // warp-uniform: tcgen05.ld is a .sync.aligned warp instruction
+            if (!__all_sync(0xffffffffu, ok && !*abort)) break;
+            tc_fence_after();
+            const int row = mb * BM + q * 32 + lane;
+            const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN);
+            const float sa = (row < M) ? ep.sa_scale[row] : 0.f;
+            // columns [0,128): real parts of bands 128 nbk + j, [128,256): imaginary
+#pragma unroll 1
+            for (int c = 0; c < 8; ++c) {
+                if (last && c % 3 != role) continue;
+                const int c0 = 16 * c;
+                float re[16], im[16];
+                tmem_ld16(tbase + c0, re);
+                tmem_ld16(tbase + 128 + c0, im);
+                if (!last && c == 7) {
+                    // accumulator read out (tcgen05.ld waited): hand it back to the MMA warp
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&sh->tempty[a]);
+                }
+                if (row < M) expand_rmw(ep, row, sa, nbk * 128 + c0, nbk * BN + c0, re, im);
             }
         }
     }
@@ -892,45 +1084,73 @@ __global__ void zero_rows_kernel(int nb, int nbp, size_t ldk, T* hi, T* lo, floa
     }
 }
 
-// W[p][b] = lambda_p * sum_z (C[z][p][re b] + i C[z][p][im b])
+// One entry of the split sum: w = lambda_p * sum_z (C[z][re b][p] + i C[z][im b][p])
+// and e = lambda_p |sum|^2 in FP64.  complex64 W: compensated FP32 sums, no FP64 pipe.
 template <typename CW>
-__global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float* __restrict__ part,
-                                   const double* __restrict__ lam, int period, CW* W, double* eterm = nullptr)
+__device__ __forceinline__ void proj_sum(int P, int N, int nsplit, const float* __restrict__ part,
+                                         const double* __restrict__ lam, int period, int p, int b, bool want_e,
+                                         CW& w, double& e)
 {
-    // consecutive threads take consecutive projectors: coalesced reads of the
-    // column-major partials part[z][n][p]
-    const size_t t_idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t_idx >= (size_t)P * nb) return;
-    const int p = (int)(t_idx % P), b = (int)(t_idx / P);
-    const size_t idx = (size_t)p * nb + b;  // W[p][b]
     const int t = b / 128, j = b % 128;
     const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
     const size_t zs = (size_t)N * P;
     const float* pre = part + cre * P + p;
     const float* pim = part + cim * P + p;
     if constexpr (std::is_same<CW, float2>::value) {
-        Sum2f re, im;  // complex64 W: compensated FP32 sums, no FP64 pipe
+        Sum2f re, im;
+#pragma unroll 4
         for (int z = 0; z < nsplit; ++z) {
             re.add(pre[z * zs]);
             im.add(pim[z * zs]);
         }
         const float f = lam ? d2f_bits(lam[p % period]) : 1.f;
-        W[idx] = make_float2(f * re.value(), f * im.value());
-        if (eterm) {
+        w = make_float2(f * re.value(), f * im.value());
+        if (want_e) {
             // lambda_p |<p|psi_b>|^2 in FP64 from the two-float sums
             const double sr = f2d_bits(re.s) + f2d_bits(re.c), si = f2d_bits(im.s) + f2d_bits(im.c);
-            eterm[idx] = (lam ? lam[p % period] : 1.0) * (sr * sr + si * si);
+            e = (lam ? lam[p % period] : 1.0) * (sr * sr + si * si);
         }
-        return;
+    } else {
+        double sr = 0.0, si = 0.0;
+        for (int z = 0; z < nsplit; ++z) {
+            sr += pre[z * zs];
+            si += pim[z * zs];
+        }
+        const double f = lam ? lam[p % period] : 1.0;
+        w = from_c128<CW>(make_double2(f * sr, f * si));
+        if (want_e) e = f * (sr * sr + si * si);  // lambda_p |<p|psi_b>|^2, FP64
     }
-    double sr = 0.0, si = 0.0;
-    for (int z = 0; z < nsplit; ++z) {
-        sr += pre[z * zs];
-        si += pim[z * zs];
+}
+
+// W[p][b] (and eterm[p][b]) over 32-projector x 8-band tiles, one entry per
+// thread: the partials are read along p (coalesced, column-major per split),
+// W is written along b through a shared-memory transpose.
+template <typename CW>
+__global__ void __launch_bounds__(256) proj_reduce_kernel(int P, int nb, int N, int nsplit,
+                                                          const float* __restrict__ part,
+                                                          const double* __restrict__ lam, int period, CW* W,
+                                                          double* eterm = nullptr)
+{
+    __shared__ CW tw[8][33];
+    __shared__ double te[8][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int p0 = blockIdx.x * 32, b0 = blockIdx.y * 8;
+    {
+        const int p = p0 + tx, b = b0 + ty;
+        CW w{};
+        double e = 0.0;
+        if (p < P && b < nb) proj_sum<CW>(P, N, nsplit, part, lam, period, p, b, eterm != nullptr, w, e);
+        tw[ty][tx] = w;
+        te[ty][tx] = e;
     }
-    const double f = lam ? lam[p % period] : 1.0;
-    W[idx] = from_c128<CW>(make_double2(f * sr, f * si));
-    if (eterm) eterm[idx] = f * (sr * sr + si * si);  // lambda_p |<p|psi_b>|^2, FP64
+    __syncthreads();
+    const int pl = threadIdx.x >> 3, bl = threadIdx.x & 7;  // 8 consecutive bands of one projector
+    const int p = p0 + pl, b = b0 + bl;
+    if (p < P && b < nb) {
+        const size_t idx = (size_t)p * nb + b;
+        W[idx] = tw[bl][pl];
+        if (eterm) eterm[idx] = te[bl][pl];
+    }
 }
 
 // out[b] = sum_p eterm[p][b], in p order
@@ -1089,47 +1309,61 @@ int tc_proj_splits(int P, int nb, size_t ldk)
     return best;
 }
 
-template <int MODE, bool GEN, bool GEN_FP16>
-static cudaError_t launch_tc_t(dim3 grid, size_t smem, cudaStream_t st, const unsigned char* ah,
-                               const unsigned char* al, const unsigned char* bh, const unsigned char* bl,
-                               const TcEpilogue& ep, int M, int N, int ktiles, int per, uint32_t idesc, int* err,
-                               const TcGen& gen)
+template <bool GEN, bool GEN_FP16>
+static cudaError_t launch_proj_t(dim3 grid, size_t smem, cudaStream_t st, const unsigned char* ah,
+                                 const unsigned char* al, const unsigned char* bh, const unsigned char* bl,
+                                 const TcEpilogue& ep, int M, int N, int ktiles, int per, uint32_t idesc, int* err,
+                                 const TcGen& gen)
 {
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<MODE, GEN, GEN_FP16>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<GEN, GEN_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e) return e;
-    tc_gemm_kernel<MODE, GEN, GEN_FP16><<<grid, TC_THREADS, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err,
-                                                                  gen);
+    tc_gemm_kernel<GEN, GEN_FP16><<<grid, TC_THREADS, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err,
+                                                                   gen);
     return cudaGetLastError();
 }
 
-// A: rows M, B: rows N (= tc_band_rows(nb)); one launch.  With gen the A
+template <bool GEN, bool GEN_FP16>
+static cudaError_t launch_expand_t(int grid, size_t smem, cudaStream_t st, const unsigned char* ah,
+                                   const unsigned char* al, const unsigned char* bh, const unsigned char* bl,
+                                   const TcEpilogue& ep, int M, int N, int ktiles, uint32_t idesc, int* err,
+                                   const TcGen& gen)
+{
+    cudaError_t e = cudaFuncSetAttribute(tc_expand_kernel<GEN, GEN_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e) return e;
+    tc_expand_kernel<GEN, GEN_FP16><<<grid, TCP_THREADS, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, idesc, err,
+                                                                      gen);
+    return cudaGetLastError();
+}
+
+// A: rows M, B: rows N (= tc_band_rows(nb)); one launch.  Mode 0: split-K
+// partials (nsplit), mode 1: the persistent expansion.  With gen the A
 // operand is generated from those tables (A.hi / A.lo unused).
 static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperand& B, int N, int nsplit, bool fp16,
                              const TcEpilogue& ep, int* err, cudaStream_t st, const TcGen* gen = nullptr)
 {
     if (A.ldk != B.ldk || A.ldk % BK) return cudaErrorInvalidValue;
     const int ktiles = (int)(A.ldk / BK);
-    const int per = ceil_div(ktiles, nsplit);
-    const int nz = ceil_div(ktiles, per);
     const size_t smem = tc_gemm_smem_bytes();
-    dim3 grid(ceil_div(M, BM), N / BN, nz);
     const uint32_t idesc = idesc_f16(BM, BN, fp16 ? 0u : 1u);
     const unsigned char *ah = (const unsigned char*)A.hi, *al = (const unsigned char*)A.lo;
     const unsigned char *bh = (const unsigned char*)B.hi, *bl = (const unsigned char*)B.lo;
-    if (!gen) {
-        const TcGen none{};
-        return mode == 0 ? launch_tc_t<0, false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc,
-                                                       err, none)
-                         : launch_tc_t<1, false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc,
-                                                       err, none);
+    const TcGen none{};
+    const TcGen& g = gen ? *gen : none;
+    if (mode == 1) {
+        const int tiles = ceil_div(M, BM) * (N / BN);
+        const int grid = std::min(tiles, sm_count());
+        if (!gen) return launch_expand_t<false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g);
+        return fp16 ? launch_expand_t<true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g)
+                    : launch_expand_t<true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g);
     }
-    if (mode == 0)
-        return fp16 ? launch_tc_t<0, true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, *gen)
-                    : launch_tc_t<0, true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err,
-                                                  *gen);
-    return fp16 ? launch_tc_t<1, true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, *gen)
-                : launch_tc_t<1, true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, *gen);
+    const int per = ceil_div(ktiles, nsplit);
+    const int nz = ceil_div(ktiles, per);
+    dim3 grid(ceil_div(M, BM), N / BN, nz);
+    if (!gen) return launch_proj_t<false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, g);
+    return fp16 ? launch_proj_t<true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, g)
+                : launch_proj_t<true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, per, idesc, err, g);
 }
 
 cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
@@ -1149,8 +1383,9 @@ cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb,
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
     h = prof->open(PH_REDUCE, st);
-    proj_reduce_kernel<float2><<<ceil_div((long)P * nb, 256), 256, 0, st>>>(P, nb, N, nz, part, lam, period, W,
-                                                                            e_nl ? eterm : nullptr);
+    proj_reduce_kernel<float2><<<dim3(ceil_div(P, 32), ceil_div(nb, 8)), 256, 0, st>>>(P, nb, N, nz, part, lam,
+                                                                                        period, W,
+                                                                                        e_nl ? eterm : nullptr);
     if (e_nl) eterm_sum_kernel<<<nb, 256, 0, st>>>(P, nb, eterm, e_nl);
     prof->close(h, st, e_nl ? 2 : 1);
     return cudaGetLastError();
@@ -1181,7 +1416,8 @@ cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, 
     const int ktiles = (int)(A.ldk / BK);
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
-    proj_reduce_kernel<double2><<<ceil_div((long)M * nb, 256), 256, 0, st>>>(M, nb, N, nz, part, nullptr, 1, out);
+    proj_reduce_kernel<double2><<<dim3(ceil_div(M, 32), ceil_div(nb, 8)), 256, 0, st>>>(M, nb, N, nz, part, nullptr,
+                                                                                         1, out);
     return cudaGetLastError();
 }
 
