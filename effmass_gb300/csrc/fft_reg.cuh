@@ -76,13 +76,22 @@ constexpr CS cossin_2pi(long j, long n)
 }
 
 // ---- complex helpers -------------------------------------------------------
-HPSI_D float2 add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-HPSI_D float2 sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex adds and subtracts are packed FP32 pair operations (one instruction
+// for the real and imaginary parts, each rounded as a scalar add): the
+// transforms are issue-bound, and most of their instructions are these adds.
+HPSI_D float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+HPSI_D float2 sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 // a * (S i)
 template <int S>
 HPSI_D float2 mul_si(float2 a)
 {
     return S > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+// a + S i d: scalar, the swapped components of i d need no pair of their own
+template <int S>
+HPSI_D float2 add_si(float2 a, float2 d)
+{
+    return S > 0 ? make_float2(a.x - d.y, a.y + d.x) : make_float2(a.x + d.y, a.y - d.x);
 }
 
 // a * exp(S 2 pi i J / N), J taken mod N; exact for the multiples of N/4
@@ -120,22 +129,22 @@ HPSI_D void dft3(float2 (&v)[N])
     constexpr float h = 0.86602540378443864676f;  // sin(2 pi / 3)
     const float2 a = v[B], b = v[B + ST], c = v[B + 2 * ST];
     const float2 s = add(b, c), d = sub(b, c);
-    const float2 m = make_float2(fmaf(-0.5f, s.x, a.x), fmaf(-0.5f, s.y, a.y));
-    const float2 t = mul_si<S>(make_float2(h * d.x, h * d.y));
+    const float2 m = __ffma2_rn(make_float2(-0.5f, -0.5f), s, a);
+    const float2 hd = __fmul2_rn(make_float2(h, h), d);
     v[B] = add(a, s);
-    v[B + ST] = add(m, t);
-    v[B + 2 * ST] = sub(m, t);
+    v[B + ST] = add_si<S>(m, hd);   // m + S i h d
+    v[B + 2 * ST] = add_si<-S>(m, hd);
 }
 
 template <int S, int B, int ST, int N>
 HPSI_D void dft4(float2 (&v)[N])
 {
     const float2 y0 = v[B], y1 = v[B + ST], y2 = v[B + 2 * ST], y3 = v[B + 3 * ST];
-    const float2 t0 = add(y0, y2), t1 = sub(y0, y2), t2 = add(y1, y3), t3 = mul_si<S>(sub(y1, y3));
+    const float2 t0 = add(y0, y2), t1 = sub(y0, y2), t2 = add(y1, y3), d = sub(y1, y3);
     v[B] = add(t0, t2);
     v[B + 2 * ST] = sub(t0, t2);
-    v[B + ST] = add(t1, t3);
-    v[B + 3 * ST] = sub(t1, t3);
+    v[B + ST] = add_si<S>(t1, d);       // t1 + S i d
+    v[B + 3 * ST] = add_si<-S>(t1, d);  // t1 - S i d
 }
 
 // 8 = 2 x 4: 4-point DFTs of the even and odd elements, W_8^k on the odd ones
@@ -148,12 +157,16 @@ HPSI_D void dft8(float2 (&v)[N])
     dft4<S, 0, 1>(o);
     constexpr float r2 = 0.70710678118654752440f;
     o[1] = make_float2(r2 * (o[1].x - S * o[1].y), r2 * (S * o[1].x + o[1].y));    // * (r2, S r2)
-    o[2] = mul_si<S>(o[2]);                                                        // * S i
     o[3] = make_float2(-r2 * (o[3].x + S * o[3].y), r2 * (S * o[3].x - o[3].y));   // * (-r2, S r2)
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        v[B + k * ST] = add(e[k], o[k]);
-        v[B + (k + 4) * ST] = sub(e[k], o[k]);
+        if (k == 2) {  // * S i
+            v[B + k * ST] = add_si<S>(e[k], o[k]);
+            v[B + (k + 4) * ST] = add_si<-S>(e[k], o[k]);
+        } else {
+            v[B + k * ST] = add(e[k], o[k]);
+            v[B + (k + 4) * ST] = sub(e[k], o[k]);
+        }
     }
 }
 
