@@ -623,6 +623,63 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
 constexpr int XREG_THREADS = 128;
 constexpr int xreg_minb(int n) { return n >= 64 ? 2 : (n >= 36 ? 3 : 4); }
 
+// The line work of the register x passes: G->r transform, the V multiply
+// (with the energy sums: four interleaved FP32 partials of V|psi(r)|^2 and
+// |psi(r)|^2, dV |psi(r)|^2 in a fifth), leaving r->G to the caller.  vp, dvp:
+// the line's V and dV (stride N^2; dvp null: none).
+template <typename PL, bool ENERGY>
+__device__ __forceinline__ void xline_g2r_v(float2 (&v)[PL::n], const float* __restrict__ vp,
+                                            const float* __restrict__ dvp, bool valid, float (&a1)[4], float (&a0)[4],
+                                            float& ac)
+{
+    constexpr int N1 = PL::r0, N2 = PL::r1, N = PL::n, N23 = N * N;
+    fftreg::fft_nat_to_split<+1, N1, N2>(v);
+#pragma unroll
+    for (int x = 0; x < N; ++x) {
+        const float w = valid ? __ldg(vp + (size_t)x * N23) : 0.f;
+        float2& e = v[fftreg::split_pos<N1, N2>(x)];
+        if constexpr (ENERGY) {
+            // four interleaved FP32 partial sums per line (N/4 terms each);
+            // the FP64 part of V the FP32 table misses (dV) in one more
+            const float mm = e.x * e.x + e.y * e.y;
+            a1[x & 3] += w * mm;
+            a0[x & 3] += mm;
+            if (dvp && valid) ac += __ldg(dvp + (size_t)x * N23) * mm;
+        }
+        // rounded product (never fused into the next stage's adds), so that
+        // both variants of the kernel give bit-identical hpsi
+        e = make_float2(__fmul_rn(e.x, w), __fmul_rn(e.y, w));
+    }
+}
+
+// one thread's line energy sums of a block of XREG_THREADS lines, added in
+// FP64 in a fixed order and written by thread 0 to e[0], e[1]; red: the
+// block's scratch (a __syncthreads separates its uses)
+__device__ __forceinline__ void xline_energy_block(const float (&a1)[4], const float (&a0)[4], float ac,
+                                                   double (&red)[2][XREG_THREADS / 32], double* e)
+{
+    double t1 = (f2d_bits(a1[0]) + f2d_bits(a1[1])) + (f2d_bits(a1[2]) + f2d_bits(a1[3])) + f2d_bits(ac);
+    double t0 = (f2d_bits(a0[0]) + f2d_bits(a0[1])) + (f2d_bits(a0[2]) + f2d_bits(a0[3]));
+    for (int o = 16; o > 0; o >>= 1) {
+        t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+        t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = t1;
+        red[1][threadIdx.x >> 5] = t0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double u1 = 0.0, u0 = 0.0;
+        for (int w = 0; w < XREG_THREADS / 32; ++w) {
+            u1 += red[0][w];
+            u0 += red[1][w];
+        }
+        e[0] = u1;
+        e[1] = u0;
+    }
+}
+
 template <typename PL, bool ENERGY>
 __global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n)) x_pass_reg(LocalArgs a, float2* __restrict__ T,
                                                               const float* __restrict__ vloc)
@@ -630,7 +687,10 @@ __global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n)) x_pass_reg(Loc
     constexpr int N1 = PL::r0, N2 = PL::r1, N = PL::n, N23 = N * N, W = (N + 31) / 32;
     __shared__ uint32_t msk[W];
     __shared__ double red[2][XREG_THREADS / 32];
-    int b = blockIdx.y;
+    // bands in reverse launch order: the G->r pass wrote the last bands last,
+    // so they are the ones still in L2 (the r->G pass then runs forward over
+    // the bands written last here)
+    int b = a.items ? (int)blockIdx.y : (int)(gridDim.y - 1 - blockIdx.y);
     int nxs = a.nxs;
     const int* plane_x = a.plane_x;
     if (a.items) {  // batched: the band's item (uniform per block)
@@ -661,50 +721,10 @@ __global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n)) x_pass_reg(Loc
             if (on) p += N23;
         }
     }
-    fftreg::fft_nat_to_split<+1, N1, N2>(v);
     float a1[4] = {0.f, 0.f, 0.f, 0.f}, a0[4] = {0.f, 0.f, 0.f, 0.f}, ac = 0.f;
-    {
-        const float* vp = vloc + jk;
-        const float* dvp = (ENERGY && a.dv32) ? a.dv32 + jk : nullptr;
-#pragma unroll
-        for (int x = 0; x < N; ++x) {
-            const float w = valid ? __ldg(vp + (size_t)x * N23) : 0.f;
-            float2& e = v[fftreg::split_pos<N1, N2>(x)];
-            if constexpr (ENERGY) {
-                // four interleaved FP32 partial sums per line (N/4 terms each);
-                // the FP64 part of V the FP32 table misses (dV) in one more
-                const float mm = e.x * e.x + e.y * e.y;
-                a1[x & 3] += w * mm;
-                a0[x & 3] += mm;
-                if (dvp && valid) ac += __ldg(dvp + (size_t)x * N23) * mm;
-            }
-            // rounded product (never fused into the next stage's adds), so that
-            // both variants of the kernel give bit-identical hpsi
-            e = make_float2(__fmul_rn(e.x, w), __fmul_rn(e.y, w));
-        }
-    }
+    xline_g2r_v<PL, ENERGY>(v, vloc + jk, (ENERGY && a.dv32) ? a.dv32 + jk : nullptr, valid, a1, a0, ac);
     if constexpr (ENERGY) {
-        double t1 = (f2d_bits(a1[0]) + f2d_bits(a1[1])) + (f2d_bits(a1[2]) + f2d_bits(a1[3])) + f2d_bits(ac);
-        double t0 = (f2d_bits(a0[0]) + f2d_bits(a0[1])) + (f2d_bits(a0[2]) + f2d_bits(a0[3]));
-        for (int o = 16; o > 0; o >>= 1) {
-            t1 += __shfl_xor_sync(0xffffffffu, t1, o);
-            t0 += __shfl_xor_sync(0xffffffffu, t0, o);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            red[0][threadIdx.x >> 5] = t1;
-            red[1][threadIdx.x >> 5] = t0;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double u1 = 0.0, u0 = 0.0;
-            for (int w = 0; w < XREG_THREADS / 32; ++w) {
-                u1 += red[0][w];
-                u0 += red[1][w];
-            }
-            double* e = a.epart + ((size_t)(a.e_band0 + b) * gridDim.x + blockIdx.x) * 2;
-            e[0] = u1;
-            e[1] = u0;
-        }
+        xline_energy_block(a1, a0, ac, red, a.epart + ((size_t)(a.e_band0 + b) * gridDim.x + blockIdx.x) * 2);
         if (!valid) return;
     }
     fftreg::fft_split_to_nat<-1, N1, N2>(v);
