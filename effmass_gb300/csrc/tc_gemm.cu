@@ -431,7 +431,7 @@ __device__ bool gen_loop_cols(const TcGen& gen, TcSmem* sh, unsigned char* tiles
 }
 
 // Split-K GEMM with partials (the projection and the complex128 GEMMs):
-//   part[z][n][m] = C[m][n] * sa[m] * sb[n]   (column-major per split)
+//   part[z][m][n] = C[m][n] * sa[m] * sb[n]   (row-major per split)
 // over K range z of A [M][K] and B [N][K].  GEN: the A operand is generated in
 // shared memory from gen (GEN_FP16 selects the FP16 split, else BF16)
 // instead of bulk-copied from Ah / Al.
@@ -556,9 +556,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const float sa = (row < M) ? ep.sa_scale[row] : 0.f;
             const bool two = nk > 1;  // the odd accumulator holds data only with two or more k-tiles
             {
-                // partials column-major within a split ([z][N][M]): the 32 lanes
-                // (consecutive rows) of a warp store one 128-byte line per column
-                float* out = ep.part + ((size_t)blockIdx.z * N + n0) * (size_t)M + row;
+                // row-major partials [z][M][N].  A lane holds one row; each
+                // 32 x 32 block is transposed through the warp's own slice of
+                // the stage buffers (free: every MMA has read them once `done`
+                // completed), so that each store instruction writes one row's
+                // 128 contiguous bytes.
+                float* tr = reinterpret_cast<float*>(tiles) + (warp - 2) * 32 * 33;
+                const int rbase = m0 + q * 32;
+                float* out = ep.part + ((size_t)blockIdx.z * M + rbase) * (size_t)N + n0;
 #pragma unroll 1
                 for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
                     float v[32], w[32];
@@ -568,15 +573,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                         for (int i = 0; i < 32; ++i) v[i] += w[i];
                     }
-                    if (row < M) {
-                        // scales first: a load after a store to out would wait for it
-                        float sb[32];
+                    const float sbl = ep.sb_scale[n0 + c0 + lane];  // this lane's column after the transpose
+                    __syncwarp();
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) sb[i] = (n0 + c0 + i < N) ? ep.sb_scale[n0 + c0 + i] : 0.f;
-#pragma unroll
-                        for (int i = 0; i < 32; ++i)
-                            if (n0 + c0 + i < N) out[(size_t)(c0 + i) * M] = v[i] * sa * sb[i];
-                    }
+                    for (int i = 0; i < 32; ++i) tr[lane * 33 + i] = v[i] * sa;
+                    __syncwarp();
+#pragma unroll 8
+                    for (int i = 0; i < 32; ++i)
+                        if (rbase + i < M) out[(size_t)i * N + c0 + lane] = tr[i * 33 + lane] * sbl;
                 }
             }
         }
@@ -1084,73 +1088,45 @@ __global__ void zero_rows_kernel(int nb, int nbp, size_t ldk, T* hi, T* lo, floa
     }
 }
 
-// One entry of the split sum: w = lambda_p * sum_z (C[z][re b][p] + i C[z][im b][p])
-// and e = lambda_p |sum|^2 in FP64.  complex64 W: compensated FP32 sums, no FP64 pipe.
+// W[p][b] = lambda_p * sum_z (C[z][p][re b] + i C[z][p][im b]) (and, with eterm,
+// lambda_p |sum|^2 in FP64); consecutive threads take consecutive bands, so the
+// reads of a split's row are coalesced, as are the writes of W[p][.]
 template <typename CW>
-__device__ __forceinline__ void proj_sum(int P, int N, int nsplit, const float* __restrict__ part,
-                                         const double* __restrict__ lam, int period, int p, int b, bool want_e,
-                                         CW& w, double& e)
+__global__ void proj_reduce_kernel(int P, int nb, int N, int nsplit, const float* __restrict__ part,
+                                   const double* __restrict__ lam, int period, CW* W, double* eterm = nullptr)
 {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)P * nb) return;
+    const int p = (int)(idx / nb), b = (int)(idx % nb);
     const int t = b / 128, j = b % 128;
     const size_t cre = (size_t)t * 256 + j, cim = cre + 128;
-    const size_t zs = (size_t)N * P;
-    const float* pre = part + cre * P + p;
-    const float* pim = part + cim * P + p;
+    const size_t zs = (size_t)P * N;
+    const float* pre = part + (size_t)p * N + cre;
+    const float* pim = part + (size_t)p * N + cim;
     if constexpr (std::is_same<CW, float2>::value) {
-        Sum2f re, im;
+        Sum2f re, im;  // complex64 W: compensated FP32 sums, no FP64 pipe
 #pragma unroll 4
         for (int z = 0; z < nsplit; ++z) {
             re.add(pre[z * zs]);
             im.add(pim[z * zs]);
         }
         const float f = lam ? d2f_bits(lam[p % period]) : 1.f;
-        w = make_float2(f * re.value(), f * im.value());
-        if (want_e) {
+        W[idx] = make_float2(f * re.value(), f * im.value());
+        if (eterm) {
             // lambda_p |<p|psi_b>|^2 in FP64 from the two-float sums
             const double sr = f2d_bits(re.s) + f2d_bits(re.c), si = f2d_bits(im.s) + f2d_bits(im.c);
-            e = (lam ? lam[p % period] : 1.0) * (sr * sr + si * si);
+            eterm[idx] = (lam ? lam[p % period] : 1.0) * (sr * sr + si * si);
         }
-    } else {
-        double sr = 0.0, si = 0.0;
-        for (int z = 0; z < nsplit; ++z) {
-            sr += pre[z * zs];
-            si += pim[z * zs];
-        }
-        const double f = lam ? lam[p % period] : 1.0;
-        w = from_c128<CW>(make_double2(f * sr, f * si));
-        if (want_e) e = f * (sr * sr + si * si);  // lambda_p |<p|psi_b>|^2, FP64
+        return;
     }
-}
-
-// W[p][b] (and eterm[p][b]) over 32-projector x 8-band tiles, one entry per
-// thread: the partials are read along p (coalesced, column-major per split),
-// W is written along b through a shared-memory transpose.
-template <typename CW>
-__global__ void __launch_bounds__(256) proj_reduce_kernel(int P, int nb, int N, int nsplit,
-                                                          const float* __restrict__ part,
-                                                          const double* __restrict__ lam, int period, CW* W,
-                                                          double* eterm = nullptr)
-{
-    __shared__ CW tw[8][33];
-    __shared__ double te[8][33];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int p0 = blockIdx.x * 32, b0 = blockIdx.y * 8;
-    {
-        const int p = p0 + tx, b = b0 + ty;
-        CW w{};
-        double e = 0.0;
-        if (p < P && b < nb) proj_sum<CW>(P, N, nsplit, part, lam, period, p, b, eterm != nullptr, w, e);
-        tw[ty][tx] = w;
-        te[ty][tx] = e;
+    double sr = 0.0, si = 0.0;
+    for (int z = 0; z < nsplit; ++z) {
+        sr += pre[z * zs];
+        si += pim[z * zs];
     }
-    __syncthreads();
-    const int pl = threadIdx.x >> 3, bl = threadIdx.x & 7;  // 8 consecutive bands of one projector
-    const int p = p0 + pl, b = b0 + bl;
-    if (p < P && b < nb) {
-        const size_t idx = (size_t)p * nb + b;
-        W[idx] = tw[bl][pl];
-        if (eterm) eterm[idx] = te[bl][pl];
-    }
+    const double f = lam ? lam[p % period] : 1.0;
+    W[idx] = from_c128<CW>(make_double2(f * sr, f * si));
+    if (eterm) eterm[idx] = f * (sr * sr + si * si);  // lambda_p |<p|psi_b>|^2, FP64
 }
 
 // out[b] = sum_p eterm[p][b], in p order
@@ -1383,9 +1359,8 @@ cudaError_t tc_projection(const TcOperand& A, int P, const TcOperand& B, int nb,
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
     h = prof->open(PH_REDUCE, st);
-    proj_reduce_kernel<float2><<<dim3(ceil_div(P, 32), ceil_div(nb, 8)), 256, 0, st>>>(P, nb, N, nz, part, lam,
-                                                                                        period, W,
-                                                                                        e_nl ? eterm : nullptr);
+    proj_reduce_kernel<float2><<<ceil_div((long)P * nb, 256), 256, 0, st>>>(P, nb, N, nz, part, lam, period, W,
+                                                                            e_nl ? eterm : nullptr);
     if (e_nl) eterm_sum_kernel<<<nb, 256, 0, st>>>(P, nb, eterm, e_nl);
     prof->close(h, st, e_nl ? 2 : 1);
     return cudaGetLastError();
@@ -1416,8 +1391,7 @@ cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, 
     const int ktiles = (int)(A.ldk / BK);
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
-    proj_reduce_kernel<double2><<<dim3(ceil_div(M, 32), ceil_div(nb, 8)), 256, 0, st>>>(M, nb, N, nz, part, nullptr,
-                                                                                         1, out);
+    proj_reduce_kernel<double2><<<ceil_div((long)M * nb, 256), 256, 0, st>>>(M, nb, N, nz, part, nullptr, 1, out);
     return cudaGetLastError();
 }
 

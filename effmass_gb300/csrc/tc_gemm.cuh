@@ -14,7 +14,7 @@ struct TcOperand {
 };
 
 struct TcEpilogue {
-    float* part;               // mode 0: [splits][N][M] partial sums
+    float* part;               // mode 0: [splits][M][N] partial sums
     double2* hpsi;             // mode 1: output, [nb][ldh]
     int ldh;
     int nb;
