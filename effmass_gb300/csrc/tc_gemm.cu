@@ -1155,29 +1155,6 @@ size_t tc_rows_pad(size_t rows) { return (rows + BM - 1) / BM * BM; }
 
 size_t tc_gemm_smem_bytes() { return (size_t)STAGES * STAGE_BYTES + 1024 + sizeof(TcSmem) + 64; }
 
-cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, TcOperand* proj, TcOperand* expand,
-                                   float* cmax_scratch, cudaStream_t st)
-{
-    if (P == 0 || npw == 0) return cudaSuccess;
-    if (fp16) {
-        split_rows_kernel<__half, float2><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__half*)proj->hi, (__half*)proj->lo,
-                                                     proj->inv_scale, true);
-    } else {
-        split_rows_kernel<__nv_bfloat16, float2><<<P, 256, 0, st>>>(pr, npw, proj->ldk, (__nv_bfloat16*)proj->hi,
-                                                            (__nv_bfloat16*)proj->lo, proj->inv_scale, false);
-    }
-    col_max_kernel<<<ceil_div(npw, 256), 256, 0, st>>>(pr, nullptr, P, npw, cmax_scratch);
-    dim3 g(ceil_div(npw, 32), ceil_div(P, 32));
-    if (fp16)
-        transpose_split_kernel<__half><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, 0, cmax_scratch, (__half*)expand->hi,
-                                                          (__half*)expand->lo, expand->inv_scale, true);
-    else
-        transpose_split_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pr, P, npw, expand->ldk, 0, cmax_scratch,
-                                                                 (__nv_bfloat16*)expand->hi,
-                                                                 (__nv_bfloat16*)expand->lo, expand->inv_scale, false);
-    return cudaGetLastError();
-}
-
 cudaError_t tc_build_grad_operands(const float2* pr4, int P, int npw, bool fp16, TcOperand* proj4, TcOperand* exp3,
                                    float* cmax_scratch, cudaStream_t st)
 {

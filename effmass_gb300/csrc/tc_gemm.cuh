@@ -58,14 +58,10 @@ size_t tc_rows_pad(size_t rows);  // rows of an operand allocation (whole 128-ro
 size_t tc_gemm_smem_bytes();
 int tc_proj_splits(int P, int nb, size_t ldk);
 
-// From the c64 projector matrix Pr[P][npw]: the projection operand [P][2npw]
-// and the expansion operand Pr^T [npw][2P] (expand buffers must be zeroed).
 // Test hook: poll limit of the MMA issuer's wait for a loaded stage (polls <
 // 0: the default, about a second); lowered only to make that wait run out.
 cudaError_t tc_set_issue_wait_limit(long polls);
 
-cudaError_t tc_build_proj_operands(const float2* pr, int P, int npw, bool fp16, TcOperand* proj, TcOperand* expand,
-                                   float* cmax_scratch, cudaStream_t st);
 // Gradient operands from the stacked c64 matrices [4P][npw] (Pr, dPr_x, dPr_y,
 // dPr_z): the projection operand [4P][2npw] and, per direction alpha, the
 // expansion operand [npw][4P] = (Pr^T | dPr_alpha^T) (buffers must be zeroed).
