@@ -38,7 +38,8 @@ def _bind(L):
 
 
 class Batch:
-    """A plan over items (hamiltonian, kid, nb); precision "fp32" or "fp64"."""
+    """A plan over items (hamiltonian, kid, nb); precision "fp32", "fp64", or
+    "tc" / "tc_bf16" (the nonlocal term as ragged tensor-core GEMMs)."""
 
     def __init__(self, items: Sequence[Tuple[object, int, int]], precision: str = "fp32", graph: bool = True,
                  tune: bool = True):

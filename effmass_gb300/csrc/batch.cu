@@ -11,6 +11,10 @@
 //                 lambda and the ragged expansion GEMM.
 // Cells are independent branches.  The sequence is captured once into a CUDA
 // graph, so a run is one graph launch whatever the number of k-points.
+// Tensor-core plans (HPSI_PREC_TC / TC_BF16) run the nonlocal term as ragged
+// tcgen05 GEMMs over an item table instead (tc_rag_project / tc_rag_expand:
+// generated projector tiles per k-point, band operands of up to 128 bands per
+// item), with the complex64 local term of the FP32 plans.
 //
 // Tuning: for each cell the plan times, on its own buffers, the x-pass line
 // shapes (z-values x bands per block), the plane-kernel block size, the
@@ -60,6 +64,16 @@ struct Group {
     bool tuned = false, cached = false;
     cudaStream_t s_main = nullptr, s_side = nullptr;
     cudaEvent_t ev_proj = nullptr, ev_done = nullptr;
+    // tensor-core plans: ragged items (<= 128 bands each) and their tables
+    std::vector<TcRagItem> rag;
+    TcRagItem* d_rag = nullptr;
+    int2* d_rag_bands = nullptr;   // (item, band)
+    int2* d_rag_rows = nullptr;    // (item, j < nbp)
+    int2* d_rag_tiles = nullptr;   // (item, 128-row G tile)
+    int rag_bands = 0, rag_rows = 0, rag_tiles = 0, rag_k1t_max = 0, rag_nz_max = 0;
+    unsigned char* rag_mem = nullptr;
+    unsigned* rag_rowmax = nullptr;
+    size_t rag_nrowmax = 0;
 };
 
 constexpr int kSplits[] = {1, 2, 4, 8, 16, 32};
@@ -118,6 +132,7 @@ static void batch_free(hpsi_batch* b)
         if (g.s_main) cudaStreamSynchronize(g.s_main);
         if (g.s_side) cudaStreamSynchronize(g.s_side);
         dfree(g.d_litems); dfree(g.d_band_item); dfree(g.d_xblk); dfree(g.d_gitems);
+        dfree(g.d_rag); dfree(g.d_rag_bands); dfree(g.d_rag_rows); dfree(g.d_rag_tiles); dfree(g.rag_mem);
         if (g.T) cudaFree(g.T);
         if (g.part) cudaFree(g.part);
         if (g.W) cudaFree(g.W);
@@ -135,6 +150,7 @@ static void batch_free(hpsi_batch* b)
 }
 
 static bool fp64(const hpsi_batch* b) { return b->prec == HPSI_PREC_FP64; }
+static bool tc(const hpsi_batch* b) { return b->prec == HPSI_PREC_TC || b->prec == HPSI_PREC_TC_BF16; }
 static size_t csize(const hpsi_batch* b) { return fp64(b) ? sizeof(double2) : sizeof(float2); }
 
 // x-pass band blocks of the current la.bb, uploaded to g.d_xblk
@@ -168,6 +184,18 @@ static cudaError_t launch_group_local(const hpsi_batch* b, const Group& g, cudaS
                                                    c->d_tw64, c->d_tw64 + c->n1, c->d_tw64 + c->n1 + c->n2, st);
     return launch_local_batch<float2, float>(g.la, g.nbands, g.max_nxs, g.nxblk, (float2*)g.T, c->d_v32, c->d_tw32,
                                              c->d_tw32 + c->n1, c->d_tw32 + c->n1 + c->n2, st);
+}
+
+static cudaError_t launch_group_rag_proj(const hpsi_batch* b, const Group& g, cudaStream_t st)
+{
+    return tc_rag_project(g.d_rag, (int)g.rag.size(), g.d_rag_bands, g.rag_bands, g.d_rag_rows, g.rag_rows, g.P,
+                          g.rag_k1t_max, g.rag_nz_max, b->prec == HPSI_PREC_TC, g.rag_rowmax, g.rag_nrowmax,
+                          g.ctx->d_err, st);
+}
+
+static cudaError_t launch_group_rag_exp(const hpsi_batch* b, const Group& g, cudaStream_t st)
+{
+    return tc_rag_expand(g.d_rag, g.d_rag_tiles, g.rag_tiles, g.P, b->prec == HPSI_PREC_TC, g.ctx->d_err, st);
 }
 
 static cudaError_t launch_group_proj(const hpsi_batch* b, const Group& g, int tile, int nsplit, cudaStream_t st)
@@ -273,6 +301,16 @@ static int tune_group(hpsi_batch* b, Group& g)
     }
     g.la.plane_threads = bpt;
     t.kt = bk; t.bb = bbb; t.plane_threads = bpt; t.local_ms = best;
+    if (tc(b)) {
+        // the ragged tensor-core GEMMs have no shape to choose: timed for the report
+        if (g.P > 0) {
+            if ((rc = time_ms(b, st, reps, [&] { return launch_group_rag_proj(b, g, st); }, &t.proj_ms))) return rc;
+            if ((rc = time_ms(b, st, reps, [&] { return launch_group_rag_exp(b, g, st); }, &t.exp_ms))) return rc;
+        }
+        g.tune = t;
+        g.tuned = true;
+        return HPSI_OK;
+    }
     // projection: tile x split
     best = 1e30;
     for (int ns : kSplits) {
@@ -325,6 +363,7 @@ static int apply_tune(hpsi_batch* b, Group& g)
     set_xshape(g, g.tune.kt, g.tune.bb);
     g.la.plane_threads = g.tune.plane_threads;
     if ((rc = upload_xblk(b, g))) return rc;
+    if (tc(b)) return HPSI_OK;
     return upload_gitems(b, g, g.tune.nsplit);
 }
 
@@ -335,14 +374,115 @@ static int enqueue(hpsi_batch* b, cudaStream_t origin)
     for (Group& g : b->groups) {
         BCUDA(b, cudaStreamWaitEvent(g.s_side, b->ev_start, 0));
         BCUDA(b, cudaStreamWaitEvent(g.s_main, b->ev_start, 0));
-        BCUDA(b, launch_group_proj(b, g, g.tune.proj_tile, g.tune.nsplit, g.s_side));
+        if (tc(b)) BCUDA(b, launch_group_rag_proj(b, g, g.s_side));
+        else BCUDA(b, launch_group_proj(b, g, g.tune.proj_tile, g.tune.nsplit, g.s_side));
         BCUDA(b, cudaEventRecord(g.ev_proj, g.s_side));
         BCUDA(b, launch_group_local(b, g, g.s_main));
         BCUDA(b, cudaStreamWaitEvent(g.s_main, g.ev_proj, 0));
-        BCUDA(b, launch_group_exp(b, g, g.tune.exp_tile, g.tune.nsplit, g.s_main));
+        if (tc(b)) BCUDA(b, launch_group_rag_exp(b, g, g.s_main));
+        else BCUDA(b, launch_group_exp(b, g, g.tune.exp_tile, g.tune.nsplit, g.s_main));
         BCUDA(b, cudaEventRecord(g.ev_done, g.s_main));
         BCUDA(b, cudaStreamWaitEvent(origin, g.ev_done, 0));
     }
+    return HPSI_OK;
+}
+
+// Ragged tensor-core items of a cell: one per (k-point, block of <= 128
+// bands), their operand workspace carved from one allocation, and the band,
+// row and tile tables of the launches.  Splits: K per split chosen so that
+// the projection fills about two waves of the SMs, at most 96 k-tiles (3072
+// of K) per FP32 accumulation chain.
+static int build_rag(hpsi_batch* b, Group& g)
+{
+    hpsi_ctx* c = g.ctx;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t k2 = tc_round_k(2 * (size_t)g.P);
+    long kt_sum = 0;
+    for (size_t i = 0; i < g.items.size(); ++i) {
+        const KSlot& s = c->slots[b->items[g.items[i]].kid];
+        const int nbk = ceil_div(b->items[g.items[i]].nb, 128);
+        kt_sum += (long)nbk * (long)(tc_round_k(2 * (size_t)s.npw) / 32);
+    }
+    int per = (int)std::max(1L, (kt_sum + 2L * sms - 1) / (2L * sms));
+    per = std::min(per, 96);
+    Carver cv;
+    struct Off { size_t b1h, b1l, b1s, part, w, b2h, b2l, b2s, rm; };
+    std::vector<Off> offs;
+    std::vector<int2> bands, rows, tiles;
+    g.rag.clear();
+    for (size_t i = 0; i < g.items.size(); ++i) {
+        const BItem& it = b->items[g.items[i]];
+        KSlot& s = c->slots[it.kid];
+        for (int b0 = 0; b0 < it.nb; b0 += 128) {
+            TcRagItem r{};
+            r.gen = s.tcgen[b->prec == HPSI_PREC_TC ? 0 : 1];
+            r.psi = b->psi + it.off + (size_t)b0 * s.npw;
+            r.hpsi = b->hpsi + it.off + (size_t)b0 * s.npw;
+            r.lam = s.d_lam;
+            r.nb = std::min(128, it.nb - b0);
+            r.nbp = tc_rag_nbp(r.nb);
+            r.npw = s.npw;
+            r.k1t = (int)(tc_round_k(2 * (size_t)s.npw) / 32);
+            r.per = per;
+            r.nz = ceil_div(r.k1t, per);
+            const size_t rp = tc_rows_pad(2 * (size_t)r.nbp), k1 = (size_t)r.k1t * 32;
+            Off o;
+            o.b1h = cv.take<uint16_t>(rp * k1);
+            o.b1l = cv.take<uint16_t>(rp * k1);
+            o.b1s = cv.take<float>(2 * (size_t)r.nbp);
+            o.part = cv.take<float>((size_t)r.nz * g.P * 2 * r.nbp);
+            o.w = cv.take<float2>((size_t)g.P * r.nb);
+            o.b2h = cv.take<uint16_t>(rp * k2);
+            o.b2l = cv.take<uint16_t>(rp * k2);
+            o.b2s = cv.take<float>(2 * (size_t)r.nbp);
+            offs.push_back(o);
+            const int ri = (int)g.rag.size();
+            for (int j = 0; j < r.nb; ++j) bands.push_back(make_int2(ri, j));
+            for (int j = 0; j < r.nbp; ++j) rows.push_back(make_int2(ri, j));
+            for (int t = 0; t < ceil_div(s.npw, 128); ++t) tiles.push_back(make_int2(ri, t));
+            g.rag_k1t_max = std::max(g.rag_k1t_max, r.k1t);
+            g.rag_nz_max = std::max(g.rag_nz_max, r.nz);
+            g.rag.push_back(r);
+        }
+    }
+    // band maxima of every item, contiguous (one memset per operand build)
+    const size_t rm0 = cv.off;
+    size_t nrm = 0;
+    for (TcRagItem& r : g.rag) nrm += (size_t)r.nbp;
+    cv.take<unsigned>(nrm);
+    if (g.rag.size() > 65535 || rows.size() > 65535 || bands.size() > 65535)
+        return bfail(b, HPSI_ERR_BAD_ARG, "a tensor-core plan holds at most 65535 bands of one cell");
+    BCUDA(b, dalloc(&g.rag_mem, cv.off));
+    BCUDA(b, cudaMemset(g.rag_mem, 0, cv.off));
+    g.rag_rowmax = reinterpret_cast<unsigned*>(g.rag_mem + rm0);
+    g.rag_nrowmax = nrm;
+    size_t rmo = 0;
+    for (size_t i = 0; i < g.rag.size(); ++i) {
+        TcRagItem& r = g.rag[i];
+        const Off& o = offs[i];
+        r.b1h = g.rag_mem + o.b1h;
+        r.b1l = g.rag_mem + o.b1l;
+        r.b1s = reinterpret_cast<float*>(g.rag_mem + o.b1s);
+        r.part = reinterpret_cast<float*>(g.rag_mem + o.part);
+        r.W = reinterpret_cast<float2*>(g.rag_mem + o.w);
+        r.b2h = g.rag_mem + o.b2h;
+        r.b2l = g.rag_mem + o.b2l;
+        r.b2s = reinterpret_cast<float*>(g.rag_mem + o.b2s);
+        r.rowmax = g.rag_rowmax + rmo;
+        rmo += (size_t)r.nbp;
+    }
+    g.rag_bands = (int)bands.size();
+    g.rag_rows = (int)rows.size();
+    g.rag_tiles = (int)tiles.size();
+    BCUDA(b, dalloc(&g.d_rag, g.rag.size()));
+    BCUDA(b, dalloc(&g.d_rag_bands, bands.size()));
+    BCUDA(b, dalloc(&g.d_rag_rows, rows.size()));
+    BCUDA(b, dalloc(&g.d_rag_tiles, tiles.size()));
+    BCUDA(b, cudaMemcpy(g.d_rag, g.rag.data(), g.rag.size() * sizeof(TcRagItem), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpy(g.d_rag_bands, bands.data(), bands.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpy(g.d_rag_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    BCUDA(b, cudaMemcpy(g.d_rag_tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
     return HPSI_OK;
 }
 
@@ -357,8 +497,9 @@ static int build_group(hpsi_batch* b, Group& g)
     for (int idx : g.items) {
         const BItem& it = b->items[idx];
         KSlot& s = c->slots[it.kid];
-        // the batched nonlocal term reads the complex64 (or complex128) projector matrix
-        int rc = prepare_slot(c, s, fp64(b) ? HPSI_PREC_FP64 : HPSI_PREC_FP32, false, 0);
+        // the batched nonlocal term reads the complex64 (or complex128) projector
+        // matrix, or, on the tensor cores, the k-point's generator tables
+        int rc = prepare_slot(c, s, tc(b) ? b->prec : (fp64(b) ? HPSI_PREC_FP64 : HPSI_PREC_FP32), false, 0);
         if (rc) return bfail(b, rc, "item %d: %s", idx, c->err.c_str());
         if (g.litems.empty()) g.P = s.P;
         if (s.P != g.P) return bfail(b, HPSI_ERR_STATE, "item %d: projector count differs within a cell", idx);
@@ -409,7 +550,10 @@ static int build_group(hpsi_batch* b, Group& g)
     BCUDA(b, cudaMemcpy(g.d_band_item, band_item.data(), band_item.size() * sizeof(int), cudaMemcpyHostToDevice));
     BCUDA(b, cudaMalloc(&g.T, std::max<size_t>(g.t_elems, 1) * cs));
     g.max_split = 1;
-    if (g.P > 0) {
+    if (g.P > 0 && tc(b)) {
+        int rc = build_rag(b, g);
+        if (rc) return rc;
+    } else if (g.P > 0) {
         for (int ns : kSplits)
             if ((size_t)ns * g.P * g.nbands * cs <= kPartBudget) g.max_split = ns;
         BCUDA(b, cudaMalloc(&g.part, (size_t)g.max_split * g.P * g.nbands * cs));
@@ -526,8 +670,9 @@ extern "C" int hpsi_batch_create(const hpsi_batch_item* items, int n_items, int 
     *out = nullptr;
     if (n_items <= 0 || !items) return bfail(nullptr, HPSI_ERR_BAD_ARG, "a batch needs at least one item");
     const int prec = flags & HPSI_PREC_MASK;
-    if (prec != HPSI_PREC_FP64 && prec != HPSI_PREC_FP32)
-        return bfail(nullptr, HPSI_ERR_BAD_ARG, "batched plans run HPSI_PREC_FP64 or HPSI_PREC_FP32 (got %d)", prec);
+    if (prec != HPSI_PREC_FP64 && prec != HPSI_PREC_FP32 && prec != HPSI_PREC_TC && prec != HPSI_PREC_TC_BF16)
+        return bfail(nullptr, HPSI_ERR_BAD_ARG,
+                     "batched plans run HPSI_PREC_FP64, HPSI_PREC_FP32, HPSI_PREC_TC or HPSI_PREC_TC_BF16 (got %d)", prec);
     hpsi_batch* b = new hpsi_batch();
     b->prec = prec;
     b->use_graph = !(flags & HPSI_BATCH_NO_GRAPH);
@@ -589,7 +734,20 @@ extern "C" int hpsi_batch_apply(hpsi_batch* b, const double* psi, double* hpsi, 
     }
     if ((rc = hpsi_batch_run(b, stream))) return rc;
     if (bytes) BCUDA(b, cudaMemcpyAsync(hpsi, b->hpsi, bytes, out, st));
-    if (!dev || (flags & HPSI_SYNC)) BCUDA(b, cudaStreamSynchronize(st));
+    if (!dev || (flags & HPSI_SYNC)) {
+        BCUDA(b, cudaStreamSynchronize(st));
+        if (tc(b)) {
+            // a bounded wait of the tensor-core GEMMs that gave up (any cell)
+            for (const Group& g : b->groups) {
+                int v = 0;
+                BCUDA(b, cudaMemcpy(&v, g.ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+                if (v) {
+                    cudaMemset(g.ctx->d_err, 0, sizeof(int));
+                    return bfail(b, HPSI_ERR_TIMEOUT, "tensor-core GEMM: a bounded pipeline wait gave up (site %d)", v);
+                }
+            }
+        }
+    }
     return HPSI_OK;
 }
 
@@ -599,7 +757,7 @@ extern "C" int hpsi_batch_info(const hpsi_batch* b, char* buf, size_t len)
     std::string s;
     char t[768];
     snprintf(t, sizeof t, "{\"precision\": \"%s\", \"graph\": %s, \"tuned\": %s, \"tune_ms\": %.3f, \"items\": %zu, "
-             "\"cells\": [", fp64(b) ? "fp64" : "fp32", b->exec ? "true" : "false", b->tuned ? "true" : "false",
+             "\"cells\": [", fp64(b) ? "fp64" : (b->prec == HPSI_PREC_TC ? "tc" : (tc(b) ? "tc_bf16" : "fp32")), b->exec ? "true" : "false", b->tuned ? "true" : "false",
              b->tune_ms, b->items.size());
     s += t;
     for (size_t i = 0; i < b->groups.size(); ++i) {

@@ -36,13 +36,16 @@ struct KSlot {
     bool pr64_grad = false;
     float2* pr32 = nullptr;
     bool pr32_grad = false;
-    // tensor-core H|psi>: generator tables of the projector operands (built
-    // from the FP64 tables on first use of a TC precision); tc_proj and
-    // tc_expand carry only their K depth and row factors
-    int tc_fmt = -1;               // -1 none, 0 FP16 split, 1 BF16 split
-    unsigned char* tc_mem = nullptr;
-    TcGen tcgen;
-    TcOperand tc_proj, tc_expand;
+    // tensor-core H|psi>: generator tables of the projector operands, one set
+    // per split format (0 FP16, 1 BF16), built from the FP64 tables on first
+    // use and kept until the slot is rebound (batch plans hold pointers into
+    // them); tc_proj and tc_expand carry only their K depth and row factors.
+    // tc_fmt: the format of the last preparation, which the call that follows
+    // it uses.
+    int tc_fmt = -1;
+    unsigned char* tc_mem[2] = {nullptr, nullptr};
+    TcGen tcgen[2];
+    TcOperand tc_proj[2], tc_expand[2];
     int tcg_fmt = -1;              // gradient operands (4P-row projection, per-direction expansion)
     unsigned char* tcg_mem = nullptr;
     TcOperand tcg_proj, tcg_exp[3];
@@ -70,7 +73,8 @@ inline void slot_free(KSlot& s)
 {
     dfree(s.d_kin); dfree(s.d_kvec); dfree(s.d_g); dfree(s.d_q); dfree(s.d_trig); dfree(s.d_ylm);
     dfree(s.d_beta); dfree(s.d_dbeta0); dfree(s.d_sf); dfree(s.d_plane); dfree(s.d_rows); dfree(s.d_lam);
-    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem); dfree(s.tcg_mem); dfree(s.hess64); dfree(s.hess32);
+    dfree(s.pr64); dfree(s.pr32); dfree(s.tc_mem[0]); dfree(s.tc_mem[1]); dfree(s.tcg_mem); dfree(s.hess64);
+    dfree(s.hess32);
     s = KSlot();
 }
 

@@ -532,9 +532,11 @@ static int check_call(hpsi_ctx* c, int kid, int nb, KSlot** sp, int flags)
 static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
 {
     if (s.P == 0 || s.npw == 0) return HPSI_OK;
-    if (s.tc_fmt == fmt && s.tc_mem) return HPSI_OK;
-    dfree(s.tc_mem);
     s.tc_fmt = -1;
+    if (s.tc_mem[fmt]) {
+        s.tc_fmt = fmt;
+        return HPSI_OK;
+    }
     // by rows: the distinct (radial function, lm) pairs of the projectors
     std::vector<int2> prow((size_t)s.P), byinfo;
     std::map<std::pair<int, int>, int> at;
@@ -549,13 +551,13 @@ static int ensure_tc(hpsi_ctx* c, KSlot& s, int fmt, cudaStream_t st)
         prow[(size_t)p] = make_int2(r.atom, it->second);
     }
     const int nby = (int)byinfo.size();
-    CUDA_TRY(c, dalloc(&s.tc_mem, tc_gen_bytes(s.P, s.npw, nby, c->natom)));
+    CUDA_TRY(c, dalloc(&s.tc_mem[fmt], tc_gen_bytes(s.P, s.npw, nby, c->natom)));
     int h = c->prof.open(PH_BUILD, st);
-    CUDA_TRY(c, tc_build_gen(s.tc_mem, s.P, s.npw, prow.data(), byinfo.data(), nby, c->natom, s.d_beta, s.d_ylm,
-                             s.d_sf, fmt == 0, &s.tcgen, st));
+    CUDA_TRY(c, tc_build_gen(s.tc_mem[fmt], s.P, s.npw, prow.data(), byinfo.data(), nby, c->natom, s.d_beta,
+                             s.d_ylm, s.d_sf, fmt == 0, &s.tcgen[fmt], st));
     c->prof.close(h, st, 4);
-    s.tc_proj = TcOperand{nullptr, nullptr, const_cast<float*>(s.tcgen.p_inv), tc_round_k(2 * (size_t)s.npw)};
-    s.tc_expand = TcOperand{nullptr, nullptr, const_cast<float*>(s.tcgen.g_inv), tc_round_k(2 * (size_t)s.P)};
+    s.tc_proj[fmt] = TcOperand{nullptr, nullptr, const_cast<float*>(s.tcgen[fmt].p_inv), tc_round_k(2 * (size_t)s.npw)};
+    s.tc_expand[fmt] = TcOperand{nullptr, nullptr, const_cast<float*>(s.tcgen[fmt].g_inv), tc_round_k(2 * (size_t)s.P)};
     s.tc_fmt = fmt;
     return HPSI_OK;
 }
@@ -643,8 +645,9 @@ static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi
     int h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_band_operand(psi, nb, s.npw, fp16, &t.B1, t.rowmax, st, have_max));
     c->prof.close(h, st, (have_max ? 1 : 2) + zero_rows);
-    CUDA_TRY(c, tc_projection(s.tc_proj, s.P, t.B1, nb, t.ns, fp16, t.part, s.d_lam, s.P, t.W, c->d_err, st,
-                              &c->prof, t.eterm, e_nl, &s.tcgen));
+    const int f = s.tc_fmt;
+    CUDA_TRY(c, tc_projection(s.tc_proj[f], s.P, t.B1, nb, t.ns, fp16, t.part, s.d_lam, s.P, t.W, c->d_err, st,
+                              &c->prof, t.eterm, e_nl, &s.tcgen[f]));
     h = c->prof.open(PH_OTHER, st);
     CUDA_TRY(c, tc_w_operand(t.W, s.P, nb, fp16, &t.B2, t.rowmax, st));
     c->prof.close(h, st, 2 + zero_rows);
@@ -656,8 +659,9 @@ static int tc_nonlocal_expand(hpsi_ctx* c, KSlot& s, int nb, double2* hpsi, unsi
                               bool energy, const float2* add32)
 {
     TcNl t = tc_layout(s, nb, ws, energy);
-    CUDA_TRY(c, tc_expansion(s.tc_expand, s.npw, t.B2, nb, s.tc_fmt == 0, hpsi, c->d_err, st, &c->prof, add32,
-                             &s.tcgen));
+    const int f = s.tc_fmt;
+    CUDA_TRY(c, tc_expansion(s.tc_expand[f], s.npw, t.B2, nb, f == 0, hpsi, c->d_err, st, &c->prof, add32,
+                             &s.tcgen[f]));
     return HPSI_OK;
 }
 

@@ -1535,3 +1535,423 @@ cudaError_t tc_set_issue_wait_limit(long polls)
     const uint32_t v = polls < 0 ? WAIT_LIMIT : (uint32_t)std::min<long>(polls, (long)WAIT_LIMIT);
     return cudaMemcpyToSymbol(g_tc_issue_wait_limit, &v, sizeof(v));
 }
+
+// ---------------------------------------------------------------- ragged (batched) GEMMs
+// The batch plans' nonlocal term on the tensor cores: the items of a cell
+// (k-points with their own projector tables and band blocks) share each
+// launch; every CTA reads its item from the table.  Band operands use the
+// compact layout of TcRagItem (re row j, im row nbp + j, N = 2 nbp).
+namespace {
+
+// band b of item I: max |re|, |im| over its len values (FROM_W: W [P][nb] column b)
+template <bool FROM_W>
+__global__ void rag_band_max_kernel(const TcRagItem* __restrict__ items, const int2* __restrict__ bands, int P)
+{
+    const int2 ib = bands[blockIdx.y];
+    const TcRagItem& I = items[ib.x];
+    const int b = ib.y;
+    const int len = FROM_W ? P : I.npw;
+    uint32_t mx = 0u;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        if (FROM_W) {
+            const float2 v = I.W[(size_t)i * I.nb + b];
+            mx = max(mx, max(abs_key(v.x), abs_key(v.y)));
+        } else {
+            const double2 v = I.psi[(size_t)b * I.npw + i];
+            mx = max(mx, max(abs_key(v.x), abs_key(v.y)));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(I.rowmax + b, mx);
+}
+
+// K of the expansion: 2 P rounded up to the stage depth
+__device__ __forceinline__ size_t rag_k2(int P) { return ((size_t)2 * P + BK - 1) / BK * BK; }
+
+// Rows j (re) and nbp + j (im) of item I's band operand, k = 4q .. 4q+3 per
+// thread: the projection's from psi (re row (x_r, x_i), im row (x_i, -x_r)),
+// the expansion's from W (re row (w_r, -w_i), im row (w_i, w_r)); bands
+// nb <= j < nbp are zero rows with unit factors.
+template <typename T, bool FROM_W>
+__global__ void rag_band_write_kernel(const TcRagItem* __restrict__ items, const int2* __restrict__ rows, int P,
+                                      bool fp16)
+{
+    const int2 ij = rows[blockIdx.y];
+    const TcRagItem& I = items[ij.x];
+    const int j = ij.y;
+    const size_t ldk = FROM_W ? rag_k2(P) : (size_t)I.k1t * BK;
+    const int len = FROM_W ? P : I.npw;
+    T* hi = reinterpret_cast<T*>(FROM_W ? I.b2h : I.b1h);
+    T* lo = reinterpret_cast<T*>(FROM_W ? I.b2l : I.b1l);
+    float* inv = FROM_W ? I.b2s : I.b1s;
+    const bool real = j < I.nb;
+    const float sc = real ? row_scale(__uint_as_float(I.rowmax[j]), fp16) : 1.f;
+    const size_t rre = (size_t)j, rim = (size_t)(I.nbp + j);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        inv[rre] = 1.f / sc;
+        inv[rim] = 1.f / sc;
+    }
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t k = 4 * (size_t)q;
+    if (k >= ldk) return;
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+    if (real) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int i = 2 * q + e;
+            if (i < len) {
+                const float2 v = FROM_W ? I.W[(size_t)i * I.nb + j] : to_c64(I.psi[(size_t)j * I.npw + i]);
+                const float r = v.x * sc, m = v.y * sc;  // sc: a power of two
+                if (!FROM_W) { a[2 * e] = r; a[2 * e + 1] = m; c[2 * e] = m; c[2 * e + 1] = -r; }
+                else { a[2 * e] = r; a[2 * e + 1] = -m; c[2 * e] = m; c[2 * e + 1] = r; }
+            }
+        }
+    }
+    __align__(8) T ah[4], al[4], ch[4], cl[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        split2<T>(a[e], ah[e], al[e]);
+        split2<T>(c[e], ch[e], cl[e]);
+    }
+    const size_t ore = tile_off(rre, k, ldk), oim = tile_off(rim, k, ldk);
+    *reinterpret_cast<uint2*>(hi + ore) = *reinterpret_cast<const uint2*>(ah);
+    *reinterpret_cast<uint2*>(lo + ore) = *reinterpret_cast<const uint2*>(al);
+    *reinterpret_cast<uint2*>(hi + oim) = *reinterpret_cast<const uint2*>(ch);
+    *reinterpret_cast<uint2*>(lo + oim) = *reinterpret_cast<const uint2*>(cl);
+}
+
+// bulk copies of the first n rows of a band operand's k-tile kt (the tiled
+// layout keeps rows 0-127 and 128-255 in separate 8 KB tiles)
+__device__ __forceinline__ void rag_load_b(unsigned char* dst, const unsigned char* src, size_t KT, size_t kt, int n,
+                                           uint64_t* bar)
+{
+    const int n0 = min(n, 128);
+    bulk_load(dst, src + kt * A_TILE, (uint32_t)n0 * 64u, bar);
+    if (n > 128) bulk_load(dst + A_TILE, src + (KT + kt) * A_TILE, (uint32_t)(n - 128) * 64u, bar);
+}
+
+// Split-K projection of every item: CTA (m tile, item, split).  Warp roles as
+// tc_gemm_kernel<GEN>; N = 2 nbp of the item (idesc per CTA); partials
+// row-major [z][P][N] through the same per-warp transpose.
+template <bool GEN_FP16>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    rag_proj_kernel(const TcRagItem* __restrict__ items, int P, int* err)
+{
+    const TcRagItem& I = items[blockIdx.y];
+    if ((int)blockIdx.z >= I.nz) return;  // uniform: before any barrier or TMEM allocation
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    TcSmem* sh = reinterpret_cast<TcSmem*>(tiles + STAGES * STAGE_BYTES);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * BM;
+    const int N = 2 * I.nbp;
+    const int KT = I.k1t;
+    const int kt0 = blockIdx.z * I.per;
+    const int nk = max(0, min(KT, kt0 + I.per) - kt0);
+    const uint32_t idesc = idesc_f16(BM, N, GEN_FP16 ? 0u : 1u);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->gfull[s], GEN_THREADS / 32);
+            mbar_init(&sh->empty[s], 1);
+        }
+        mbar_init(&sh->done, 1);
+        sh->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        int issued = 0;
+        for (int it = 0; it < nk; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (it / STAGES) & 1;
+            if (!mbar_wait_abort(&sh->empty[s], ph ^ 1, &sh->abort_flag)) {
+                if (!*(volatile uint32_t*)&sh->abort_flag) { atomicExch(err, 1); sh->abort_flag = 1; }
+                break;
+            }
+            if (*(volatile uint32_t*)&sh->abort_flag) break;
+            unsigned char* st = tiles + s * STAGE_BYTES;
+            mbar_arrive_expect_tx(&sh->full[s], 2u * (uint32_t)N * 64u);
+            const size_t kt = (size_t)(kt0 + it);
+            rag_load_b(st + 2 * A_TILE, I.b1h, (size_t)KT, kt, N, &sh->full[s]);
+            rag_load_b(st + 2 * A_TILE + B_TILE, I.b1l, (size_t)KT, kt, N, &sh->full[s]);
+            issued = it + 1;
+        }
+        for (int it = max(0, issued - STAGES); it < issued; ++it) mbar_wait(&sh->full[it % STAGES], (it / STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t lim = g_tc_issue_wait_limit;
+        for (int it = 0; it < nk; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (it / STAGES) & 1;
+            if (!mbar_wait_n(&sh->full[s], ph, lim) || !mbar_wait_n(&sh->gfull[s], ph, lim)) {
+                atomicExch(err, 2);
+                sh->abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
+            const uint64_t ah = sdesc_sw64(st), al = sdesc_sw64(st + A_TILE);
+            const uint64_t bh = sdesc_sw64(st + 2 * A_TILE), bl = sdesc_sw64(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+                const uint32_t acc = tmem + (uint32_t)((it & 1) * BN);
+                const uint32_t first = (it < 2 && kk == 0) ? 0u : 1u;
+                tc_mma(acc, ah + adv, bh + adv, idesc, first);
+                tc_mma(acc, ah + adv, bl + adv, idesc, 1u);
+                tc_mma(acc, al + adv, bh + adv, idesc, 1u);
+            }
+            tc_commit(&sh->empty[s]);
+        }
+        tc_commit(&sh->done);
+    } else if (warp >= 2) {
+        using GT = typename std::conditional<GEN_FP16, __half, __nv_bfloat16>::type;
+        gen_loop_rows<GT>(I.gen, sh, tiles, m0, kt0, nk, threadIdx.x - 64, err);
+        const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int row = m0 + q * 32 + lane;
+        bool ok = mbar_wait(&sh->done, 0);
+        tc_fence_after();
+        if (!ok) atomicExch(err, 3);
+        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
+        const bool go = __all_sync(0xffffffffu, ok && nk > 0 && !*(volatile uint32_t*)&sh->abort_flag);
+        if (go) {
+            const float sa = (row < P) ? I.gen.p_inv[row] : 0.f;
+            const bool two = nk > 1;
+            float* tr = reinterpret_cast<float*>(tiles) + (warp - 2) * 32 * 33;
+            const int rbase = m0 + q * 32;
+            float* out = I.part + ((size_t)blockIdx.z * P + rbase) * (size_t)N;
+#pragma unroll 1
+            for (int c0 = half * (BN / 2); c0 < min(N, (half + 1) * (BN / 2)); c0 += 32) {
+                float v[32], w[32];
+                tmem_ld32(tbase + c0, v);
+                if (two) {
+                    tmem_ld32(tbase + BN + c0, w);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[i] += w[i];
+                }
+                const int col = c0 + lane;
+                const float sbl = col < N ? I.b1s[col] : 0.f;
+                __syncwarp();
+#pragma unroll
+                for (int i = 0; i < 32; ++i) tr[lane * 33 + i] = v[i] * sa;
+                __syncwarp();
+#pragma unroll 8
+                for (int i = 0; i < 32; ++i)
+                    if (rbase + i < P && col < N) out[(size_t)i * N + col] = tr[i * 33 + lane] * sbl;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// W[p][b] = lambda_p sum_z (C[z][p][b] + i C[z][p][nbp + b]), compensated FP32
+__global__ void rag_reduce_kernel(const TcRagItem* __restrict__ items, int P)
+{
+    const TcRagItem& I = items[blockIdx.y];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= P * I.nb) return;
+    const int p = idx / I.nb, b = idx % I.nb;
+    const int N = 2 * I.nbp;
+    const size_t zs = (size_t)P * N;
+    const float* pre = I.part + (size_t)p * N + b;
+    const float* pim = pre + I.nbp;
+    Sum2f re, im;
+    for (int z = 0; z < I.nz; ++z) {
+        re.add(pre[z * zs]);
+        im.add(pim[z * zs]);
+    }
+    const float f = I.lam ? d2f_bits(I.lam[p]) : 1.f;
+    I.W[idx] = make_float2(f * re.value(), f * im.value());
+}
+
+// Expansion of every item: CTA = one 128-row G tile (item, tile) of tiles.
+// Warp 0 copies the W' tiles, warp 1 issues the MMAs (one accumulator),
+// warps 2-9 generate Pr^T and then add into hpsi, the 16-band chunks of the
+// item split between the two warp halves.
+template <bool GEN_FP16>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    rag_exp_kernel(const TcRagItem* __restrict__ items, const int2* __restrict__ tiles_of, int P, int* err)
+{
+    const int2 it2 = tiles_of[blockIdx.x];
+    const TcRagItem& I = items[it2.x];
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    TcSmem* sh = reinterpret_cast<TcSmem*>(tiles + STAGES * STAGE_BYTES);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = it2.y * BM;
+    const int N = 2 * I.nbp;
+    const int KT = (int)(rag_k2(P) / BK);
+    const int nk = KT;
+    const uint32_t idesc = idesc_f16(BM, N, GEN_FP16 ? 0u : 1u);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->gfull[s], GEN_THREADS / 32);
+            mbar_init(&sh->empty[s], 1);
+        }
+        mbar_init(&sh->done, 1);
+        sh->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh->tmem_base)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = sh->tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        int issued = 0;
+        for (int it = 0; it < nk; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (it / STAGES) & 1;
+            if (!mbar_wait_abort(&sh->empty[s], ph ^ 1, &sh->abort_flag)) {
+                if (!*(volatile uint32_t*)&sh->abort_flag) { atomicExch(err, 1); sh->abort_flag = 1; }
+                break;
+            }
+            if (*(volatile uint32_t*)&sh->abort_flag) break;
+            unsigned char* st = tiles + s * STAGE_BYTES;
+            mbar_arrive_expect_tx(&sh->full[s], 2u * (uint32_t)N * 64u);
+            rag_load_b(st + 2 * A_TILE, I.b2h, (size_t)KT, (size_t)it, N, &sh->full[s]);
+            rag_load_b(st + 2 * A_TILE + B_TILE, I.b2l, (size_t)KT, (size_t)it, N, &sh->full[s]);
+            issued = it + 1;
+        }
+        for (int it = max(0, issued - STAGES); it < issued; ++it) mbar_wait(&sh->full[it % STAGES], (it / STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t lim = g_tc_issue_wait_limit;
+        for (int it = 0; it < nk; ++it) {
+            const int s = it % STAGES;
+            const uint32_t ph = (it / STAGES) & 1;
+            if (!mbar_wait_n(&sh->full[s], ph, lim) || !mbar_wait_n(&sh->gfull[s], ph, lim)) {
+                atomicExch(err, 2);
+                sh->abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t st = smem_u32(tiles + s * STAGE_BYTES);
+            const uint64_t ah = sdesc_sw64(st), al = sdesc_sw64(st + A_TILE);
+            const uint64_t bh = sdesc_sw64(st + 2 * A_TILE), bl = sdesc_sw64(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+                const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+                const uint32_t first = (it == 0 && kk == 0) ? 0u : 1u;
+                tc_mma(tmem, ah + adv, bh + adv, idesc, first);
+                tc_mma(tmem, ah + adv, bl + adv, idesc, 1u);
+                tc_mma(tmem, al + adv, bh + adv, idesc, 1u);
+            }
+            tc_commit(&sh->empty[s]);
+        }
+        tc_commit(&sh->done);
+    } else if (warp >= 2) {
+        using GT = typename std::conditional<GEN_FP16, __half, __nv_bfloat16>::type;
+        gen_loop_cols<GT>(I.gen, sh, tiles, m0, 0, nk, threadIdx.x - 64, err);
+        const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int row = m0 + q * 32 + lane;
+        bool ok = mbar_wait(&sh->done, 0);
+        tc_fence_after();
+        if (!ok) atomicExch(err, 3);
+        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16);
+        const bool go = __all_sync(0xffffffffu, ok && !*(volatile uint32_t*)&sh->abort_flag);
+        if (go) {
+            TcEpilogue ep{};
+            ep.hpsi = I.hpsi;
+            ep.ldh = I.npw;
+            ep.nb = I.nb;
+            ep.sb_scale = I.b2s;
+            const float sa = (row < I.npw) ? I.gen.g_inv[row] : 0.f;
+            // column j: re of band j, nbp + j: its im; 16-band chunks alternate between the halves
+#pragma unroll 1
+            for (int c0 = 16 * half; c0 < I.nbp; c0 += 32) {
+                float re[16], im[16];
+                tmem_ld16(tbase + c0, re);
+                tmem_ld16(tbase + I.nbp + c0, im);
+                if (row < I.npw) expand_rmw(ep, row, sa, c0, c0, re, im);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+template <typename T>
+static void rag_operands(bool from_w, const TcRagItem* d_items, const int2* d_bands, int nbands, const int2* d_rows,
+                         int nrows, int P, int len_max, size_t ldk_max, unsigned* rowmax_all, size_t n_rowmax,
+                         bool fp16, cudaStream_t st)
+{
+    cudaMemsetAsync(rowmax_all, 0, n_rowmax * sizeof(unsigned), st);
+    const int chunks = min(64, ceil_div(len_max, 256 * 4));
+    if (from_w) rag_band_max_kernel<true><<<dim3(chunks, nbands), 256, 0, st>>>(d_items, d_bands, P);
+    else rag_band_max_kernel<false><<<dim3(chunks, nbands), 256, 0, st>>>(d_items, d_bands, P);
+    const dim3 g(ceil_div((long)(ldk_max / 4), 256), nrows);
+    if (from_w) rag_band_write_kernel<T, true><<<g, 256, 0, st>>>(d_items, d_rows, P, fp16);
+    else rag_band_write_kernel<T, false><<<g, 256, 0, st>>>(d_items, d_rows, P, fp16);
+}
+
+}  // namespace
+
+int tc_rag_nbp(int nb) { return (nb + 15) / 16 * 16; }
+
+cudaError_t tc_rag_project(const TcRagItem* d_items, int n_items, const int2* d_bands, int nbands, const int2* d_rows,
+                           int nrows, int P, int k1t_max, int nz_max, bool fp16, unsigned* rowmax_all,
+                           size_t n_rowmax, int* err, cudaStream_t st)
+{
+    if (n_items == 0 || nbands == 0 || P == 0) return cudaSuccess;
+    if (n_items > 65535 || nrows > 65535 || nbands > 65535 || nz_max > 65535) return cudaErrorInvalidValue;
+    const size_t k1_max = (size_t)k1t_max * BK;
+    const int npw_max = (int)(k1_max / 2);
+    if (fp16) rag_operands<__half>(false, d_items, d_bands, nbands, d_rows, nrows, P, npw_max, k1_max, rowmax_all,
+                                   n_rowmax, true, st);
+    else rag_operands<__nv_bfloat16>(false, d_items, d_bands, nbands, d_rows, nrows, P, npw_max, k1_max, rowmax_all,
+                                     n_rowmax, false, st);
+    cudaError_t e;
+    const size_t smem = tc_gemm_smem_bytes();
+    auto k = fp16 ? rag_proj_kernel<true> : rag_proj_kernel<false>;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    k<<<dim3(ceil_div(P, BM), n_items, nz_max), TC_THREADS, smem, st>>>(d_items, P, err);
+    rag_reduce_kernel<<<dim3(ceil_div((long)P * 128, 256), n_items), 256, 0, st>>>(d_items, P);
+    const size_t k2 = tc_round_k(2 * (size_t)P);
+    if (fp16) rag_operands<__half>(true, d_items, d_bands, nbands, d_rows, nrows, P, P, k2, rowmax_all, n_rowmax,
+                                   true, st);
+    else rag_operands<__nv_bfloat16>(true, d_items, d_bands, nbands, d_rows, nrows, P, P, k2, rowmax_all, n_rowmax,
+                                     false, st);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_rag_expand(const TcRagItem* d_items, const int2* d_tiles, int ntiles, int P, bool fp16, int* err,
+                          cudaStream_t st)
+{
+    if (ntiles == 0 || P == 0) return cudaSuccess;
+    cudaError_t e;
+    const size_t smem = tc_gemm_smem_bytes();
+    auto k = fp16 ? rag_exp_kernel<true> : rag_exp_kernel<false>;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    k<<<ntiles, TC_THREADS, smem, st>>>(d_items, d_tiles, P, err);
+    return cudaGetLastError();
+}

@@ -89,3 +89,38 @@ cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, 
 // (gen as in tc_projection; A.inv_scale = gen->g_inv)
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
                          cudaStream_t st, Prof* prof, const float2* add32 = nullptr, const TcGen* gen = nullptr);
+
+// ---- ragged (batched) tensor-core nonlocal term ------------------------------
+// One item per (k-point, band block) of a batch plan, nb <= 128 bands.  Band
+// operands use the compact row layout: band j's re row at j, its im row at
+// nbp + j (nbp = nb rounded up to 16, N = 2 nbp <= 256 rows, tiled like the
+// other operands).  All items of a call share P (and so K = tc_round_k(2 P)
+// of the expansion).
+struct TcRagItem {
+    TcGen gen;                   // the k-point's generator tables
+    const double2* psi;          // [nb][npw]
+    double2* hpsi;               // [nb][npw] (+= the nonlocal term)
+    const double* lam;           // [P]
+    int nb, nbp, npw;
+    int k1t;                     // k-tiles of the projection: tc_round_k(2 npw) / 32
+    int per, nz;                 // k-tiles per split, splits (every split holds >= 1 k-tile)
+    unsigned char *b1h, *b1l;    // projection band operand, tc_rows_pad(2 nbp) x (32 k1t)
+    float* b1s;                  // its row factors [2 nbp]
+    float* part;                 // [nz][P][2 nbp] split partials
+    float2* W;                   // [P][nb] lambda <p|psi>
+    unsigned char *b2h, *b2l;    // expansion band operand, tc_rows_pad(2 nbp) x tc_round_k(2 P)
+    float* b2s;                  // [2 nbp]
+    unsigned* rowmax;            // [nbp] band maxima scratch
+};
+int tc_rag_nbp(int nb);          // nb rounded up to 16
+// Projection chain of every item: band operands from psi, split-K projection
+// GEMM (generated projector tiles), reduction to W, band operands of W.
+// bands: (item, band) of every band of the call; rows: (item, j) for j < nbp
+// of every item; rowmax_all / n_rowmax: the items' rowmax arrays, contiguous.
+cudaError_t tc_rag_project(const TcRagItem* d_items, int n_items, const int2* d_bands, int nbands, const int2* d_rows,
+                           int nrows, int P, int k1t_max, int nz_max, bool fp16, unsigned* rowmax_all,
+                           size_t n_rowmax, int* err, cudaStream_t st);
+// Expansion of every item over its 128-row G tiles (item, tile) in tiles.
+cudaError_t tc_rag_expand(const TcRagItem* d_items, const int2* d_tiles, int ntiles, int P, bool fp16, int* err,
+                          cudaStream_t st);
+

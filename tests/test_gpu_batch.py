@@ -2,8 +2,9 @@
 of several cells with ragged npw and band counts.
 
 Pinned to the reference through the golden fixtures (an item of the batch is
-a fixture's k-point and bands): FP64 within 1e-12, FP32 within 1e-6.  Every
-other item is compared with the per-k hpsi_apply of the same precision
+a fixture's k-point and bands): FP64 within 1e-12, FP32 and the tensor-core
+plans (ragged tcgen05 GEMMs, split FP16) within 1e-6, split BF16 within 2e-6.
+Every other item is compared with the per-k hpsi_apply of the same precision
 (itself pinned by test_gpu_parity.py)."""
 import numpy as np
 import pytest
@@ -56,9 +57,12 @@ def _plan(items, precision, **kw):
     return Batch([(H, kid, psi.shape[0]) for H, kid, psi in items], precision=precision, **kw)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+TOL = {"fp64": 1e-12, "fp32": 1e-6, "tc": 1e-6, "tc_bf16": 2e-6}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "tc", "tc_bf16"])
 def test_batch_matches_reference_and_per_k(cells, precision):
-    tol = {"fp64": 1e-12, "fp32": 1e-6}[precision]
+    tol = TOL[precision]
     items = _items(cells)
     with _plan(items, precision) as plan:
         psi = plan.pack([p for _, _, p in items])
@@ -155,12 +159,40 @@ def test_rebinding_a_slot_invalidates_the_plan(cells):
 
 
 def test_unbound_slot_and_precision_refused(cells):
-    from effmass_gb300._lib import HpsiError
+    import ctypes as C
+    from effmass_gb300._lib import HpsiError, load
     from effmass_gb300.batch import Batch
     H, *_ = cells["tinyd"]
     with pytest.raises(HpsiError) as ei:
         Batch([(H, 99, 4)], precision="fp32")
     assert ei.value.status == abi.HPSI_ERR_STATE
-    with pytest.raises(HpsiError) as ei:
-        Batch([(H, 0, 4)], precision="tc")
-    assert ei.value.status == abi.HPSI_ERR_BAD_ARG
+    lib = load()
+    Batch([(H, 0, 1)], precision="fp32").close()  # binds the batch entry points
+    arr = (abi.HpsiBatchItem * 1)(abi.HpsiBatchItem(H.ctx.value, 0, 4))
+    out = C.c_void_p()
+    assert lib.hpsi_batch_create(arr, 1, 7, C.byref(out)) == abi.HPSI_ERR_BAD_ARG  # no such precision
+    assert not out.value
+
+
+@pytest.mark.parametrize("precision", ["tc", "tc_bf16"])
+def test_tensor_core_plan_blocks_of_bands(cells, precision):
+    """Items of more than 128 bands (split into 128-band blocks of the ragged
+    GEMMs, the last one with N = 2 nbp > 128 rows), items of one band, and the
+    graph against eager launches: all equal the per-k tensor-core hpsi_apply."""
+    from effmass_gb300 import system as S
+    H, kps, _, _ = cells["fcc2"]
+    items = [(H, 1, S.make_bands(kps[1], 200, seed=5)), (H, 2, S.make_bands(kps[2], 1, seed=6)),
+             (H, 3, S.make_bands(kps[3], 17, seed=7))]
+    res = []
+    for graph in (True, False):
+        with _plan(items, precision, graph=graph, tune=False) as plan:
+            psi = plan.pack([p for _, _, p in items])
+            hpsi = plan.empty()
+            plan.apply(psi, hpsi)
+            assert plan.info()["precision"] == precision
+            res.append(plan.split(hpsi))
+    for (H_, kid, p), got, got_eager in zip(items, res[0], res[1]):
+        ref = np.zeros_like(p)
+        H_.apply(kid, p.shape[0], p, ref, precision)
+        assert rel_err(got, ref) <= TOL[precision], (kid, rel_err(got, ref))
+        assert np.array_equal(got, got_eager)
