@@ -611,8 +611,8 @@ def batched_cells():
 
 
 def run_batched(args):
-    """All k-points of both cells in one graph-launched plan (FP32 and FP64),
-    against a per-k-point loop of hpsi_apply on the same device data."""
+    """All k-points of both cells in one graph-launched plan (FP32, tensor-core
+    and FP64), against a per-k-point loop of hpsi_apply on the same device data."""
     import numpy as np
     import torch
     from effmass_gb300.batch import Batch
@@ -637,7 +637,7 @@ def run_batched(args):
         return e0.elapsed_time(e1) / n
 
     res, outs, infos = {}, {}, {}
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "tc", "fp64"):
         t0 = time.perf_counter()
         plan = Batch(items, precision=prec)
         create_s = time.perf_counter() - t0
@@ -673,18 +673,21 @@ def run_batched(args):
             res[prec]["per_k_ms_per_run"] = ev_time(per_k, 2)
             del tp, th
         plan.close()
-    a32, a64 = outs["fp32"], outs["fp64"]
-    err = float(np.linalg.norm(a32 - a64) / np.linalg.norm(a64))
-    # band energies <psi_n|H|psi_n> (FP64 sums on the host of both results)
-    psi_all = np.concatenate([p.ravel() for p in psis])
-    de, off = 0.0, 0
-    for p in psis:
-        n = p.size
-        e32 = np.einsum("bg,bg->b", p.conj(), a32[off:off + n].reshape(p.shape)).real
-        e64 = np.einsum("bg,bg->b", p.conj(), a64[off:off + n].reshape(p.shape)).real
-        de = max(de, float(np.abs(e32 - e64).max()))
-        off += n
-    del psi_all
+    a64 = outs["fp64"]
+
+    def accuracy(a):
+        """relative 2-norm error against the FP64 plan and the largest band-energy
+        difference <psi_n|H|psi_n> (FP64 sums on the host)"""
+        de, off = 0.0, 0
+        for p in psis:
+            n = p.size
+            e = np.einsum("bg,bg->b", p.conj(), a[off:off + n].reshape(p.shape)).real
+            e64 = np.einsum("bg,bg->b", p.conj(), a64[off:off + n].reshape(p.shape)).real
+            de = max(de, float(np.abs(e - e64).max()))
+            off += n
+        return float(np.linalg.norm(a - a64) / np.linalg.norm(a64)), de
+    err, de = accuracy(outs["fp32"])
+    err_tc, de_tc = accuracy(outs["tc"])
     # local-term roofline per cell from the tuner's event timing of the three FFT launches:
     # algorithmic bytes per band 3*N*8 + 3*npw*8 (complex64 grid passes, psi read, hpsi read+write)
     hbm, _, src = peaks()
@@ -706,6 +709,11 @@ def run_batched(args):
         "value": r32["value"], "unit": "band-apps/s", "ms_per_run": r32["ms_per_run"],
         "e2e_value": r32["e2e_value"], "fp64_value": res["fp64"]["value"],
         "speedup_vs_fp64": r32["value"] / res["fp64"]["value"],
+        "tc": {"value": res["tc"]["value"], "ms_per_run": res["tc"]["ms_per_run"], "e2e_value": res["tc"]["e2e_value"],
+               "rel_err_vs_fp64": err_tc, "band_energy_max_abs_diff_Ha": de_tc,
+               "nonlocal_ms_proj_exp": {"%dx%dx%d" % tuple(c["grid"]): [c["timed"]["proj_ms"], c["timed"]["exp_ms"]]
+                                        for c in infos["tc"]["cells"]},
+               "note": "nonlocal term as ragged tcgen05 GEMMs (split FP16, generated projector tiles)"},
         "eager_ms_per_run": r32["eager_ms_per_run"], "per_k_api_ms_per_run": r32["per_k_ms_per_run"],
         "rel_err_fp32_vs_fp64": err, "band_energy_max_abs_diff_Ha": de,
         "plan_create_s": {k: v["create_s"] for k, v in res.items()},
