@@ -366,9 +366,9 @@ def run_gb300(args, rank, world, local):
                 "frac": ach / bf16, "peak_source": src + " dense bf16 tensor peak"}
     # DRAM bytes (read + write) of one launch of this workload (128 bands per
     # launch, 64-atom cell, tensor-core path) from ncu --set full captures of
-    # this bench command: x pass 219.2 + 157.9 MB, G->r planes 76.3 + 159.4 MB,
-    # r->G planes 294.2 + 29.1 MB
-    ncu_traffic = {"x_pass": 377.15e6, "g2r_planes": 235.76e6, "r2g_planes": 323.30e6}
+    # this bench command: x pass 219.2 + 156.7 MB, G->r planes 76.3 + 159.6 MB,
+    # r->G planes 294.2 + 29.1 MB (cold caches: ncu flushes them between passes)
+    ncu_traffic = {"x_pass": 375.91e6, "g2r_planes": 235.86e6, "r2g_planes": 323.32e6}
     roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec != "fp64") else None
     if roof["traffic"] is not None and bound == "hbm":
         roof["algorithmic_bytes_per_launch"] = alg[dom][1] / prof[dom][1]
@@ -382,6 +382,16 @@ def run_gb300(args, rank, world, local):
         roof_gemm = {"bound": "tensor", "kernel": "proj_gemm", "achieved": a_g, "peak": bf16, "unit": "TFLOP/s",
                      "frac": a_g / bf16, "peak_source": src + " dense bf16 tensor peak",
                      "note": "algorithmic flops 8*P*npw*nb; the split operands issue 3x that on the tensor pipe"}
+    # the whole local term (the three FFT passes) on its canonical bytes
+    roof_local = None
+    loc = [k for k in ("g2r_planes", "x_pass", "r2g_planes") if prof.get(k, (0, 0))[1]]
+    if len(loc) == 3:
+        t_l = sum(prof[k][0] for k in loc)
+        b_l = sum(alg[k][1] for k in loc)
+        a_l = b_l / (t_l * 1e-3) / 1e9
+        roof_local = {"bound": "hbm", "kernels": loc, "achieved": a_l, "peak": hbm, "unit": "GB/s",
+                      "frac": a_l / hbm, "peak_source": src, "bytes_per_band": b_l / (steps * nb),
+                      "ms_per_step": t_l / steps}
     phases = {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps} for k, v in prof.items() if v[1]}
 
     serving = None
@@ -421,7 +431,8 @@ def run_gb300(args, rank, world, local):
         "rayleigh_quotient_of_hpsi_max_abs_diff_Ha": de, "band_energies": energies, "density": density,
         "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "grad_value": grad_value, "grad_unit": "band-apps/s of dH/dk_{x,y,z}|psi> (all three directions)",
-        "e2e": e2e, "roofline": roof, "roofline_gemm": roof_gemm, "phases": phases, "gpu_launches": gpu_launches,
+        "e2e": e2e, "roofline": roof, "roofline_gemm": roof_gemm, "roofline_local": roof_local, "phases": phases,
+        "gpu_launches": gpu_launches,
         "cpu_baseline": cpu, "clocks": clk, "serving": serving, "batched": batched, "kp": kp_out, "sternheimer": stern,
     }
     if rank == 0:
