@@ -382,12 +382,13 @@ def run_gb300(args, rank, world, local):
         roof_gemm = {"bound": "tensor", "kernel": "proj_gemm", "achieved": a_g, "peak": bf16, "unit": "TFLOP/s",
                      "frac": a_g / bf16, "peak_source": src + " dense bf16 tensor peak",
                      "note": "algorithmic flops 8*P*npw*nb; the split operands issue 3x that on the tensor pipe"}
-    # the whole local term (the three FFT passes) on its canonical bytes
+    # the whole local term (the three FFT passes) on its canonical bytes per
+    # band, 3 N s_c + 3 npw s_c, plus V (4 or 8 B per grid point) once per band block
     roof_local = None
     loc = [k for k in ("g2r_planes", "x_pass", "r2g_planes") if prof.get(k, (0, 0))[1]]
     if len(loc) == 3:
         t_l = sum(prof[k][0] for k in loc)
-        b_l = sum(alg[k][1] for k in loc)
+        b_l = steps * (nb * (3 * N * csz + 3 * npw * csz) + N * csz // 2)
         a_l = b_l / (t_l * 1e-3) / 1e9
         roof_local = {"bound": "hbm", "kernels": loc, "achieved": a_l, "peak": hbm, "unit": "GB/s",
                       "frac": a_l / hbm, "peak_source": src, "bytes_per_band": b_l / (steps * nb),

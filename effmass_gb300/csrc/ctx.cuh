@@ -109,6 +109,10 @@ struct hpsi_ctx {
     // only the tensor-core expansion reads, runs beside the FFT passes
     cudaStream_t copy = nullptr;
     cudaEvent_t ev_copy_after = nullptr, ev_copy_done = nullptr;
+    // hpsi_apply with host buffers on the tensor-core path: hpsi moves in and
+    // out in two G halves (uploads on the copy stream, the first half's
+    // download on the side stream beside the second half's expansion)
+    cudaEvent_t ev_half_in[2] = {nullptr, nullptr}, ev_half_exp = nullptr, ev_half_out = nullptr;
     long gen_counter = 0;         // source of KSlot::gen
     double* d_hess = nullptr;     // Hessian radial tables [nrad][3][hess_nq] (F0, F1, F3), raw
     int hess_nq = 0;

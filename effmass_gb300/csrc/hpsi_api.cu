@@ -45,6 +45,8 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     if (c->copy) cudaStreamDestroy(c->copy);
     if (c->ev_copy_after) cudaEventDestroy(c->ev_copy_after);
     if (c->ev_copy_done) cudaEventDestroy(c->ev_copy_done);
+    for (cudaEvent_t e : {c->ev_half_in[0], c->ev_half_in[1], c->ev_half_exp, c->ev_half_out})
+        if (e) cudaEventDestroy(e);
     for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof.pool) cudaEventDestroy(e);
     delete c;
@@ -132,6 +134,8 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
     CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_copy_after, cudaEventDisableTiming));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_copy_done, cudaEventDisableTiming));
+    for (cudaEvent_t* e : {&c->ev_half_in[0], &c->ev_half_in[1], &c->ev_half_exp, &c->ev_half_out})
+        CUDA_TRY(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     CUDA_TRY(c, dalloc(&c->d_err, (size_t)1));
     CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
     const size_t N = (size_t)c->n1 * c->n2 * c->n3;
@@ -656,12 +660,12 @@ static int tc_nonlocal_project(hpsi_ctx* c, KSlot& s, int nb, const double2* psi
 
 // Expansion half: hpsi += P^T W (+ add32, the local term in complex64)
 static int tc_nonlocal_expand(hpsi_ctx* c, KSlot& s, int nb, double2* hpsi, unsigned char* ws, cudaStream_t st,
-                              bool energy, const float2* add32)
+                              bool energy, const float2* add32, int row0 = 0, int row1 = -1)
 {
     TcNl t = tc_layout(s, nb, ws, energy);
     const int f = s.tc_fmt;
     CUDA_TRY(c, tc_expansion(s.tc_expand[f], s.npw, t.B2, nb, f == 0, hpsi, c->d_err, st, &c->prof, add32,
-                             &s.tcgen[f]));
+                             &s.tcgen[f], row0, row1));
     return HPSI_OK;
 }
 
@@ -883,9 +887,20 @@ static size_t apply_ws_bytes(const hpsi_ctx* c, const KSlot& s, int nb, int prec
 // hpsi += H psi on device pointers with an explicit workspace (prepare_slot first)
 // hpsi_ready: an event after which hpsi holds its input (an H2D copy on
 // another stream); only the tensor-core expansion reads hpsi, so only it waits
+// hpsi_apply with host buffers: hpsi arrives in two G halves [0, mid) and
+// [mid, npw) (events in[0], in[1]); the expansion runs per half, and the first
+// half goes back to host_out on the side stream while the second half is
+// expanded (out: recorded after that copy).
+struct HostHalves {
+    int mid;
+    cudaEvent_t in[2];
+    double* host_out;
+    cudaEvent_t out;
+};
+
 static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, int prec, unsigned char* work,
                      cudaStream_t st, double* epart = nullptr, double* e_nl = nullptr, bool fork = true,
-                     cudaEvent_t hpsi_ready = nullptr)
+                     cudaEvent_t hpsi_ready = nullptr, const HostHalves* halves = nullptr)
 {
     int rc;
     if ((rc = prepare_slot(c, s, prec, false, st))) return rc;
@@ -930,6 +945,21 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         }
         CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
         CUDA_TRY(c, cudaStreamWaitEvent(st, c->ev_join, 0));
+        if (halves) {
+            const size_t pitch = (size_t)s.npw * sizeof(double2);
+            CUDA_TRY(c, cudaStreamWaitEvent(st, halves->in[0], 0));
+            if ((rc = tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32, 0, halves->mid))) {
+                cudaStreamWaitEvent(st, halves->in[1], 0);  // leave no copy unordered behind st
+                return rc;
+            }
+            CUDA_TRY(c, cudaEventRecord(c->ev_half_exp, st));
+            CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_half_exp, 0));
+            CUDA_TRY(c, cudaMemcpy2DAsync(halves->host_out, pitch, hpsi, pitch, (size_t)halves->mid * sizeof(double2),
+                                          nb, cudaMemcpyDeviceToHost, c->side));
+            CUDA_TRY(c, cudaEventRecord(halves->out, c->side));
+            CUDA_TRY(c, cudaStreamWaitEvent(st, halves->in[1], 0));
+            return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32, halves->mid, s.npw);
+        }
         if (hpsi_ready) CUDA_TRY(c, cudaStreamWaitEvent(st, hpsi_ready, 0));
         return tc_nonlocal_expand(c, s, nb, hpsi, wnl, st, e_nl != nullptr, loc32);
     }
@@ -1130,11 +1160,28 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
     double2* hpsi = (double2*)hpsi_;
     const bool fork = !(flags & HPSI_ONE_STREAM);
     cudaEvent_t hpsi_ready = nullptr;
+    // host buffers on the forked tensor-core path: hpsi in two G halves
+    const int mid = (s->npw / 2 + 127) / 128 * 128;
+    const bool halves = !dev && fork && is_tc(prec) && s->P > 0 && mid > 0 && mid < s->npw;
+    HostHalves hh{mid, {c->ev_half_in[0], c->ev_half_in[1]}, hpsi_, c->ev_half_out};
+    const size_t pitch = (size_t)s->npw * sizeof(double2);
     if (!dev) {
         psi = reinterpret_cast<const double2*>(c->ws + o_psi);
         hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
         CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
-        if (fork && is_tc(prec) && s->P > 0) {
+        if (halves) {
+            // only the expansion reads hpsi, one G half per launch: each half's
+            // upload on the copy stream, after the work already queued on st
+            CUDA_TRY(c, cudaEventRecord(c->ev_copy_after, st));
+            CUDA_TRY(c, cudaStreamWaitEvent(c->copy, c->ev_copy_after, 0));
+            CUDA_TRY(c, cudaMemcpy2DAsync(hpsi, pitch, hpsi_, pitch, (size_t)mid * sizeof(double2), nb,
+                                          cudaMemcpyHostToDevice, c->copy));
+            CUDA_TRY(c, cudaEventRecord(c->ev_half_in[0], c->copy));
+            CUDA_TRY(c, cudaMemcpy2DAsync(hpsi + mid, pitch, hpsi_ + 2 * (size_t)mid, pitch,
+                                          (size_t)(s->npw - mid) * sizeof(double2), nb, cudaMemcpyHostToDevice,
+                                          c->copy));
+            CUDA_TRY(c, cudaEventRecord(c->ev_half_in[1], c->copy));
+        } else if (fork && is_tc(prec) && s->P > 0) {
             // hpsi is read only by the expansion at the end: copy it on the copy
             // stream, after the work already queued on st (which may still use
             // the staging area), beside the FFT passes
@@ -1147,12 +1194,25 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
             CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
         }
     }
-    rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st, nullptr, nullptr, fork, hpsi_ready);
+    rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st, nullptr, nullptr, fork, hpsi_ready,
+                   halves ? &hh : nullptr);
     if (rc) {
-        if (hpsi_ready) cudaStreamWaitEvent(st, hpsi_ready, 0);  // leave no copy unordered behind st
+        // leave no copy unordered behind st
+        if (hpsi_ready) cudaStreamWaitEvent(st, hpsi_ready, 0);
+        if (halves) {
+            cudaStreamWaitEvent(st, c->ev_half_in[1], 0);
+            cudaStreamSynchronize(c->side);
+        }
         return rc;
     }
-    if (!dev) CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    if (halves) {
+        // the second half; the first one is on its way on the side stream
+        CUDA_TRY(c, cudaMemcpy2DAsync(hpsi_ + 2 * (size_t)mid, pitch, hpsi + mid, pitch,
+                                      (size_t)(s->npw - mid) * sizeof(double2), nb, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(c, cudaStreamWaitEvent(st, c->ev_half_out, 0));
+    } else if (!dev) {
+        CUDA_TRY(c, cudaMemcpyAsync(hpsi_, hpsi, nel * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    }
     if (!dev || (flags & HPSI_SYNC)) {
         CUDA_TRY(c, cudaStreamSynchronize(st));
         if (is_tc(prec) && (rc = check_device_flag(c))) return rc;

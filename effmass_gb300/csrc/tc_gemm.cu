@@ -639,14 +639,15 @@ template <bool GEN, bool GEN_FP16>
 __global__ void __launch_bounds__(TCP_THREADS, 1)
     tc_expand_kernel(const unsigned char* __restrict__ Ah, const unsigned char* __restrict__ Al,
                      const unsigned char* __restrict__ Bh, const unsigned char* __restrict__ Bl, TcEpilogue ep, int M,
-                     int N, int ktiles, uint32_t idesc, int* err, TcGen gen)
+                     int N, int ktiles, uint32_t idesc, int* err, TcGen gen, int row0)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* tiles = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     TcSmem* sh = reinterpret_cast<TcSmem*>(tiles + STAGES * STAGE_BYTES);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mt = (M + BM - 1) / BM, ntile = mt * (N / BN);
+    // output rows [row0, M) (row0 a multiple of BM)
+    const int mt = (M - row0 + BM - 1) / BM, ntile = mt * (N / BN);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -680,7 +681,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
         int git = 0;  // stage uses issued
         bool stop = false;
         for (int tile = blockIdx.x; tile < ntile && !stop; tile += gridDim.x) {
-            const int mb = tile % mt, nbk = tile / mt;
+            const int mb = row0 / BM + tile % mt, nbk = tile / mt;
             const unsigned char* ah = GEN ? nullptr : Ah + (size_t)mb * KT * A_TILE;
             const unsigned char* al = GEN ? nullptr : Al + (size_t)mb * KT * A_TILE;
             const unsigned char* bh = Bh + (size_t)(2 * nbk) * KT * A_TILE;
@@ -770,7 +771,8 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
                 using GT = typename std::conditional<GEN_FP16, __half, __nv_bfloat16>::type;
                 int git = 0;
                 for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-                    if (!gen_loop_cols<GT>(gen, sh, tiles, (tile % mt) * BM, 0, ktiles, threadIdx.x - 64, err, git))
+                    if (!gen_loop_cols<GT>(gen, sh, tiles, row0 + (tile % mt) * BM, 0, ktiles, threadIdx.x - 64, err,
+                                           git))
                         break;
                     git += ktiles;
                 }
@@ -779,7 +781,7 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
         }
         // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31
         for (int tile = blockIdx.x + lt * gridDim.x; tile < ntile; tile += gridDim.x, ++lt) {
-            const int a = lt & 1, mb = tile % mt, nbk = tile / mt;
+            const int a = lt & 1, mb = row0 / BM + tile % mt, nbk = tile / mt;
             const bool last = lt == last_lt;
             // warps 2-9 join at the last tile only, at any point of the
             // accumulators' phases: they wait on the single-phase barrier
@@ -1280,13 +1282,13 @@ template <bool GEN, bool GEN_FP16>
 static cudaError_t launch_expand_t(int grid, size_t smem, cudaStream_t st, const unsigned char* ah,
                                    const unsigned char* al, const unsigned char* bh, const unsigned char* bl,
                                    const TcEpilogue& ep, int M, int N, int ktiles, uint32_t idesc, int* err,
-                                   const TcGen& gen)
+                                   const TcGen& gen, int row0)
 {
     cudaError_t e = cudaFuncSetAttribute(tc_expand_kernel<GEN, GEN_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e) return e;
     tc_expand_kernel<GEN, GEN_FP16><<<grid, TCP_THREADS, smem, st>>>(ah, al, bh, bl, ep, M, N, ktiles, idesc, err,
-                                                                      gen);
+                                                                      gen, row0);
     return cudaGetLastError();
 }
 
@@ -1294,7 +1296,7 @@ static cudaError_t launch_expand_t(int grid, size_t smem, cudaStream_t st, const
 // partials (nsplit), mode 1: the persistent expansion.  With gen the A
 // operand is generated from those tables (A.hi / A.lo unused).
 static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperand& B, int N, int nsplit, bool fp16,
-                             const TcEpilogue& ep, int* err, cudaStream_t st, const TcGen* gen = nullptr)
+                             const TcEpilogue& ep, int* err, cudaStream_t st, const TcGen* gen = nullptr, int row0 = 0)
 {
     if (A.ldk != B.ldk || A.ldk % BK) return cudaErrorInvalidValue;
     const int ktiles = (int)(A.ldk / BK);
@@ -1305,11 +1307,14 @@ static cudaError_t launch_tc(int mode, const TcOperand& A, int M, const TcOperan
     const TcGen none{};
     const TcGen& g = gen ? *gen : none;
     if (mode == 1) {
-        const int tiles = ceil_div(M, BM) * (N / BN);
+        if (row0 % BM || row0 >= M) return cudaErrorInvalidValue;
+        const int tiles = ceil_div(M - row0, BM) * (N / BN);
         const int grid = std::min(tiles, sm_count());
-        if (!gen) return launch_expand_t<false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g);
-        return fp16 ? launch_expand_t<true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g)
-                    : launch_expand_t<true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g);
+        if (!gen)
+            return launch_expand_t<false, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g, row0);
+        return fp16 ? launch_expand_t<true, true>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g, row0)
+                    : launch_expand_t<true, false>(grid, smem, st, ah, al, bh, bl, ep, M, N, ktiles, idesc, err, g,
+                                                   row0);
     }
     const int per = ceil_div(ktiles, nsplit);
     const int nz = ceil_div(ktiles, per);
@@ -1373,7 +1378,8 @@ cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, 
 }
 
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi,
-                         int* err, cudaStream_t st, Prof* prof, const float2* add32, const TcGen* gen)
+                         int* err, cudaStream_t st, Prof* prof, const float2* add32, const TcGen* gen, int row0,
+                         int row1)
 {
     const int N = tc_band_rows(nb);
     TcEpilogue ep{};
@@ -1384,7 +1390,7 @@ cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb
     ep.sa_scale = A.inv_scale;
     ep.sb_scale = B.inv_scale;
     int h = prof->open(PH_EXPAND, st);
-    cudaError_t e = launch_tc(1, A, npw, B, N, 1, fp16, ep, err, st, gen);
+    cudaError_t e = launch_tc(1, A, row1 < 0 ? npw : row1, B, N, 1, fp16, ep, err, st, gen, row0);
     prof->close(h, st);
     return e;
 }

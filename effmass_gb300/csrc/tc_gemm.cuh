@@ -86,9 +86,11 @@ cudaError_t tc_rows_operand(const double2* x, int rows, int npw, bool fp16, TcOp
 cudaError_t tc_gemm_c128(const TcOperand& A, int M, const TcOperand& B, int nb, int nsplit, bool fp16, float* part,
                          double2* out, int* err, cudaStream_t st);
 // hpsi[b][G] += sum_p W[p][b] Pr[p][G] (+ add32[b][G] when given, summed in FP32 first)
-// (gen as in tc_projection; A.inv_scale = gen->g_inv)
+// (gen as in tc_projection; A.inv_scale = gen->g_inv).  Only the G rows
+// [row0, row1) (row0 a multiple of 128; row1 < 0: npw) when given.
 cudaError_t tc_expansion(const TcOperand& A, int npw, const TcOperand& B, int nb, bool fp16, double2* hpsi, int* err,
-                         cudaStream_t st, Prof* prof, const float2* add32 = nullptr, const TcGen* gen = nullptr);
+                         cudaStream_t st, Prof* prof, const float2* add32 = nullptr, const TcGen* gen = nullptr,
+                         int row0 = 0, int row1 = -1);
 
 // ---- ragged (batched) tensor-core nonlocal term ------------------------------
 // One item per (k-point, band block) of a batch plan, nb <= 128 bands.  Band
