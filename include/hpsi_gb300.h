@@ -342,7 +342,11 @@ const char* hpsi_server_last_error(const hpsi_server* srv);
  * whole sequence is captured in one CUDA graph.  At creation a tuner times the
  * candidate FFT block shapes, GEMM tiles and split-K counts on the plan's own
  * buffers and keeps the fastest (results are cached per shape for the
- * process).  Precisions: HPSI_PREC_FP64 or HPSI_PREC_FP32.  The items' slots
+ * process).  Precisions: HPSI_PREC_FP64, HPSI_PREC_FP32, or HPSI_PREC_TC /
+ * HPSI_PREC_TC_BF16 (the complex64 local term of FP32 and the nonlocal term as
+ * ragged tensor-core GEMMs over the items, in blocks of up to 128 bands; a
+ * bounded wait of those GEMMs that gives up is reported as HPSI_ERR_TIMEOUT by
+ * a synchronising hpsi_batch_apply).  The items' slots
  * must stay bound: rebinding one makes later runs fail with HPSI_ERR_STATE;
  * destroy plans before their contexts.  The reference has no batched call: it
  * applies Callable::operator() per k-point and band
