@@ -610,9 +610,10 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
 // reordering), transforms it r->G and stores the sphere planes back.  No
 // shared memory but the block's plane mask, no barrier inside the line work.
 // Blocks never straddle bands (grid.y = band), so the plane set is uniform.
-// Resident blocks per SM by line length: two for N >= 64 (72: up to 255
-// registers; a 168-register bound, three blocks, spilled and measured slower,
-// 0.142 vs 0.129 ms on the 64-atom cell), three for 36, four for 24.
+// Resident blocks per SM by line length: three for N >= 64 (168 registers:
+// with the packed pair adds of the transforms the 72-point line fits with a
+// 20-byte spill, 0.120 -> 0.116 ms on the 64-atom cell; the energy variant
+// keeps two blocks and 255 registers), three for 36, four for 24.
 //
 // ENERGY: after the G->r transform each thread also sums over its line's N
 // points V|psi(r)|^2 (+ dV |psi(r)|^2, the FP64 part of V the FP32 table
@@ -621,7 +622,9 @@ __global__ void __launch_bounds__(256, xpass_min<C, WIDE, PL>()) x_pass(LocalArg
 // one slot per (band, block):
 // epart[((e_band0 + band) * gridDim.x + blockIdx.x) * 2 + {0, 1}].
 constexpr int XREG_THREADS = 128;
-constexpr int xreg_minb(int n) { return n >= 64 ? 2 : (n >= 36 ? 3 : 4); }
+// resident blocks per SM (the register bound): three for N >= 64 without the
+// energy sums (168 registers), two with them (255), three for 36, four for 24
+constexpr int xreg_minb(int n, bool energy = false) { return n >= 64 ? (energy ? 2 : 3) : (n >= 36 ? 3 : 4); }
 
 // The line work of the register x passes: G->r transform, the V multiply
 // (with the energy sums: four interleaved FP32 partials of V|psi(r)|^2 and
@@ -681,7 +684,7 @@ __device__ __forceinline__ void xline_energy_block(const float (&a1)[4], const f
 }
 
 template <typename PL, bool ENERGY>
-__global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n)) x_pass_reg(LocalArgs a, float2* __restrict__ T,
+__global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n, ENERGY)) x_pass_reg(LocalArgs a, float2* __restrict__ T,
                                                               const float* __restrict__ vloc)
 {
     constexpr int N1 = PL::r0, N2 = PL::r1, N = PL::n, N23 = N * N, W = (N + 31) / 32;
