@@ -113,6 +113,7 @@ struct hpsi_ctx {
     // out in two G halves (uploads on the copy stream, the first half's
     // download on the side stream beside the second half's expansion)
     cudaEvent_t ev_half_in[2] = {nullptr, nullptr}, ev_half_exp = nullptr, ev_half_out = nullptr;
+    cudaEvent_t ev_psi_in[2] = {nullptr, nullptr};  // psi's two band halves on the copy stream
     long gen_counter = 0;         // source of KSlot::gen
     double* d_hess = nullptr;     // Hessian radial tables [nrad][3][hess_nq] (F0, F1, F3), raw
     int hess_nq = 0;

@@ -45,7 +45,8 @@ extern "C" int hpsi_ctx_destroy(hpsi_ctx* c)
     if (c->copy) cudaStreamDestroy(c->copy);
     if (c->ev_copy_after) cudaEventDestroy(c->ev_copy_after);
     if (c->ev_copy_done) cudaEventDestroy(c->ev_copy_done);
-    for (cudaEvent_t e : {c->ev_half_in[0], c->ev_half_in[1], c->ev_half_exp, c->ev_half_out})
+    for (cudaEvent_t e : {c->ev_half_in[0], c->ev_half_in[1], c->ev_half_exp, c->ev_half_out, c->ev_psi_in[0],
+                          c->ev_psi_in[1]})
         if (e) cudaEventDestroy(e);
     for (auto& r : c->prof.recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : c->prof.pool) cudaEventDestroy(e);
@@ -134,7 +135,8 @@ static int ctx_init(hpsi_ctx* c, const hpsi_system* s)
     CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_copy_after, cudaEventDisableTiming));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_copy_done, cudaEventDisableTiming));
-    for (cudaEvent_t* e : {&c->ev_half_in[0], &c->ev_half_in[1], &c->ev_half_exp, &c->ev_half_out})
+    for (cudaEvent_t* e : {&c->ev_half_in[0], &c->ev_half_in[1], &c->ev_half_exp, &c->ev_half_out, &c->ev_psi_in[0],
+                           &c->ev_psi_in[1]})
         CUDA_TRY(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     CUDA_TRY(c, dalloc(&c->d_err, (size_t)1));
     CUDA_TRY(c, cudaMemset(c->d_err, 0, sizeof(int)));
@@ -448,7 +450,8 @@ static int chunk_bands(const KSlot& s, const hpsi_ctx* c, int nb, size_t csize)
 template <typename C, typename V>
 static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, unsigned char* ws,
                        const V* vloc, const C* tw, cudaStream_t st, double* epart = nullptr,
-                       float2* out32 = nullptr, unsigned* rowmax = nullptr, cudaEvent_t after_g2r = nullptr)
+                       float2* out32 = nullptr, unsigned* rowmax = nullptr, cudaEvent_t after_g2r = nullptr,
+                       const cudaEvent_t* psi_in = nullptr, int psi_mid = 0)
 {
     if (nb == 0 || s.npw == 0) return HPSI_OK;
     const int* pl = s.d_plane;
@@ -466,6 +469,11 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
     const int ch = chunk_bands(s, c, nb, sizeof(C));
     C* T = reinterpret_cast<C*>(ws);
+    if (psi_in && ch < nb) {
+        // several band chunks: no split, every launch after all of psi
+        for (int i = 0; i < 2; ++i) CUDA_TRY(c, cudaStreamWaitEvent(st, psi_in[i], 0));
+        psi_in = nullptr;
+    }
     for (int b0 = 0; b0 < nb; b0 += ch) {
         int nbc = std::min(ch, nb - b0);
         a.epart = epart;
@@ -474,6 +482,11 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
         a.rowmax = rowmax ? rowmax + b0 : nullptr;
         a.after_g2r = b0 == 0 ? after_g2r : nullptr;
         a.dv32 = (epart && sizeof(V) == sizeof(float)) ? c->d_dv32 : nullptr;
+        // psi in two band halves (one chunk only; the plans that run the lane-pair G->r pass)
+        const bool split = psi_in && b0 == 0 && nbc == nb;
+        a.psi_in[0] = split ? psi_in[0] : nullptr;
+        a.psi_in[1] = split ? psi_in[1] : nullptr;
+        a.psi_mid = split ? psi_mid : 0;
         CUDA_TRY(c, (launch_local<C, V>(a, nbc, psi + (size_t)b0 * s.npw, hpsi + (size_t)b0 * s.npw, s.d_kin, T, vloc,
                                         tw, tw + c->n1, tw + c->n1 + c->n2, st, &c->prof)));
     }
@@ -896,6 +909,8 @@ struct HostHalves {
     cudaEvent_t in[2];
     double* host_out;
     cudaEvent_t out;
+    cudaEvent_t psi_in[2];  // psi's band halves [0, psi_mid), [psi_mid, nb) (null: psi is on st already)
+    int psi_mid;
 };
 
 static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2* hpsi, int prec, unsigned char* work,
@@ -935,9 +950,11 @@ static int apply_dev(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double2*
         // fork after the G->r pass when it takes the maxima, else right away
         if (!g2r_max) CUDA_TRY(c, cudaEventRecord(c->ev_fork, st));
         rc = local_apply<float2, float>(c, s, nb, psi, hpsi, work, c->d_v32, c->d_tw32, st, epart, loc32, rm,
-                                        g2r_max ? c->ev_fork : nullptr);
+                                        g2r_max ? c->ev_fork : nullptr, halves ? halves->psi_in : nullptr,
+                                        halves ? halves->psi_mid : 0);
         if (rc) return rc;
         CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        if (halves && halves->psi_in[1]) CUDA_TRY(c, cudaStreamWaitEvent(c->side, halves->psi_in[1], 0));
         if ((rc = tc_nonlocal_project(c, s, nb, psi, wnl, c->side, e_nl, g2r_max))) {
             cudaEventRecord(c->ev_join, c->side);  // still join, so that no work is left unordered
             cudaStreamWaitEvent(st, c->ev_join, 0);
@@ -1163,17 +1180,27 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
     // host buffers on the forked tensor-core path: hpsi in two G halves
     const int mid = (s->npw / 2 + 127) / 128 * 128;
     const bool halves = !dev && fork && is_tc(prec) && s->P > 0 && mid > 0 && mid < s->npw;
-    HostHalves hh{mid, {c->ev_half_in[0], c->ev_half_in[1]}, hpsi_, c->ev_half_out};
+    const int pmid = nb / 2;  // psi's band halves
+    HostHalves hh{mid, {c->ev_half_in[0], c->ev_half_in[1]}, hpsi_, c->ev_half_out,
+                  {c->ev_psi_in[0], c->ev_psi_in[1]}, pmid};
     const size_t pitch = (size_t)s->npw * sizeof(double2);
     if (!dev) {
         psi = reinterpret_cast<const double2*>(c->ws + o_psi);
         hpsi = reinterpret_cast<double2*>(c->ws + o_hpsi);
-        CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
         if (halves) {
-            // only the expansion reads hpsi, one G half per launch: each half's
-            // upload on the copy stream, after the work already queued on st
+            // every upload on the copy stream, after the work already queued on
+            // st (which may still use the staging area): psi in two band halves,
+            // each half of the G->r pass waiting for its own; then hpsi in two G
+            // halves, one per expansion launch
             CUDA_TRY(c, cudaEventRecord(c->ev_copy_after, st));
             CUDA_TRY(c, cudaStreamWaitEvent(c->copy, c->ev_copy_after, 0));
+            const size_t pb = (size_t)pmid * s->npw;
+            if (pb)
+                CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, pb * sizeof(double2), cudaMemcpyHostToDevice, c->copy));
+            CUDA_TRY(c, cudaEventRecord(c->ev_psi_in[0], c->copy));
+            CUDA_TRY(c, cudaMemcpyAsync((void*)(psi + pb), psi_ + 2 * pb, (nel - pb) * sizeof(double2),
+                                        cudaMemcpyHostToDevice, c->copy));
+            CUDA_TRY(c, cudaEventRecord(c->ev_psi_in[1], c->copy));
             CUDA_TRY(c, cudaMemcpy2DAsync(hpsi, pitch, hpsi_, pitch, (size_t)mid * sizeof(double2), nb,
                                           cudaMemcpyHostToDevice, c->copy));
             CUDA_TRY(c, cudaEventRecord(c->ev_half_in[0], c->copy));
@@ -1181,17 +1208,20 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
                                           (size_t)(s->npw - mid) * sizeof(double2), nb, cudaMemcpyHostToDevice,
                                           c->copy));
             CUDA_TRY(c, cudaEventRecord(c->ev_half_in[1], c->copy));
-        } else if (fork && is_tc(prec) && s->P > 0) {
-            // hpsi is read only by the expansion at the end: copy it on the copy
-            // stream, after the work already queued on st (which may still use
-            // the staging area), beside the FFT passes
-            CUDA_TRY(c, cudaEventRecord(c->ev_copy_after, st));
-            CUDA_TRY(c, cudaStreamWaitEvent(c->copy, c->ev_copy_after, 0));
-            CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, c->copy));
-            CUDA_TRY(c, cudaEventRecord(c->ev_copy_done, c->copy));
-            hpsi_ready = c->ev_copy_done;
         } else {
-            CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+            CUDA_TRY(c, cudaMemcpyAsync((void*)psi, psi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+            if (fork && is_tc(prec) && s->P > 0) {
+                // hpsi is read only by the expansion at the end: copy it on the
+                // copy stream, after the work already queued on st (which may
+                // still use the staging area), beside the FFT passes
+                CUDA_TRY(c, cudaEventRecord(c->ev_copy_after, st));
+                CUDA_TRY(c, cudaStreamWaitEvent(c->copy, c->ev_copy_after, 0));
+                CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, c->copy));
+                CUDA_TRY(c, cudaEventRecord(c->ev_copy_done, c->copy));
+                hpsi_ready = c->ev_copy_done;
+            } else {
+                CUDA_TRY(c, cudaMemcpyAsync(hpsi, hpsi_, nel * sizeof(double2), cudaMemcpyHostToDevice, st));
+            }
         }
     }
     rc = apply_dev(c, *s, nb, psi, hpsi, prec, c->ws + o_work, st, nullptr, nullptr, fork, hpsi_ready,
@@ -1200,7 +1230,7 @@ extern "C" int hpsi_apply(hpsi_ctx* c, int kid, int nb, const double* psi_, doub
         // leave no copy unordered behind st
         if (hpsi_ready) cudaStreamWaitEvent(st, hpsi_ready, 0);
         if (halves) {
-            cudaStreamWaitEvent(st, c->ev_half_in[1], 0);
+            cudaStreamWaitEvent(st, c->ev_half_in[1], 0);  // the last upload on the copy stream
             cudaStreamSynchronize(c->side);
         }
         return rc;

@@ -81,6 +81,8 @@ struct LocalArgs {
     unsigned* rowmax;       // complex64 G->r: per band, atomicMax of the float bits of
                             // |re|, |im| of psi (zeroed before; null: not taken)
     cudaEvent_t after_g2r;  // host side: recorded on the stream after the G->r launch
+    cudaEvent_t psi_in[2];  // host side (register-transform plans): psi arrives in two band
+    int psi_mid;            // halves [0, psi_mid), [psi_mid, nb); G->r waits per half (null: no split)
     const int* plane_x;     // [nxs] grid x index of plane p
     const int* plane_off;   // [nxs+1] entry range of plane p
     const int* ent_ig;      // [npw] caller-order G index; negative = gather only

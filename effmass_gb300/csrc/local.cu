@@ -992,8 +992,24 @@ static cudaError_t launch_local_t(const LocalArgs& a, int nb, const double2* psi
     const int ptg = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::g2r_threads;
     int h = prof->open(PH_G2R, st);
     if constexpr (xreg_plan<C, PL>()) {
-        g2r_planes_pair<PL><<<gp, pair_block<PL>(), pair_smem<PL>(), st>>>(a, psi, T);
+        if (a.psi_in[0] && a.psi_mid > 0 && a.psi_mid < nb) {
+            // psi in two band halves: each half of the G->r pass as soon as its bands arrived
+            const int m = a.psi_mid;
+            LocalArgs a2 = a;
+            a2.rowmax = a.rowmax ? a.rowmax + m : nullptr;
+            if ((e = cudaStreamWaitEvent(st, a.psi_in[0], 0))) return e;
+            g2r_planes_pair<PL><<<dim3(a.nxs, m), pair_block<PL>(), pair_smem<PL>(), st>>>(a, psi, T);
+            if ((e = cudaStreamWaitEvent(st, a.psi_in[1], 0))) return e;
+            g2r_planes_pair<PL><<<dim3(a.nxs, nb - m), pair_block<PL>(), pair_smem<PL>(), st>>>(
+                a2, psi + (size_t)m * a.npw, T + (size_t)m * a.nxs * a.n2 * a.n3);
+        } else {
+            for (int i = 0; i < 2; ++i)
+                if (a.psi_in[i] && (e = cudaStreamWaitEvent(st, a.psi_in[i], 0))) return e;
+            g2r_planes_pair<PL><<<gp, pair_block<PL>(), pair_smem<PL>(), st>>>(a, psi, T);
+        }
     } else {
+        for (int i = 0; i < 2; ++i)
+            if (a.psi_in[i] && (e = cudaStreamWaitEvent(st, a.psi_in[i], 0))) return e;
         g2r<<<gp, ptg, sp, st>>>(a, psi, T, twy, twz);
     }
     prof->close(h, st);
