@@ -273,7 +273,7 @@ def run_gb300(args, rank, world, local):
                 "max_abs_diff_vs_fp64_Ha": de_api, "value": nb / (ms_e * 1e-3), "unit": "band-apps/s",
                 "ms_per_step": ms_e}
     del h_e
-    # charge density of the same bands (G->r only, FP64 band sums), complex64 transforms
+    # charge density of the same bands (G->r only), complex64 transforms
     occ_d = torch.full((nb,), 2.0, dtype=torch.float64, device="cuda")
     rho_d = torch.zeros((sysm.n1, sysm.n2, sysm.n3), dtype=torch.float64, device="cuda")
     H.density(0, nb, psi_d, occ_d, rho=rho_d, precision="fp32")
@@ -284,7 +284,7 @@ def run_gb300(args, rank, world, local):
     g1.record(stream)
     torch.cuda.synchronize()
     ms_d = g0.elapsed_time(g1) / args.steps
-    density = {"api": "hpsi_density (complex64 G->r, FP64 band sums)", "bands": nb,
+    density = {"api": "hpsi_density (complex64 G->r, compensated FP32 sums per 8 bands, FP64 across them)", "bands": nb,
                "value": nb / (ms_d * 1e-3), "unit": "band-densities/s", "ms_per_step": ms_d}
     del rho_d
 

@@ -493,6 +493,8 @@ static int local_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, double
     return HPSI_OK;
 }
 
+static size_t local_ws(const hpsi_ctx* c, const KSlot& s, int nb, size_t csize);
+
 // rho += sum_b occ_b |psi_b(r)|^2 on device pointers (T chunks in ws)
 template <typename C>
 static int density_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, const double* occ, double* rho,
@@ -514,10 +516,14 @@ static int density_apply(hpsi_ctx* c, KSlot& s, int nb, const double2* psi, cons
     a.Lx = c->L[0]; a.Ly = c->L[1]; a.Lz = c->L[2];
     const int ch = chunk_bands(s, c, nb, sizeof(C));
     C* T = reinterpret_cast<C*>(ws);
+    // the register density pass's group partials, after T
+    double* part = density_part_bytes(a, ch, sizeof(C))
+                       ? reinterpret_cast<double*>(ws + (local_ws(c, s, nb, sizeof(C)) + 255) / 256 * 256)
+                       : nullptr;
     for (int b0 = 0; b0 < nb; b0 += ch) {
         const int nbc = std::min(ch, nb - b0);
         CUDA_TRY(c, launch_density<C>(a, nbc, psi + (size_t)b0 * s.npw, occ + b0, rho, T, tw, tw + c->n1,
-                                      tw + c->n1 + c->n2, st));
+                                      tw + c->n1 + c->n2, st, part));
     }
     return HPSI_OK;
 }
@@ -1774,7 +1780,12 @@ extern "C" int hpsi_density(hpsi_ctx* c, int kid, int nb, const double* psi_, co
     const size_t o_occ = dev ? 0 : cv.take<double>((size_t)nb);
     const size_t o_rho = dev ? 0 : cv.take<double>(N);
     const size_t o_work = cv.off;
-    if ((rc = ws_reserve(c, o_work + local_ws(c, *s, nb, fp64 ? sizeof(double2) : sizeof(float2))))) return rc;
+    const size_t csz = fp64 ? sizeof(double2) : sizeof(float2);
+    LocalArgs la{};
+    la.n1 = c->n1; la.n2 = c->n2; la.n3 = c->n3;
+    la.Lx = c->L[0]; la.Ly = c->L[1]; la.Lz = c->L[2];
+    const size_t part = density_part_bytes(la, chunk_bands(*s, c, nb, csz), csz);
+    if ((rc = ws_reserve(c, o_work + (local_ws(c, *s, nb, csz) + 255) / 256 * 256 + part))) return rc;
     const double2* psi = (const double2*)psi_;
     const double* occ = occ_;
     double* rho = rho_;

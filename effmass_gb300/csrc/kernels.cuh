@@ -118,10 +118,14 @@ void local_xpass_shape(LocalArgs* a, size_t csize);
 template <typename C, typename V>
 cudaError_t launch_local(const LocalArgs& a, int nb, const double2* psi, double2* hpsi, const double* kinetic, C* T,
                          const V* vloc, const C* twx, const C* twy, const C* twz, cudaStream_t st, Prof* prof);
-// rho[i][j][k] += sum_b occ_b |psi_b(r)|^2 over nb bands (FP64 sums; FFT in C)
+// rho[i][j][k] += sum_b occ_b |psi_b(r)|^2 over nb bands (FFT in C; FP64 band
+// sums, or on the complex64 register plans compensated FP32 sums per group of
+// bands added in FP64, with part: density_part_bytes of scratch, else null)
 template <typename C>
 cudaError_t launch_density(const LocalArgs& a, int nb, const double2* psi, const double* occ, double* rho, C* T,
-                           const C* twx, const C* twy, const C* twz, cudaStream_t st);
+                           const C* twx, const C* twy, const C* twz, cudaStream_t st, double* part = nullptr);
+// scratch of the register density x pass for nb bands (0: the plan has none)
+size_t density_part_bytes(const LocalArgs& a, int nb, size_t csize);
 // x-pass line buffer bytes of a given (kt, bb) shape
 size_t local_xpass_smem(const LocalArgs& a, bool fp64);
 // Batched local term over the items of a.items: nbands = all bands of the

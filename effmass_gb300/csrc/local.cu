@@ -743,6 +743,67 @@ __global__ void __launch_bounds__(XREG_THREADS, xreg_minb(PL::n, ENERGY)) x_pass
     }
 }
 
+// Density x pass of the register plans (complex64, N in {24, 36, 64, 72}):
+// one x-line (j, k) per lane pair (lanes l and l ^ 16; a half-warp takes 16
+// consecutive lines, so every load is a 128-byte run), and a group of
+// XD_BANDS bands per thread (blockIdx.y).  Per band the pair loads its line's
+// sphere planes (even lane the even x, odd lane the odd x), transforms it G->r
+// with the lane-pair transform and adds occ_b |psi_b(x)|^2 (the product in
+// FP32) to compensated FP32 sums of its 36 outputs; the group's sums go to
+// part[group][x][jk] in FP64, and density_groups_kernel adds the groups in
+// order into rho: the result does not depend on the launch shape.
+constexpr int XD_BANDS = 8, XD_THREADS = 128;
+
+template <typename PL>
+__global__ void __launch_bounds__(XD_THREADS, PL::n >= 64 ? 2 : 3)
+    x_density_pair(LocalArgs a, int nb, const float2* __restrict__ T, const double* __restrict__ occ,
+                   double* __restrict__ part)
+{
+    constexpr int N = PL::n, N23 = N * N, H1 = fftreg::PairPlan<N>::h1, H2 = fftreg::PairPlan<N>::h2, H = N / 2;
+    __shared__ int poff[N];  // plane index of x (-1: no sphere plane), times N^2
+    const int nxs = a.nxs;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) poff[t] = -1;
+    __syncthreads();
+    for (int t = threadIdx.x; t < nxs; t += blockDim.x) poff[a.plane_x[t]] = t * N23;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int line = ((blockIdx.x * XD_THREADS + threadIdx.x) >> 5) * 16 + (lane & 15);
+    const bool odd = lane >= 16;
+    const bool valid = line < N23;
+    const int b0 = blockIdx.y * XD_BANDS, b1 = min(nb, b0 + XD_BANDS);
+    Sum2f acc[H];
+    for (int b = b0; b < b1; ++b) {
+        const float2* src = T + (size_t)b * nxs * N23 + (valid ? line : 0);
+        float2 v[H];
+#pragma unroll
+        for (int n = 0; n < H; ++n) {
+            const int o = poff[2 * n + (odd ? 1 : 0)];
+            v[n] = (valid && o >= 0) ? __ldcs(src + o) : make_float2(0.f, 0.f);
+        }
+        fftreg::fft_pair<+1, H1, H2>(v, odd);
+        const float w = (float)occ[b];
+#pragma unroll
+        for (int r = 0; r < H; ++r) acc[r].add(w * (v[r].x * v[r].x + v[r].y * v[r].y));
+    }
+    if (!valid) return;
+    double* out = part + (size_t)blockIdx.y * N * N23 + line;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+        const Sum2f& q = acc[fftreg::split_pos<H1, H2>(m)];
+        out[(size_t)(m + (odd ? H : 0)) * N23] = f2d_bits(q.s) + f2d_bits(q.c);
+    }
+}
+
+// rho[x][jk] += sum over band groups g (in order) of part[g][x][jk]
+__global__ void density_groups_kernel(const double* __restrict__ part, int groups, size_t n, double* __restrict__ rho)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int g = 0; g < groups; ++g) s += part[(size_t)g * n + i];
+    rho[i] += s;
+}
+
 // Density x pass: a block owns (j, k0..k0+KT) and loops over all bands of the
 // chunk in groups of BB: G->r along x, then
 //   rho[x][j][k0+kk] += sum_b occ_b |psi_b(x, j, k0+kk)|^2
@@ -1116,7 +1177,8 @@ static size_t density_smem(const LocalArgs& a)
 
 template <typename C, bool WIDE, typename PL>
 static cudaError_t launch_density_t(const LocalArgs& a, int nb, const double2* psi, const double* occ, double* rho,
-                                    C* T, const C* twx, const C* twy, const C* twz, cudaStream_t st)
+                                    C* T, const C* twx, const C* twy, const C* twz, cudaStream_t st,
+                                    double* part)
 {
     const size_t sp = plane_smem<C>(a), sx = density_smem<C>(a);
     cudaError_t e;
@@ -1126,21 +1188,39 @@ static cudaError_t launch_density_t(const LocalArgs& a, int nb, const double2* p
     if ((e = cudaFuncSetAttribute(xd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx))) return e;
     if (a.nxs == 0 || nb == 0) return cudaSuccess;
     const int ptg = a.plane_threads > 0 ? a.plane_threads : Cfg<C>::g2r_threads;
-    if constexpr (xreg_plan<C, PL>())
+    if constexpr (xreg_plan<C, PL>()) {
         g2r_planes_pair<PL><<<dim3(a.nxs, nb), pair_block<PL>(), pair_smem<PL>(), st>>>(a, psi, T);
-    else g2r<<<dim3(a.nxs, nb), ptg, sp, st>>>(a, psi, T, twy, twz);
+        if (part) {
+            constexpr int N23 = PL::n * PL::n;
+            const int groups = ceil_div(nb, XD_BANDS);
+            x_density_pair<PL><<<dim3(ceil_div(ceil_div(N23, 16) * 32, XD_THREADS), groups), XD_THREADS, 0, st>>>(
+                a, nb, reinterpret_cast<const float2*>(T), occ, part);
+            const size_t n = (size_t)PL::n * N23;
+            density_groups_kernel<<<ceil_div((long)n, 256), 256, 0, st>>>(part, groups, n, rho);
+            return cudaGetLastError();
+        }
+    } else {
+        g2r<<<dim3(a.nxs, nb), ptg, sp, st>>>(a, psi, T, twy, twz);
+    }
     xd<<<dim3(ceil_div(a.n3, a.kt), a.n2), 256, sx, st>>>(a, nb, T, occ, rho, twx);
     return cudaGetLastError();
 }
 
 template <typename C>
 cudaError_t launch_density(const LocalArgs& a, int nb, const double2* psi, const double* occ, double* rho, C* T,
-                           const C* twx, const C* twy, const C* twz, cudaStream_t st)
+                           const C* twx, const C* twy, const C* twz, cudaStream_t st, double* part)
 {
     if (a.items || a.epart) return cudaErrorInvalidValue;
     return with_kernels<C>(a, [&](auto wide, auto pl, auto) {
-        return launch_density_t<C, decltype(wide)::value, decltype(pl)>(a, nb, psi, occ, rho, T, twx, twy, twz, st);
+        return launch_density_t<C, decltype(wide)::value, decltype(pl)>(a, nb, psi, occ, rho, T, twx, twy, twz, st,
+                                                                         part);
     });
+}
+
+size_t density_part_bytes(const LocalArgs& a, int nb, size_t csize)
+{
+    if (csize != sizeof(float2) || local_energy_slots(a, csize) != ceil_div(a.n2 * a.n3, XREG_THREADS)) return 0;
+    return (size_t)ceil_div(nb, XD_BANDS) * a.n1 * a.n2 * a.n3 * sizeof(double);
 }
 
 int local_energy_slots(const LocalArgs& a, size_t csize)
@@ -1179,6 +1259,6 @@ template cudaError_t launch_local_batch<double2, double>(const LocalArgs&, int, 
 template cudaError_t launch_local_batch<float2, float>(const LocalArgs&, int, int, int, float2*, const float*,
                                                        const float2*, const float2*, const float2*, cudaStream_t);
 template cudaError_t launch_density<double2>(const LocalArgs&, int, const double2*, const double*, double*, double2*,
-                                             const double2*, const double2*, const double2*, cudaStream_t);
+                                             const double2*, const double2*, const double2*, cudaStream_t, double*);
 template cudaError_t launch_density<float2>(const LocalArgs&, int, const double2*, const double*, double*, float2*,
-                                            const float2*, const float2*, const float2*, cudaStream_t);
+                                            const float2*, const float2*, const float2*, cudaStream_t, double*);
