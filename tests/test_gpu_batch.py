@@ -196,3 +196,21 @@ def test_tensor_core_plan_blocks_of_bands(cells, precision):
         H_.apply(kid, p.shape[0], p, ref, precision)
         assert rel_err(got, ref) <= TOL[precision], (kid, rel_err(got, ref))
         assert np.array_equal(got, got_eager)
+
+
+def test_tensor_core_plan_survives_per_k_format_switch(cells):
+    """A tensor-core plan reads the k-points' generator tables; per-k calls in
+    the other split format build that format's tables beside them (nothing the
+    plan points to is freed), so the plan's next run gives the same result."""
+    from effmass_gb300 import system as S
+    H, kps, _, _ = cells["tinyd"]
+    items = [(H, 2, S.make_bands(kps[2], 5, seed=21)), (H, 3, S.make_bands(kps[3], 3, seed=22))]
+    with _plan(items, "tc", tune=False) as plan:
+        psi = plan.pack([p for _, _, p in items])
+        first = plan.empty()
+        plan.apply(psi, first)
+        for H_, kid, p in items:
+            H_.apply(kid, p.shape[0], p, np.zeros_like(p), "tc_bf16")  # the other format's tables
+        again = plan.empty()
+        plan.apply(psi, again)
+    assert np.array_equal(first, again)
