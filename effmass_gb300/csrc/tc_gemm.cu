@@ -17,12 +17,20 @@
 // TMEM, and the epilogue removes 2^-(s_a + s_b).  FP16 pieces carry 11
 // significand bits each, so hi+lo represents x to ~2^-22; BF16 pieces to ~2^-18.
 //
-// Kernel: one 128 x 256 output tile per CTA (cta_group::1, UMMA M=128, N=256,
-// K=16), 32-deep K stages of A_hi, A_lo, B_hi, B_lo in four pipeline stages,
-// filled by bulk copies of the pre-tiled operands (see tile_off); warp 0
-// issues the copies, warp 1 owns TMEM and issues the MMAs from one thread,
-// warps 2-5 drain TMEM.  Every mbarrier wait is bounded; on timeout the CTA
-// sets an error flag, drains and frees TMEM.
+// Kernels (cta_group::1, UMMA M=128, N=256, K=16; 32-deep K stages of A_hi,
+// A_lo, B_hi, B_lo in four pipeline stages): warp 0 issues the bulk copies of
+// the pre-tiled operands (see tile_off), warp 1 owns TMEM and issues the MMAs
+// from one thread, the other warps drain TMEM.  With generator tables (TcGen)
+// the A pieces are written in shared memory by eight generator warps instead
+// of copied (H|psi> and band energies).
+//   tc_gemm_kernel    one 128 x 256 tile per CTA, split over K (projection,
+//                     complex128 band-pair GEMMs); partials per split
+//   tc_expand_kernel  persistent over the tiles of the expansion, TMEM
+//                     accumulators alternating by tile so that the hpsi
+//                     read-modify-write of one tile overlaps the next's MMAs
+//   rag_*             the batch plans' ragged GEMMs over an item table
+// Every mbarrier wait is bounded; on timeout the CTA sets an error flag,
+// drains its copies and frees TMEM.
 #include <type_traits>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
