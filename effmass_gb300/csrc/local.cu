@@ -207,6 +207,28 @@ struct PlaneRows {
     HPSI_D bool holds(int j) const { return all || j <= jr || j >= n - jr; }
 };
 
+// one scatter batch of the G->r plane pass: SB entries per thread, NT apart,
+// index loads first, then the psi loads (jk = -1 past the plane's end)
+template <int SB, int NT>
+HPSI_D void scatter_load(int eb, int e1, const int* __restrict__ ent_ig, const int* __restrict__ ent_jk,
+                         const double2* __restrict__ ps, bool want_max, int (&ig)[SB], int (&jk)[SB],
+                         double2 (&c)[SB])
+{
+#pragma unroll
+    for (int u = 0; u < SB; ++u) {
+        const int e = eb + u * NT;
+        ig[u] = e < e1 ? ent_ig[e] : -1;
+        jk[u] = e < e1 ? ent_jk[e] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < SB; ++u) {
+        // a G that shares its grid point with a later one (ig < 0) is not
+        // scattered, but its coefficient is still a row element of the band operand
+        const bool need = jk[u] >= 0 && (ig[u] >= 0 || want_max);
+        c[u] = need ? ps[ig[u] & 0x7fffffff] : make_double2(0.0, 0.0);
+    }
+}
+
 template <typename PL>
 __global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
     g2r_planes_pair(LocalArgs a, const double2* __restrict__ psi, float2* __restrict__ T)
@@ -230,36 +252,33 @@ __global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
     }
     const PlaneRows rows(plane_jr ? plane_jr[p] : N, N);
     const int nrows = rows.count();
-    // zero the rows in use (the others are never read)
-    for (int t = threadIdx.x; t < nrows * NP; t += NT) {
-        const int L = t / NP, k = t - L * NP;
-        pl[rows.row(L) * NP + k] = make_float2(0.f, 0.f);
-    }
-    __syncthreads();
     const double2* ps = psi + (size_t)b * npw;
     const int e0 = plane_off[p], e1 = plane_off[p + 1];
     uint32_t mx = 0u;  // float bits of the largest |re|, |im| this thread scattered
     // in batches of SB entries per thread: all index loads, then all psi loads,
     // then the stores, so the two dependent global round trips are paid once
-    // per batch, not once per entry
+    // per batch, not once per entry; the first batch's loads are issued before
+    // the plane buffer is zeroed, which hides the zeroing behind them
     constexpr int SB = 8;
     const bool want_max = a.rowmax && !a.items;
-    for (int eb = e0 + threadIdx.x; eb < e1; eb += SB * NT) {
-        int ig[SB], jk[SB];
-#pragma unroll
-        for (int u = 0; u < SB; ++u) {
-            const int e = eb + u * NT;
-            ig[u] = e < e1 ? ent_ig[e] : -1;
-            jk[u] = e < e1 ? ent_jk[e] : -1;
-        }
-        double2 c[SB];
-#pragma unroll
-        for (int u = 0; u < SB; ++u) {
-            // a G that shares its grid point with a later one (ig < 0) is not
-            // scattered, but its coefficient is still a row element of the band operand
-            const bool need = jk[u] >= 0 && (ig[u] >= 0 || want_max);
-            c[u] = need ? ps[ig[u] & 0x7fffffff] : make_double2(0.0, 0.0);
-        }
+    int eb = e0 + threadIdx.x;
+    int ig[SB], jk[SB];
+    double2 c[SB];
+    scatter_load<SB, NT>(eb, e1, ent_ig, ent_jk, ps, want_max, ig, jk, c);
+    // zero the rows in use (the others are never read): one run of the plane
+    // buffer, or two (rows 0..jr and N-jr..N-1), in 16-byte stores; a run's
+    // ends are rounded outwards to whole float4s, which only touches elements
+    // of rows not in use (N is even, so the buffer is a whole number of float4s)
+    {
+        constexpr int E4 = N * NP / 2;
+        const int a1 = rows.all ? E4 : ((rows.jr + 1) * NP + 1) / 2;
+        const int b0 = rows.all ? E4 : ((N - rows.jr) * NP) / 2;
+        const int cnt = a1 + (E4 - b0);
+        float4* z4 = reinterpret_cast<float4*>(pl);
+        for (int t = threadIdx.x; t < cnt; t += NT) z4[t < a1 ? t : t - a1 + b0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    for (;;) {
 #pragma unroll
         for (int u = 0; u < SB; ++u) {
             if (jk[u] < 0) continue;
@@ -270,6 +289,9 @@ __global__ void __launch_bounds__(pair_threads<PL::n>(), pair_minb<PL::n>())
             }
             mx = max(mx, max(__float_as_uint(v.x) & 0x7fffffffu, __float_as_uint(v.y) & 0x7fffffffu));
         }
+        eb += SB * NT;
+        if (eb >= e1) break;
+        scatter_load<SB, NT>(eb, e1, ent_ig, ent_jk, ps, want_max, ig, jk, c);
     }
     if (a.rowmax && !a.items) {
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
