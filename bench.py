@@ -365,15 +365,22 @@ def run_gb300(args, rank, world, local):
         roof = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                 "frac": ach / bf16, "peak_source": src + " dense bf16 tensor peak"}
     # DRAM bytes (read + write) of one launch of this workload (128 bands per
-    # launch, 64-atom cell, tensor-core path) from ncu --set full captures of
-    # this bench command: x pass 219.2 + 156.7 MB, G->r planes 76.3 + 159.6 MB,
-    # r->G planes 294.2 + 29.1 MB (cold caches: ncu flushes them between passes)
-    ncu_traffic = {"x_pass": 375.91e6, "g2r_planes": 235.86e6, "r2g_planes": 323.32e6}
-    roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec != "fp64") else None
+    # launch, 64-atom cell, split-FP16 tensor-core path) from ncu --set full
+    # captures of this bench command: x pass 219.2 + 156.7 MB, G->r planes
+    # 76.3 + 160.5 MB, r->G planes 294.2 + 29.1 MB, projection GEMM 98.2 +
+    # 13.1 MB, expansion GEMM 138.4 + 25.7 MB (cold caches: ncu flushes them
+    # between passes)
+    ncu_traffic = {"x_pass": 375.91e6, "g2r_planes": 236.75e6, "r2g_planes": 323.32e6, "proj_gemm": 111.3e6,
+                   "expand_gemm": 164.1e6}
+    roof["traffic"] = ncu_traffic.get(dom) if (args.system == "sc64" and args.prec == "tc") else None
     if roof["traffic"] is not None and bound == "hbm":
         roof["algorithmic_bytes_per_launch"] = alg[dom][1] / prof[dom][1]
         roof["traffic_note"] = "ncu dram__bytes_read+write of one launch; below the algorithmic bytes because " \
                                "part of the launch's writes are still in the 129 MB L2 when it ends"
+    elif roof["traffic"] is not None:
+        roof["traffic_note"] = "ncu dram__bytes_read+write of one launch: the band operand and hpsi / the " \
+                               "local term the epilogue reads and writes; the projector tiles are generated " \
+                               "in shared memory and add no DRAM traffic"
     # the tensor-core projection GEMM, reported beside the dominant phase
     roof_gemm = None
     if prof["proj_gemm"][1]:
@@ -426,8 +433,10 @@ def run_gb300(args, rank, world, local):
         "config": {"workload": f"{args.system}: 64-atom SC diamond, 72^3 grid, Ecut 20 Ha, Gamma",
                    "npw": npw, "fft_grid": [sysm.n1, sysm.n2, sysm.n3], "bands_per_step": nb, "projectors": P,
                    "parallelism": "replicas" if world > 1 else "1 GPU",
-                   "l2": "inputs larger than L2 (projector matrix %d MB, psi %d MB)" % (P * npw * csz >> 20,
-                                                                                       psi.nbytes >> 20)},
+                   "l2": "inputs larger than L2 (psi %d MB and hpsi %d MB per step, FFT planes %d MB per pass%s)"
+                         % (psi.nbytes >> 20, psi.nbytes >> 20, (nb * plane) >> 20,
+                            "; projector tiles generated in shared memory" if args.prec.startswith("tc")
+                            else ", projector matrix %d MB" % (P * npw * csz >> 20))},
         "rel_err_vs_fp64": err, "band_energy_max_abs_diff_Ha": de_api,
         "rayleigh_quotient_of_hpsi_max_abs_diff_Ha": de, "band_energies": energies, "density": density,
         "fp64_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
