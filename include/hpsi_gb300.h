@@ -120,8 +120,12 @@ int hpsi_ctx_create(const hpsi_system* sys, hpsi_ctx** out);
 int hpsi_ctx_destroy(hpsi_ctx* ctx);
 
 /* Bind G-sphere data to slot `kid` (0 <= kid < 4096): derives q, theta, phi,
- * Y_lm, beta(q), structure factors and the projector matrices on the device.
- * Rebinding a slot replaces it. */
+ * Y_lm, beta(q) and the structure factors on the device.  The first call at a
+ * precision builds what it needs from them: the projector matrices for
+ * HPSI_PREC_FP64 / HPSI_PREC_FP32; for the tensor-core precisions the
+ * beta*Y_lm rows, structure-factor rows and split scales from which the GEMMs
+ * generate their projector tiles in shared memory.  Rebinding a slot
+ * replaces it. */
 int hpsi_set_kpoint(hpsi_ctx* ctx, int kid, const hpsi_kpoint* kp);
 
 /* Number of plane waves of slot kid (Callable::dim), or a negative status. */
