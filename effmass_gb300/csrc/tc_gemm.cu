@@ -360,6 +360,7 @@ struct GenCols {
     int4 o[3][2];    // offsets (sf, by) of the 4 projectors, two per int4
     float2 b[2][4];  // by of each projector at the two rows
     float4 f[2][4];  // sf of each projector at the two rows
+    bool e[2][3];    // projector i + 1 has projector i's structure-factor row (f not loaded)
     __device__ __forceinline__ void load_offsets(const TcGen& gen, int buf, int p0)
     {
         const int4* src = reinterpret_cast<const int4*>(gen.rows + p0);
@@ -368,14 +369,24 @@ struct GenCols {
     }
     __device__ __forceinline__ void load(const TcGen& gen, int buf, int obuf, int g)
     {
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int4 v = o[obuf][q];
-            b[buf][2 * q] = __ldg(reinterpret_cast<const float2*>(gen.by + v.y + g));
-            f[buf][2 * q] = __ldg(reinterpret_cast<const float4*>(gen.sf + v.x + g));
-            b[buf][2 * q + 1] = __ldg(reinterpret_cast<const float2*>(gen.by + v.w + g));
-            f[buf][2 * q + 1] = __ldg(reinterpret_cast<const float4*>(gen.sf + v.z + g));
-        }
+        const int4 v0 = o[obuf][0], v1 = o[obuf][1];
+        b[buf][0] = __ldg(reinterpret_cast<const float2*>(gen.by + v0.y + g));
+        b[buf][1] = __ldg(reinterpret_cast<const float2*>(gen.by + v0.w + g));
+        b[buf][2] = __ldg(reinterpret_cast<const float2*>(gen.by + v1.y + g));
+        b[buf][3] = __ldg(reinterpret_cast<const float2*>(gen.by + v1.w + g));
+        // consecutive projectors of one atom share its structure-factor row: a
+        // row equal to the previous projector's is not loaded again, and emit
+        // takes it from that projector once the loads have arrived (the
+        // offsets are the same in all lanes of a warp, so is the choice; the
+        // values, and so the tiles, are unchanged)
+        const int s0 = v0.x, s1 = v0.z, s2 = v1.x, s3 = v1.z;
+        e[buf][0] = s1 == s0;
+        e[buf][1] = s2 == s1;
+        e[buf][2] = s3 == s2;
+        f[buf][0] = __ldg(reinterpret_cast<const float4*>(gen.sf + s0 + g));
+        if (!e[buf][0]) f[buf][1] = __ldg(reinterpret_cast<const float4*>(gen.sf + s1 + g));
+        if (!e[buf][1]) f[buf][2] = __ldg(reinterpret_cast<const float4*>(gen.sf + s2 + g));
+        if (!e[buf][2]) f[buf][3] = __ldg(reinterpret_cast<const float4*>(gen.sf + s3 + g));
     }
     __device__ __forceinline__ bool emit(TcSmem* sh, unsigned char* tiles, int it, int buf, float sc0, float sc1,
                                          int r0, int c, int first, int* err)
@@ -385,10 +396,11 @@ struct GenCols {
         uint32_t* lp0 = reinterpret_cast<uint32_t*>(&l0);
         uint32_t* hp1 = reinterpret_cast<uint32_t*>(&h1);
         uint32_t* lp1 = reinterpret_cast<uint32_t*>(&l1);
+        float4 fv = f[buf][0];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const float2 bv = b[buf][i];
-            const float4 fv = f[buf][i];
+            if (i > 0 && !e[buf][i - 1]) fv = f[buf][i];
             const float b0 = bv.x * sc0, b1 = bv.y * sc1;  // power-of-two scales: exact
             split_pair<T>(b0 * fv.x, b0 * fv.y, hp0[i], lp0[i]);
             split_pair<T>(b1 * fv.z, b1 * fv.w, hp1[i], lp1[i]);
